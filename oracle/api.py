@@ -1,0 +1,378 @@
+"""NumPy wrappers over the CPU oracle (``libpdr_oracle.so``) and the reference-built checker
+(``libpdr_ref.so``). TEST INFRASTRUCTURE ONLY: imported by tests, ``smoke()`` and the
+CPU-baseline leg of ``bench.py``; never by the product package.
+
+Array conventions follow the reference's Python bindings (python/bindings.cpp): clip positions
+``[V, 4]`` float32, indices ``[T, 3]`` uint32, raster ``[H, W, 4]``, textures ``[H, W, C]``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_i32p = C.POINTER(C.c_int32)
+
+ERRORS = {-1: ValueError, -2: IndexError, -3: OverflowError}
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(_build.build_oracle())
+        _declare(_lib)
+    return _lib
+
+
+def ref():
+    """The reference's own shaders/padding built for the CPU, or None when unavailable."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None or not os.path.exists(path):
+            return None
+        _ref = C.CDLL(path)
+    return _ref
+
+
+def _declare(L):
+    L.ora_bin_tiles.restype = C.c_int64
+    L.ora_suggest_softmax_scale.restype = C.c_float
+    L.ora_photometric_gradient.restype = C.c_float
+    L.ora_seam_gradient.restype = C.c_float
+    L.ora_tv_gradient.restype = C.c_double
+
+
+def _p(a, t=_f32p):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _check(rc):
+    if rc < 0:
+        raise ERRORS.get(int(rc), RuntimeError)(f"oracle error {rc}")
+    return rc
+
+
+def _vp(viewport, w, h):
+    if viewport is None:
+        return np.array([0.0, 0.0, float(w), float(h)], dtype=np.float32)
+    return np.asarray(viewport, dtype=np.float32)
+
+
+# ---- raster ------------------------------------------------------------------------------
+
+def bin_tiles(pos, idx, resolution, viewport=None):
+    pos, idx = _f(pos), _u(idx)
+    h, w = resolution
+    vp = _vp(viewport, w, h)
+    tiles = ((w + 15) // 16) * ((h + 15) // 16)
+    offsets = np.zeros(tiles + 1, dtype=np.uint32)
+    n = _check(lib().ora_bin_tiles(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp),
+                                   _p(offsets, _u32p), None, C.c_int64(0)))
+    lst = np.zeros(max(n, 1), dtype=np.uint32)
+    lib().ora_bin_tiles(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp),
+                        _p(offsets, _u32p), _p(lst, _u32p), C.c_int64(n))
+    return offsets, lst[:n]
+
+
+def rasterize_forward(pos, idx, resolution, cull_mode=0, output_derivatives=True, viewport=None):
+    pos, idx = _f(pos), _u(idx)
+    h, w = resolution
+    vp = _vp(viewport, w, h)
+    raster = np.zeros((h, w, 4), dtype=np.float32)
+    deriv = np.zeros((h, w, 4), dtype=np.float32) if output_derivatives else None
+    _check(lib().ora_rasterize_forward(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, cull_mode,
+                                       int(bool(output_derivatives)), _p(vp), _p(raster), _p(deriv)))
+    return raster, deriv
+
+
+def rasterize_forward_f64(pos, idx, raster, viewport=None):
+    pos, idx, raster = _f(pos), _u(idx), _f(raster)
+    h, w = raster.shape[:2]
+    vp = _vp(viewport, w, h)
+    r64 = np.zeros((h, w, 4)), np.zeros((h, w, 4))
+    lib().ora_rasterize_forward_f64(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp),
+                                    _p(raster), _p(r64[0], _f64p), _p(r64[1], _f64p))
+    return r64
+
+
+def rasterize_backward(pos, idx, raster, grad_raster, viewport=None, f64=False):
+    pos, idx, raster, grad_raster = _f(pos), _u(idx), _f(raster), _f(grad_raster)
+    h, w = raster.shape[:2]
+    vp = _vp(viewport, w, h)
+    if f64:
+        out = np.zeros((pos.shape[0], 4), dtype=np.float64)
+        fn, t = lib().ora_rasterize_backward_f64, _f64p
+    else:
+        out = np.zeros((pos.shape[0], 4), dtype=np.float32)
+        fn, t = lib().ora_rasterize_backward, _f32p
+    _check(fn(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp), _p(raster), _p(grad_raster),
+              _p(out, t)))
+    return out
+
+
+# ---- interpolation -------------------------------------------------------------------------
+
+def interpolate_forward(attr, idx, raster):
+    attr, idx, raster = _f(attr), _u(idx), _f(raster)
+    h, w = raster.shape[:2]
+    A = attr.shape[1]
+    out = np.zeros((h, w, A), dtype=np.float32)
+    _check(lib().ora_interpolate_forward(_p(attr), attr.shape[0], A, _p(idx, _u32p), idx.shape[0], _p(raster),
+                                         C.c_uint64(h * w), _p(out)))
+    return out
+
+
+def interpolate_backward(attr, idx, raster, grad, f64=False):
+    attr, idx, raster, grad = _f(attr), _u(idx), _f(raster), _f(grad)
+    h, w = raster.shape[:2]
+    V, A = attr.shape
+    dt, t = (np.float64, _f64p) if f64 else (np.float32, _f32p)
+    ga = np.zeros((V, A), dtype=dt)
+    gr = np.zeros((h, w, 4), dtype=dt)
+    fn = lib().ora_interpolate_backward_f64 if f64 else lib().ora_interpolate_backward
+    _check(fn(_p(attr), V, A, _p(idx, _u32p), idx.shape[0], _p(raster), C.c_uint64(h * w), _p(grad), _p(ga, t),
+              _p(gr, t)))
+    return ga, gr
+
+
+# ---- texture -------------------------------------------------------------------------------
+
+ADDRESS = {"clamp": 0, "wrap": 1, "mirror": 2}
+
+
+def texture_forward(tex, uv, raster, address_mode="clamp"):
+    tex, uv, raster = _f(tex), _f(uv), _f(raster)
+    th, tw, Cc = tex.shape
+    h, w = raster.shape[:2]
+    out = np.zeros((h, w, Cc), dtype=np.float32)
+    _check(lib().ora_texture_forward(_p(tex), tw, th, Cc, ADDRESS[address_mode], _p(uv), _p(raster),
+                                     C.c_uint64(h * w), _p(out)))
+    return out
+
+
+def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gradient=True, f64=False):
+    tex, uv, raster, grad = _f(tex), _f(uv), _f(raster), _f(grad)
+    th, tw, Cc = tex.shape
+    h, w = raster.shape[:2]
+    dt, t = (np.float64, _f64p) if f64 else (np.float32, _f32p)
+    gt = np.zeros(tex.shape, dtype=dt)
+    gu = np.zeros((h, w, 2), dtype=dt) if compute_uv_gradient else None
+    fn = lib().ora_texture_backward_f64 if f64 else lib().ora_texture_backward
+    _check(fn(_p(tex), tw, th, Cc, ADDRESS[address_mode], _p(uv), _p(raster), C.c_uint64(h * w), _p(grad),
+              _p(gt, t), _p(gu, t)))
+    return gt, gu
+
+
+# ---- bake / refine ---------------------------------------------------------------------------
+
+class _View(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("channel_count", C.c_uint32),
+        ("image", _f32p), ("visibility_mask", _f32p),
+        ("world_to_clip", C.c_float * 16), ("camera_position", C.c_float * 3),
+        ("has_viewport", C.c_int), ("viewport", C.c_float * 4),
+        ("weight", C.c_float), ("depth_bias", C.c_float), ("min_view_cosine", C.c_float),
+    ]
+
+
+class _RefineOptions(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("steps", C.c_uint32), ("batch_size", C.c_uint32),
+        ("learning_rate", C.c_float), ("minimum_learning_rate", C.c_float), ("photometric_epsilon", C.c_float),
+        ("adam_beta1", C.c_float), ("adam_beta2", C.c_float), ("adam_epsilon", C.c_float),
+        ("clamp_min", C.c_float), ("clamp_max", C.c_float), ("seam_polish_steps", C.c_uint32),
+        ("seam_learning_rate", C.c_float), ("seam_epsilon", C.c_float),
+    ]
+
+
+def _views(images, world_to_clip, camera_positions=None, visibility_masks=None, viewports=None, weights=None,
+           depth_bias=1e-3, min_view_cosine=0.05):
+    keep = []
+    arr = (_View * len(images))()
+    for k, img in enumerate(images):
+        img = _f(img)
+        keep.append(img)
+        v = arr[k]
+        v.height, v.width, v.channel_count = img.shape
+        v.image = _p(img)
+        m = None if visibility_masks is None else visibility_masks[k]
+        if m is not None:
+            m = _f(m)
+            keep.append(m)
+            v.visibility_mask = _p(m)
+        v.world_to_clip[:] = [float(x) for x in np.asarray(world_to_clip[k], dtype=np.float32).reshape(16)]
+        if camera_positions is not None:
+            v.camera_position[:] = [float(x) for x in np.asarray(camera_positions[k], dtype=np.float32)]
+        vp = None if viewports is None else viewports[k]
+        v.has_viewport = int(vp is not None)
+        if vp is not None:
+            v.viewport[:] = [float(x) for x in vp]
+        v.weight = 1.0 if weights is None else float(weights[k])
+        v.depth_bias = depth_bias
+        v.min_view_cosine = min_view_cosine
+    return arr, keep
+
+
+BLEND = {"best_view": 0, "weighted_average": 1, "softmax": 2}
+
+
+def bake(positions, normals, uv, indices, images, world_to_clip, camera_positions, *, visibility_masks=None,
+         viewports=None, resolution=(1024, 1024), blend_mode="weighted_average", pcf_radius=1, softmax_scale=0.0,
+         mask_floor=0.0, weights=None, depth_bias=1e-3, min_view_cosine=0.05):
+    pos, nrm, uvv, idx = _f(positions), _f(normals), _f(uv), _u(indices)
+    h, w = resolution
+    views, keep = _views(images, world_to_clip, camera_positions, visibility_masks, viewports, weights, depth_bias,
+                         min_view_cosine)
+    color = np.zeros((h, w, 4), dtype=np.float32)
+    conf = np.zeros((h, w), dtype=np.float32)
+    src = np.zeros((h, w), dtype=np.uint32)
+    valid = np.zeros((h, w), dtype=np.float32)
+    cov = np.zeros((h, w), dtype=np.float32)
+    faces = np.zeros((h, w), dtype=np.uint32)
+    _check(lib().ora_bake(_p(pos), _p(nrm), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views, len(images),
+                          w, h, BLEND[blend_mode], pcf_radius, C.c_float(mask_floor), C.c_float(softmax_scale),
+                          _p(color), _p(conf), _p(src, _u32p), _p(valid), _p(cov), _p(faces, _u32p)))
+    del keep
+    return color, conf, src, valid, cov, faces
+
+
+def refine_options(width, height, steps=1000, batch_size=4, learning_rate=5e-3, minimum_learning_rate=2.5e-4,
+                   photometric_epsilon=1e-3, adam_beta1=0.9, adam_beta2=0.999, adam_epsilon=1e-8, clamp_min=0.0,
+                   clamp_max=1.0, seam_polish_steps=30, seam_learning_rate=1e-3, seam_epsilon=1e-4):
+    o = _RefineOptions()
+    o.width, o.height, o.steps, o.batch_size = width, height, steps, batch_size
+    o.learning_rate, o.minimum_learning_rate, o.photometric_epsilon = learning_rate, minimum_learning_rate, photometric_epsilon
+    o.adam_beta1, o.adam_beta2, o.adam_epsilon = adam_beta1, adam_beta2, adam_epsilon
+    o.clamp_min, o.clamp_max, o.seam_polish_steps = clamp_min, clamp_max, seam_polish_steps
+    o.seam_learning_rate, o.seam_epsilon = seam_learning_rate, seam_epsilon
+    return o
+
+
+def refine(initial_texture, positions, uv, indices, images, world_to_clip, *, visibility_masks=None, viewports=None,
+           seam_uv_pairs=None, **kw):
+    init = _f(initial_texture)
+    h, w, _ = init.shape
+    o = refine_options(w, h, **kw)
+    pos, uvv, idx = _f(positions), _f(uv), _u(indices)
+    views, keep = _views(images, world_to_clip, None, visibility_masks, viewports)
+    pairs = _f(seam_uv_pairs) if seam_uv_pairs is not None else np.zeros((0, 2, 2), np.float32)
+    npairs = pairs.shape[0]
+    out = np.zeros_like(init)
+    loss = np.zeros(o.steps, dtype=np.float32)
+    seam_steps = 0 if npairs == 0 else o.seam_polish_steps
+    seam = np.zeros(seam_steps, dtype=np.float32)
+    _check(lib().ora_refine(_p(init), _p(pos), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views, len(images),
+                            _p(pairs), npairs, C.byref(o), _p(out), _p(loss), _p(seam)))
+    del keep
+    return out, loss, seam
+
+
+def refine_view_cache(positions, uv, indices, image, world_to_clip, visibility_mask=None, viewport=None):
+    pos, uvv, idx = _f(positions), _f(uv), _u(indices)
+    views, keep = _views([image], [world_to_clip], None, [visibility_mask], [viewport])
+    h, w = image.shape[:2]
+    uv_out = np.zeros((h, w, 2), np.float32)
+    tgt = np.zeros((h, w, 3), np.float32)
+    msk = np.zeros((h, w), np.float32)
+    vw = C.c_double(0.0)
+    _check(lib().ora_refine_view_cache(_p(pos), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views,
+                                       _p(uv_out), _p(tgt), _p(msk), C.byref(vw)))
+    del keep
+    return uv_out, tgt, msk, vw.value
+
+
+def photometric_gradient(tex3, uv, target, mask, eps, normalization, grad=None):
+    tex3, uv, target, mask = _f(tex3), _f(uv), _f(target), _f(mask)
+    th, tw, _ = tex3.shape
+    g = np.zeros_like(tex3) if grad is None else grad
+    P = int(np.prod(mask.shape))
+    loss = lib().ora_photometric_gradient(_p(tex3), tw, th, _p(uv), _p(target), _p(mask), P, C.c_float(eps),
+                                          C.c_float(normalization), _p(g))
+    return g, loss
+
+
+def seam_gradient(tex3, pairs, eps, normalization, grad=None):
+    tex3, pairs = _f(tex3), _f(pairs)
+    th, tw, _ = tex3.shape
+    g = np.zeros_like(tex3) if grad is None else grad
+    loss = lib().ora_seam_gradient(_p(tex3), tw, th, _p(pairs), pairs.shape[0], C.c_float(eps),
+                                   C.c_float(normalization), _p(g))
+    return g, loss
+
+
+def adam_update(tex, grad, m, v, lr, b1, b2, eps, bc1, bc2, cmin, cmax):
+    lib().ora_adam_update(_p(tex), _p(grad), _p(m), _p(v), C.c_uint64(tex.size), C.c_float(lr), C.c_float(b1),
+                          C.c_float(b2), C.c_float(eps), C.c_float(bc1), C.c_float(bc2), C.c_float(cmin),
+                          C.c_float(cmax))
+
+
+def tv_gradient(tex, valid=None, chart=None, eps=1e-4, weight=1.0, grad=None):
+    tex = _f(tex)
+    th, tw, Cc = tex.shape
+    valid = np.ones((th, tw), np.uint8) if valid is None else np.ascontiguousarray(valid, dtype=np.uint8)
+    chart = None if chart is None else np.ascontiguousarray(chart, dtype=np.int32)
+    g = np.zeros_like(tex) if grad is None else grad
+    loss = lib().ora_tv_gradient(_p(tex), tw, th, Cc, _p(valid, _u8p), _p(chart, _i32p), C.c_float(eps),
+                                 C.c_float(weight), _p(g))
+    return g, loss
+
+
+def transform_positions(pos3, m):
+    pos3 = _f(pos3)
+    m = _f(np.asarray(m).reshape(16))
+    out = np.zeros((pos3.shape[0], 4), np.float32)
+    lib().ora_transform_positions(_p(pos3), pos3.shape[0], _p(m), _p(out))
+    return out
+
+
+def suggest_softmax_scale(positions, camera_positions):
+    pos, cams = _f(positions), _f(camera_positions)
+    return float(lib().ora_suggest_softmax_scale(_p(pos), pos.shape[0], _p(cams), cams.shape[0]))
+
+
+class _ProjectParams(C.Structure):
+    _fields_ = [
+        ("world_to_clip", C.c_float * 16), ("camera_position", C.c_float * 3), ("view_weight", C.c_float),
+        ("viewport", C.c_float * 4), ("atlas_width", C.c_uint32), ("atlas_height", C.c_uint32),
+        ("image_width", C.c_uint32), ("image_height", C.c_uint32), ("depth_bias", C.c_float),
+        ("min_view_cosine", C.c_float), ("channel_count", C.c_uint32), ("blend_mode", C.c_uint32),
+        ("pcf_radius", C.c_uint32), ("has_mask", C.c_uint32), ("visibility_mode", C.c_uint32),
+        ("view_index", C.c_uint32),
+    ]
+
+
+def project_texture_view(m16, camera, view_weight, viewport, atlas_wh, image_wh, depth_bias, min_cos, channels,
+                         blend_mode, pcf_radius, has_mask, visibility_mode, view_index, apos, anrm, araster, shadow,
+                         photo, mask, rayvis, acc_color, acc_weight, best_conf, source_view):
+    """One shaders/project_texture.hlsl dispatch; accumulator arrays are updated in place."""
+    pp = _ProjectParams()
+    pp.world_to_clip[:] = [float(x) for x in np.asarray(m16, np.float32).reshape(16)]
+    pp.camera_position[:] = [float(x) for x in camera]
+    pp.view_weight = view_weight
+    pp.viewport[:] = [float(x) for x in viewport]
+    pp.atlas_width, pp.atlas_height = atlas_wh
+    pp.image_width, pp.image_height = image_wh
+    pp.depth_bias, pp.min_view_cosine = depth_bias, min_cos
+    pp.channel_count, pp.blend_mode, pp.pcf_radius = channels, blend_mode, pcf_radius
+    pp.has_mask, pp.visibility_mode, pp.view_index = int(has_mask), visibility_mode, view_index
+    lib().ora_project_texture(C.byref(pp), _p(apos), _p(anrm), _p(araster), _p(shadow), _p(photo), _p(mask),
+                              _p(rayvis), _p(acc_color), _p(acc_weight), _p(best_conf), _p(source_view, _u32p))

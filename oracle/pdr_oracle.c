@@ -1,0 +1,1132 @@
+/*
+ * CPU oracle for the photara_drender raster / texture / bake / refine path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, never linked into it.
+ * Compile with -O2 -ffp-contract=off (no fused multiply-add, no fast-math) so that every
+ * fp32 expression rounds exactly once per operation, in the order the reference's
+ * HLSL source and host C++ write it. Citations are paths inside the reference
+ * (fenghuayumo/photara_drender v0.4.0).
+ *
+ * Conventions chosen where the reference leaves behaviour to the platform:
+ *  - float -> int conversions saturate (NaN -> 0), as CUDA's cvt does.
+ *  - HLSL clamp/min/max follow IEEE maxNum/minNum (fmaxf/fminf): NaN yields the other operand.
+ *  - HLSL round() is round-half-to-even (rintf).
+ *  - HLSL lerp(x, y, s) is x*(1-s) + y*s (the GLSL FMix definition DXC lowers to).
+ *  - HLSL normalize(v) is v / sqrt(dot(v, v)).
+ */
+#include "pdr_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define TILE 16u
+
+/* ---- scalar helpers ------------------------------------------------------------------ */
+
+static int32_t f2i_sat(float f) {
+    if (f != f) return 0;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f < -2147483648.0f) return INT32_MIN;
+    return (int32_t)f;
+}
+
+static int32_t d2i_sat(double f) {
+    if (f != f) return 0;
+    if (f >= 2147483648.0) return INT32_MAX;
+    if (f < -2147483648.0) return INT32_MIN;
+    return (int32_t)f;
+}
+
+static uint32_t f2u_sat(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return UINT32_MAX;
+    return (uint32_t)f;
+}
+
+/* (uint)round(x) as the shaders write it for triangle ids */
+static uint32_t rid(float x) { return f2u_sat(rintf(x)); }
+
+static float clampf_hlsl(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+static int32_t clampi(int32_t x, int32_t lo, int32_t hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+static float cross2(float ax, float ay, float bx, float by) { return ax * by - ay * bx; }
+static double cross2d(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
+
+static float lerpf_hlsl(float x, float y, float s) { return x * (1.0f - s) + y * s; }
+
+/* texture_forward.hlsl:16-35 / rasterizer.cpp:164-179 */
+static int32_t positive_modulo(int32_t value, int32_t divisor) {
+    const int32_t r = value % divisor;
+    return r < 0 ? r + divisor : r;
+}
+
+static int32_t address_coordinate(int32_t c, uint32_t size, uint32_t mode) {
+    if (mode == 0) return clampi(c, 0, (int32_t)size - 1);
+    if (mode == 1) return positive_modulo(c, (int32_t)size);
+    const int32_t period = (int32_t)size * 2;
+    const int32_t m = positive_modulo(c, period);
+    return m < (int32_t)size ? m : period - 1 - m;
+}
+
+/* wrapping int add (HLSL int arithmetic wraps) */
+static int32_t add1(int32_t x) { return (int32_t)((uint32_t)x + 1u); }
+
+static float sample_ndc(uint32_t p, float v0, float vsize) {
+    /* rasterize_forward.hlsl:55-57: ((float(p) - v0 + 0.5) * 2 / vsize) - 1 */
+    return ((float)p - v0 + 0.5f) * 2.0f / vsize - 1.0f;
+}
+
+/* ---- tile binning: src/rasterizer.cpp:61-138 ----------------------------------------- */
+
+int64_t ora_bin_tiles(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                      uint32_t width, uint32_t height, const float vp[4],
+                      uint32_t* offsets, uint32_t* list, int64_t cap) {
+    const uint32_t tcx = (width + TILE - 1) / TILE;
+    const uint32_t tcy = (height + TILE - 1) / TILE;
+    const uint64_t tiles = (uint64_t)tcx * tcy;
+    (void)V;
+    memset(offsets, 0, (tiles + 1) * sizeof(uint32_t));
+    for (int pass = 0; pass < 2; ++pass) {
+        uint32_t* cursor = NULL;
+        if (pass == 1) {
+            if (!list) break;
+            cursor = (uint32_t*)malloc(tiles * sizeof(uint32_t));
+            memcpy(cursor, offsets, tiles * sizeof(uint32_t));
+        }
+        for (uint32_t t = 0; t < T; ++t) {
+            float min_x = INFINITY, min_y = INFINITY, max_x = -INFINITY, max_y = -INFINITY;
+            int valid = 1;
+            for (uint32_t c = 0; c < 3; ++c) {
+                const uint32_t vi = idx[t * 3 + c];
+                const float w = pos[(uint64_t)vi * 4 + 3];
+                if (!(w > 1e-8f) || !isfinite(w)) { valid = 0; break; }
+                const float x = pos[(uint64_t)vi * 4 + 0] / w;
+                const float y = pos[(uint64_t)vi * 4 + 1] / w;
+                if (!isfinite(x) || !isfinite(y)) { valid = 0; break; }
+                /* std::min/std::max on finite values */
+                min_x = x < min_x ? x : min_x;
+                min_y = y < min_y ? y : min_y;
+                max_x = max_x < x ? x : max_x;
+                max_y = max_y < y ? y : max_y;
+            }
+            if (!valid || max_x < -1.0f || min_x > 1.0f || max_y < -1.0f || min_y > 1.0f) continue;
+            const int64_t px0 = f2i_sat(floorf((min_x * 0.5f + 0.5f) * vp[2] + vp[0]));
+            const int64_t px1 = (int64_t)f2i_sat(ceilf((max_x * 0.5f + 0.5f) * vp[2] + vp[0])) - 1;
+            const int64_t py0 = f2i_sat(floorf((min_y * 0.5f + 0.5f) * vp[3] + vp[1]));
+            const int64_t py1 = (int64_t)f2i_sat(ceilf((max_y * 0.5f + 0.5f) * vp[3] + vp[1])) - 1;
+            const uint32_t x0 = (uint32_t)(px0 < 0 ? 0 : (px0 > (int64_t)width - 1 ? (int64_t)width - 1 : px0));
+            const uint32_t x1 = (uint32_t)(px1 < 0 ? 0 : (px1 > (int64_t)width - 1 ? (int64_t)width - 1 : px1));
+            const uint32_t y0 = (uint32_t)(py0 < 0 ? 0 : (py0 > (int64_t)height - 1 ? (int64_t)height - 1 : py0));
+            const uint32_t y1 = (uint32_t)(py1 < 0 ? 0 : (py1 > (int64_t)height - 1 ? (int64_t)height - 1 : py1));
+            for (uint32_t ty = y0 / TILE; ty <= y1 / TILE; ++ty) {
+                for (uint32_t tx = x0 / TILE; tx <= x1 / TILE; ++tx) {
+                    const uint64_t tile = (uint64_t)ty * tcx + tx;
+                    if (pass == 0) {
+                        offsets[tile + 1] += 1;
+                    } else {
+                        const uint32_t slot = cursor[tile]++;
+                        if ((int64_t)slot < cap) list[slot] = t;
+                    }
+                }
+            }
+        }
+        if (pass == 0) {
+            uint64_t acc = 0;
+            for (uint64_t i = 1; i <= tiles; ++i) {
+                acc += offsets[i];
+                if (acc > UINT32_MAX) return ORA_OVERFLOW;
+                offsets[i] = (uint32_t)acc;
+            }
+        } else {
+            free(cursor);
+        }
+    }
+    return (int64_t)offsets[tiles];
+}
+
+/* ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ------------------------ */
+
+static int validate_mesh(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T) {
+    (void)pos;
+    if (V == 0) return ORA_INVALID;
+    if (T == 0) return ORA_INVALID;
+    for (uint64_t i = 0; i < (uint64_t)T * 3; ++i)
+        if (idx[i] >= V) return ORA_RANGE;
+    return ORA_OK;
+}
+
+int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                          uint32_t W, uint32_t H, uint32_t cull_mode, int out_deriv,
+                          const float vp[4], float* raster, float* deriv) {
+    int rc = validate_mesh(pos, V, idx, T);
+    if (rc) return rc;
+    if (W == 0 || H == 0) return ORA_INVALID;
+    if (!isfinite(vp[0]) || !isfinite(vp[1]) || !isfinite(vp[2]) || !isfinite(vp[3]) ||
+        vp[2] <= 0.0f || vp[3] <= 0.0f)
+        return ORA_INVALID;
+    const uint32_t tcx = (W + TILE - 1) / TILE, tcy = (H + TILE - 1) / TILE;
+    uint32_t* offsets = (uint32_t*)malloc(((uint64_t)tcx * tcy + 1) * sizeof(uint32_t));
+    int64_t n = ora_bin_tiles(pos, V, idx, T, W, H, vp, offsets, NULL, 0);
+    if (n < 0) { free(offsets); return (int)n; }
+    uint32_t* list = (uint32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(uint32_t));
+    ora_bin_tiles(pos, V, idx, T, W, H, vp, offsets, list, n);
+
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t py = 0; py < (int64_t)H; ++py) {
+        for (uint32_t px = 0; px < W; ++px) {
+            const uint64_t pixel = (uint64_t)py * W + px;
+            const float sx = sample_ndc(px, vp[0], vp[2]);
+            const float sy = sample_ndc((uint32_t)py, vp[1], vp[3]);
+            float best_depth = 3.402823466e+38f;
+            uint32_t best_tri = 0;
+            float bb0 = 0.0f, bb1 = 0.0f;
+            float bd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            const uint64_t tile = ((uint64_t)py / TILE) * tcx + px / TILE;
+            for (uint32_t e = offsets[tile]; e < offsets[tile + 1]; ++e) {
+                const uint32_t t = list[e];
+                const uint32_t i0 = idx[t * 3 + 0], i1 = idx[t * 3 + 1], i2 = idx[t * 3 + 2];
+                if (i0 >= V || i1 >= V || i2 >= V) continue;
+                const float* p0 = pos + (uint64_t)i0 * 4;
+                const float* p1 = pos + (uint64_t)i1 * 4;
+                const float* p2 = pos + (uint64_t)i2 * 4;
+                if (p0[3] <= 1e-8f || p1[3] <= 1e-8f || p2[3] <= 1e-8f) continue;
+                const float s0x = p0[0] / p0[3], s0y = p0[1] / p0[3];
+                const float s1x = p1[0] / p1[3], s1y = p1[1] / p1[3];
+                const float s2x = p2[0] / p2[3], s2y = p2[1] / p2[3];
+                const float screen_area = cross2(s1x - s0x, s1y - s0y, s2x - s0x, s2y - s0y);
+                if (fabsf(screen_area) <= 1e-12f) continue;
+                if ((cull_mode == 1 && screen_area <= 0.0f) || (cull_mode == 2 && screen_area >= 0.0f)) continue;
+                const float e0 = cross2(s1x - sx, s1y - sy, s2x - sx, s2y - sy);
+                const float e1 = cross2(s2x - sx, s2y - sy, s0x - sx, s0y - sy);
+                const float e2 = cross2(s0x - sx, s0y - sy, s1x - sx, s1y - sy);
+                const float sign = screen_area > 0.0f ? 1.0f : -1.0f;
+                const float ceps = -1e-7f;
+                if (e0 * sign < ceps || e1 * sign < ceps || e2 * sign < ceps) continue;
+                const float q0x = p0[0] - sx * p0[3], q0y = p0[1] - sy * p0[3];
+                const float q1x = p1[0] - sx * p1[3], q1y = p1[1] - sy * p1[3];
+                const float q2x = p2[0] - sx * p2[3], q2y = p2[1] - sy * p2[3];
+                const float a0 = cross2(q1x, q1y, q2x, q2y);
+                const float a1 = cross2(q2x, q2y, q0x, q0y);
+                const float a2 = cross2(q0x, q0y, q1x, q1y);
+                const float ha = a0 + a1 + a2;
+                if (fabsf(ha) <= 1e-12f) continue;
+                const float inv = 1.0f / ha;
+                const float b0 = clampf_hlsl(a0 * inv, 0.0f, 1.0f);
+                const float b1 = clampf_hlsl(a1 * inv, 0.0f, 1.0f);
+                const float iz = p0[2] * a0 + p1[2] * a1 + p2[2] * a2;
+                const float iw = p0[3] * a0 + p1[3] * a1 + p2[3] * a2;
+                if (fabsf(iw) <= 1e-12f) continue;
+                const float depth = clampf_hlsl(iz / iw, -1.0f, 1.0f);
+                if (depth > best_depth || (depth == best_depth && best_tri != 0 && t + 1 >= best_tri)) continue;
+                best_depth = depth;
+                best_tri = t + 1;
+                bb0 = b0;
+                bb1 = b1;
+                if (out_deriv) {
+                    const float da0_dx = -p1[3] * p2[1] + p2[3] * p1[1];
+                    const float da0_dy = -p1[0] * p2[3] + p1[3] * p2[0];
+                    const float da1_dx = -p2[3] * p0[1] + p2[1] * p0[3];
+                    const float da1_dy = -p2[0] * p0[3] + p2[3] * p0[0];
+                    const float da2_dx = -p0[3] * p1[1] + p0[1] * p1[3];
+                    const float da2_dy = -p0[0] * p1[3] + p0[3] * p1[0];
+                    const float dadx = da0_dx + da1_dx + da2_dx;
+                    const float dady = da0_dy + da1_dy + da2_dy;
+                    bd[0] = (da0_dx - b0 * dadx) * inv * 2.0f / vp[2];
+                    bd[2] = (da1_dx - b1 * dadx) * inv * 2.0f / vp[2];
+                    bd[1] = (da0_dy - b0 * dady) * inv * 2.0f / vp[3];
+                    bd[3] = (da1_dy - b1 * dady) * inv * 2.0f / vp[3];
+                }
+            }
+            float* r = raster + pixel * 4;
+            if (best_tri == 0) {
+                r[0] = r[1] = r[2] = r[3] = 0.0f;
+                if (deriv) deriv[pixel * 4 + 0] = deriv[pixel * 4 + 1] = deriv[pixel * 4 + 2] = deriv[pixel * 4 + 3] = 0.0f;
+            } else {
+                r[0] = bb0;
+                r[1] = bb1;
+                r[2] = best_depth;
+                r[3] = (float)best_tri;
+                if (deriv) {
+                    deriv[pixel * 4 + 0] = bd[0];
+                    deriv[pixel * 4 + 1] = bd[1];
+                    deriv[pixel * 4 + 2] = bd[2];
+                    deriv[pixel * 4 + 3] = bd[3];
+                }
+            }
+        }
+    }
+    free(list);
+    free(offsets);
+    return ORA_OK;
+}
+
+/* FP64 twin: same formulas in double for the triangle the fp32 pass selected. */
+int ora_rasterize_forward_f64(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                              uint32_t W, uint32_t H, const float vp[4], const float* raster,
+                              double* r64, double* d64) {
+    (void)V;
+    for (uint64_t pixel = 0; pixel < (uint64_t)W * H; ++pixel) {
+        const uint32_t px = (uint32_t)(pixel % W), py = (uint32_t)(pixel / W);
+        const uint32_t id = rid(raster[pixel * 4 + 3]);
+        double* r = r64 + pixel * 4;
+        double* d = d64 + pixel * 4;
+        r[0] = r[1] = r[2] = r[3] = 0.0;
+        d[0] = d[1] = d[2] = d[3] = 0.0;
+        if (id == 0 || id > T) continue;
+        const uint32_t t = id - 1;
+        const float* p0 = pos + (uint64_t)idx[t * 3 + 0] * 4;
+        const float* p1 = pos + (uint64_t)idx[t * 3 + 1] * 4;
+        const float* p2 = pos + (uint64_t)idx[t * 3 + 2] * 4;
+        const double sx = ((double)px - vp[0] + 0.5) * 2.0 / vp[2] - 1.0;
+        const double sy = ((double)py - vp[1] + 0.5) * 2.0 / vp[3] - 1.0;
+        const double q0x = p0[0] - sx * p0[3], q0y = p0[1] - sy * p0[3];
+        const double q1x = p1[0] - sx * p1[3], q1y = p1[1] - sy * p1[3];
+        const double q2x = p2[0] - sx * p2[3], q2y = p2[1] - sy * p2[3];
+        const double a0 = cross2d(q1x, q1y, q2x, q2y);
+        const double a1 = cross2d(q2x, q2y, q0x, q0y);
+        const double a2 = cross2d(q0x, q0y, q1x, q1y);
+        const double inv = 1.0 / (a0 + a1 + a2);
+        const double b0 = fmin(fmax(a0 * inv, 0.0), 1.0), b1 = fmin(fmax(a1 * inv, 0.0), 1.0);
+        const double iz = (double)p0[2] * a0 + (double)p1[2] * a1 + (double)p2[2] * a2;
+        const double iw = (double)p0[3] * a0 + (double)p1[3] * a1 + (double)p2[3] * a2;
+        r[0] = b0;
+        r[1] = b1;
+        r[2] = fmin(fmax(iz / iw, -1.0), 1.0);
+        r[3] = (double)id;
+        const double da0_dx = -(double)p1[3] * p2[1] + (double)p2[3] * p1[1];
+        const double da0_dy = -(double)p1[0] * p2[3] + (double)p1[3] * p2[0];
+        const double da1_dx = -(double)p2[3] * p0[1] + (double)p2[1] * p0[3];
+        const double da1_dy = -(double)p2[0] * p0[3] + (double)p2[3] * p0[0];
+        const double da2_dx = -(double)p0[3] * p1[1] + (double)p0[1] * p1[3];
+        const double da2_dy = -(double)p0[0] * p1[3] + (double)p0[3] * p1[0];
+        const double dadx = da0_dx + da1_dx + da2_dx, dady = da0_dy + da1_dy + da2_dy;
+        d[0] = (da0_dx - b0 * dadx) * inv * 2.0 / vp[2];
+        d[2] = (da1_dx - b1 * dadx) * inv * 2.0 / vp[2];
+        d[1] = (da0_dy - b0 * dady) * inv * 2.0 / vp[3];
+        d[3] = (da1_dy - b1 * dady) * inv * 2.0 / vp[3];
+    }
+    return ORA_OK;
+}
+
+/* ---- rasterize backward: rasterize_backward.hlsl:36-158, reduce_vertex_gradients.hlsl,
+ *      rasterizer.cpp:145-162 (vertex CSR over corners, ascending corner order) ---------- */
+
+#define RB_BODY(REAL, CROSS, EPS_AREA, SAMPLE)                                                       \
+    for (uint32_t t = 0; t < T; ++t) {                                                               \
+        REAL g[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};                                  \
+        const uint32_t vi[3] = {idx[t * 3 + 0], idx[t * 3 + 1], idx[t * 3 + 2]};                     \
+        if (vi[0] < V && vi[1] < V && vi[2] < V) {                                                   \
+            const float* p[3] = {pos + (uint64_t)vi[0] * 4, pos + (uint64_t)vi[1] * 4,               \
+                                 pos + (uint64_t)vi[2] * 4};                                          \
+            if (!(p[0][3] <= 1e-8f || p[1][3] <= 1e-8f || p[2][3] <= 1e-8f)) {                        \
+                const float s0x = p[0][0] / p[0][3], s0y = p[0][1] / p[0][3];                        \
+                const float s1x = p[1][0] / p[1][3], s1y = p[1][1] / p[1][3];                        \
+                const float s2x = p[2][0] / p[2][3], s2y = p[2][1] / p[2][3];                        \
+                const float mnx = fminf(s0x, fminf(s1x, s2x)), mny = fminf(s0y, fminf(s1y, s2y));    \
+                const float mxx = fmaxf(s0x, fmaxf(s1x, s2x)), mxy = fmaxf(s0y, fmaxf(s1y, s2y));    \
+                const int32_t x0 = clampi(f2i_sat(floorf((mnx * 0.5f + 0.5f) * vp[2] + vp[0])), 0, (int32_t)W); \
+                const int32_t x1 = clampi(f2i_sat(ceilf((mxx * 0.5f + 0.5f) * vp[2] + vp[0])), 0, (int32_t)W);  \
+                const int32_t y0 = clampi(f2i_sat(floorf((mny * 0.5f + 0.5f) * vp[3] + vp[1])), 0, (int32_t)H); \
+                const int32_t y1 = clampi(f2i_sat(ceilf((mxy * 0.5f + 0.5f) * vp[3] + vp[1])), 0, (int32_t)H);  \
+                for (int32_t y = y0; y < y1; ++y) {                                                  \
+                    for (int32_t x = x0; x < x1; ++x) {                                              \
+                        const uint64_t pix = (uint64_t)y * W + (uint64_t)x;                          \
+                        if (rid(raster[pix * 4 + 3]) != t + 1) continue;                             \
+                        const float lgx = grad_raster[pix * 4 + 0], lgy = grad_raster[pix * 4 + 1];  \
+                        if (lgx == 0.0f && lgy == 0.0f) continue;                                    \
+                        REAL sx, sy;                                                                 \
+                        SAMPLE;                                                                      \
+                        const REAL q0x = p[0][0] - sx * p[0][3], q0y = p[0][1] - sy * p[0][3];       \
+                        const REAL q1x = p[1][0] - sx * p[1][3], q1y = p[1][1] - sy * p[1][3];       \
+                        const REAL q2x = p[2][0] - sx * p[2][3], q2y = p[2][1] - sy * p[2][3];       \
+                        const REAL area = CROSS(q1x, q1y, q2x, q2y) + CROSS(q2x, q2y, q0x, q0y) +    \
+                                          CROSS(q0x, q0y, q1x, q1y);                                 \
+                        if (fabs((double)area) <= (double)1e-12f) continue;                          \
+                        const REAL eps = area >= 0 ? (REAL)EPS_AREA : -(REAL)EPS_AREA;               \
+                        const REAL inv = (REAL)1 / (area + eps);                                     \
+                        const REAL a0 = CROSS(q1x, q1y, q2x, q2y);                                   \
+                        const REAL a1 = CROSS(q2x, q2y, q0x, q0y);                                   \
+                        const REAL b0 = a0 * inv, b1 = a1 * inv;                                     \
+                        const REAL gb0 = lgx * inv, gb1 = lgy * inv;                                 \
+                        const REAL gc = gb0 * b0 + gb1 * b1;                                         \
+                        const REAL g0x = gc * (q2y - q1y) - gb1 * q2y;                               \
+                        const REAL g1x = gc * (q0y - q2y) + gb0 * q2y;                               \
+                        const REAL g2x = gc * (q1y - q0y) - gb0 * q1y + gb1 * q0y;                   \
+                        const REAL g0y = gc * (q1x - q2x) + gb1 * q2x;                               \
+                        const REAL g1y = gc * (q2x - q0x) - gb0 * q2x;                               \
+                        const REAL g2y = gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x;                   \
+                        g[0][0] += g0x; g[0][1] += g0y; g[0][2] += (REAL)0; g[0][3] += -sx * g0x - sy * g0y; \
+                        g[1][0] += g1x; g[1][1] += g1y; g[1][2] += (REAL)0; g[1][3] += -sx * g1x - sy * g1y; \
+                        g[2][0] += g2x; g[2][1] += g2y; g[2][2] += (REAL)0; g[2][3] += -sx * g2x - sy * g2y; \
+                    }                                                                                \
+                }                                                                                    \
+            }                                                                                        \
+        }                                                                                            \
+        for (int k = 0; k < 3; ++k)                                                                  \
+            for (int c = 0; c < 4; ++c) corner[((uint64_t)t * 3 + k) * 4 + c] = g[k][c];             \
+    }
+
+static void vertex_csr(const uint32_t* idx, uint32_t T, uint32_t V, uint32_t** off_out, uint32_t** corners_out) {
+    uint32_t* off = (uint32_t*)calloc((size_t)V + 1, sizeof(uint32_t));
+    for (uint64_t c = 0; c < (uint64_t)T * 3; ++c) off[idx[c] + 1]++;
+    for (uint32_t v = 1; v <= V; ++v) off[v] += off[v - 1];
+    uint32_t* cur = (uint32_t*)malloc(((size_t)V + 1) * sizeof(uint32_t));
+    memcpy(cur, off, ((size_t)V + 1) * sizeof(uint32_t));
+    uint32_t* corners = (uint32_t*)malloc((size_t)T * 3 * sizeof(uint32_t));
+    for (uint32_t c = 0; c < T * 3; ++c) corners[cur[idx[c]]++] = c;
+    free(cur);
+    *off_out = off;
+    *corners_out = corners;
+}
+
+int ora_rasterize_backward(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                           uint32_t W, uint32_t H, const float vp[4], const float* raster,
+                           const float* grad_raster, float* grad_pos) {
+    int rc = validate_mesh(pos, V, idx, T);
+    if (rc) return rc;
+    float* corner = (float*)malloc((size_t)T * 12 * sizeof(float));
+#define SAMPLE_F sx = sample_ndc((uint32_t)x, vp[0], vp[2]); sy = sample_ndc((uint32_t)y, vp[1], vp[3])
+    RB_BODY(float, cross2, 1e-6f, SAMPLE_F)
+    uint32_t *off, *corners;
+    vertex_csr(idx, T, V, &off, &corners);
+    for (uint32_t v = 0; v < V; ++v) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (uint32_t a = off[v]; a < off[v + 1]; ++a)
+            for (int c = 0; c < 4; ++c) acc[c] += corner[(uint64_t)corners[a] * 4 + c];
+        for (int c = 0; c < 4; ++c) grad_pos[(uint64_t)v * 4 + c] = acc[c];
+    }
+    free(off);
+    free(corners);
+    free(corner);
+    return ORA_OK;
+}
+
+int ora_rasterize_backward_f64(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                               uint32_t W, uint32_t H, const float vp[4], const float* raster,
+                               const float* grad_raster, double* grad_pos) {
+    int rc = validate_mesh(pos, V, idx, T);
+    if (rc) return rc;
+    double* corner = (double*)malloc((size_t)T * 12 * sizeof(double));
+#define SAMPLE_D sx = ((double)x - vp[0] + 0.5) * 2.0 / vp[2] - 1.0; sy = ((double)y - vp[1] + 0.5) * 2.0 / vp[3] - 1.0
+    RB_BODY(double, cross2d, 1e-6f, SAMPLE_D)
+    uint32_t *off, *corners;
+    vertex_csr(idx, T, V, &off, &corners);
+    for (uint32_t v = 0; v < V; ++v) {
+        double acc[4] = {0, 0, 0, 0};
+        for (uint32_t a = off[v]; a < off[v + 1]; ++a)
+            for (int c = 0; c < 4; ++c) acc[c] += corner[(uint64_t)corners[a] * 4 + c];
+        for (int c = 0; c < 4; ++c) grad_pos[(uint64_t)v * 4 + c] = acc[c];
+    }
+    free(off);
+    free(corners);
+    free(corner);
+    return ORA_OK;
+}
+
+/* ---- interpolation: interpolate_forward.hlsl:15-54 ---------------------------------- */
+
+int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
+                            uint32_t T, const float* raster, uint64_t P, float* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < (int64_t)P; ++p) {
+        const uint32_t id = rid(raster[p * 4 + 3]);
+        int ok = id != 0 && id <= T;
+        uint32_t i0 = 0, i1 = 0, i2 = 0;
+        if (ok) {
+            i0 = idx[(id - 1) * 3 + 0];
+            i1 = idx[(id - 1) * 3 + 1];
+            i2 = idx[(id - 1) * 3 + 2];
+            ok = i0 < V && i1 < V && i2 < V;
+        }
+        for (uint32_t a = 0; a < A; ++a) {
+            if (!ok) { out[p * A + a] = 0.0f; continue; }
+            const float u = raster[p * 4 + 0], v = raster[p * 4 + 1];
+            const float w = 1.0f - u - v;
+            const float a0 = attr[(uint64_t)i0 * A + a], a1 = attr[(uint64_t)i1 * A + a], a2 = attr[(uint64_t)i2 * A + a];
+            out[p * A + a] = u * a0 + v * a1 + w * a2;
+        }
+    }
+    return ORA_OK;
+}
+
+/* interpolate_grad_attributes.hlsl:15-58 sums, per (vertex, attribute), weight * grad over all
+ * pixels in ascending order; adding zero-weight terms leaves a finite sum unchanged, so the
+ * per-pixel scatter below accumulates every vertex in the same order. interpolate_grad_raster.hlsl
+ * gives the raster gradient. */
+#define IB_BODY(REAL)                                                                                \
+    memset(grad_attr, 0, (size_t)V * A * sizeof(REAL));                                              \
+    for (uint64_t p = 0; p < P; ++p) {                                                               \
+        const uint32_t id = rid(raster[p * 4 + 3]);                                                  \
+        REAL* gr = grad_raster + p * 4;                                                              \
+        gr[0] = gr[1] = gr[2] = gr[3] = 0;                                                           \
+        if (id == 0 || id > T) continue;                                                             \
+        const uint32_t i0 = idx[(id - 1) * 3 + 0], i1 = idx[(id - 1) * 3 + 1], i2 = idx[(id - 1) * 3 + 2]; \
+        const float u = raster[p * 4 + 0], v = raster[p * 4 + 1];                                    \
+        const uint32_t vs[3] = {i0, i1, i2};                                                         \
+        for (int k = 0; k < 3; ++k) {                                                                \
+            const uint32_t vx = vs[k];                                                               \
+            int first = 1;                                                                           \
+            for (int j = 0; j < k; ++j) if (vs[j] == vx) first = 0;                                  \
+            if (!first) continue;                                                                    \
+            REAL wgt = 0;                                                                            \
+            if (i0 == vx) wgt += (REAL)u;                                                            \
+            if (i1 == vx) wgt += (REAL)v;                                                            \
+            if (i2 == vx) wgt += (REAL)1 - (REAL)u - (REAL)v;                                        \
+            for (uint32_t a = 0; a < A; ++a) grad_attr[(uint64_t)vx * A + a] += wgt * (REAL)grad_out[p * A + a]; \
+        }                                                                                            \
+        if (i0 < V && i1 < V && i2 < V) {                                                            \
+            REAL gx = 0, gy = 0;                                                                     \
+            for (uint32_t a = 0; a < A; ++a) {                                                       \
+                const REAL a0 = attr[(uint64_t)i0 * A + a], a1 = attr[(uint64_t)i1 * A + a];        \
+                const REAL a2 = attr[(uint64_t)i2 * A + a];                                          \
+                const REAL g = grad_out[p * A + a];                                                  \
+                gx += g * (a0 - a2);                                                                 \
+                gy += g * (a1 - a2);                                                                 \
+            }                                                                                        \
+            gr[0] = gx;                                                                              \
+            gr[1] = gy;                                                                              \
+        }                                                                                            \
+    }
+
+int ora_interpolate_backward(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
+                             uint32_t T, const float* raster, uint64_t P, const float* grad_out,
+                             float* grad_attr, float* grad_raster) {
+    IB_BODY(float)
+    return ORA_OK;
+}
+
+int ora_interpolate_backward_f64(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
+                                 uint32_t T, const float* raster, uint64_t P, const float* grad_out,
+                                 double* grad_attr, double* grad_raster) {
+    IB_BODY(double)
+    return ORA_OK;
+}
+
+/* ---- texture: texture_forward.hlsl:37-79 --------------------------------------------- */
+
+int ora_texture_forward(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
+                        const float* uv, const float* raster, uint64_t P, float* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < (int64_t)P; ++p) {
+        if (rid(raster[p * 4 + 3]) == 0) {
+            for (uint32_t c = 0; c < C; ++c) out[p * C + c] = 0.0f;
+            continue;
+        }
+        const float tx = uv[p * 2 + 0] * (float)tw - 0.5f;
+        const float ty = uv[p * 2 + 1] * (float)th - 0.5f;
+        const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+        const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+        const int32_t x0 = address_coordinate(bx, tw, mode), x1 = address_coordinate(add1(bx), tw, mode);
+        const int32_t y0 = address_coordinate(by, th, mode), y1 = address_coordinate(add1(by), th, mode);
+        const float w0 = (1.0f - fx) * (1.0f - fy), w1 = fx * (1.0f - fy);
+        const float w2 = (1.0f - fx) * fy, w3 = fx * fy;
+        for (uint32_t c = 0; c < C; ++c) {
+            const float t0 = tex[((uint64_t)(uint32_t)y0 * tw + (uint32_t)x0) * C + c];
+            const float t1 = tex[((uint64_t)(uint32_t)y0 * tw + (uint32_t)x1) * C + c];
+            const float t2 = tex[((uint64_t)(uint32_t)y1 * tw + (uint32_t)x0) * C + c];
+            const float t3 = tex[((uint64_t)(uint32_t)y1 * tw + (uint32_t)x1) * C + c];
+            out[p * C + c] = t0 * w0 + t1 * w1 + t2 * w2 + t3 * w3;
+        }
+    }
+    return ORA_OK;
+}
+
+/* rasterizer.cpp:187-258: the texel->sample table uses double texel positions and float
+ * weights; texture_grad_texture.hlsl:15-38 sums each texel's entries in ascending order,
+ * which the ascending-entry scatter below reproduces. texture_grad_uv.hlsl:38-80 for uv. */
+#define TB_BODY(REAL)                                                                                \
+    const uint64_t texels = (uint64_t)tw * th;                                                       \
+    memset(grad_tex, 0, texels * C * sizeof(REAL));                                                  \
+    for (uint64_t p = 0; p < P; ++p) {                                                               \
+        if (raster[p * 4 + 3] == 0.0f) continue;                                                     \
+        const float u = uv[p * 2 + 0], v = uv[p * 2 + 1];                                            \
+        if (!isfinite(u) || !isfinite(v)) return ORA_INVALID;                                        \
+        const double tx = (double)u * tw - 0.5, ty = (double)v * th - 0.5;                           \
+        if (fabs(tx) > 1.0e9 || fabs(ty) > 1.0e9) return ORA_RANGE;                                  \
+        const int32_t bx = d2i_sat(floor(tx)), by = d2i_sat(floor(ty));                              \
+        const REAL fx = (REAL)(tx - floor(tx)), fy = (REAL)(ty - floor(ty));                         \
+        const int32_t xs[2] = {address_coordinate(bx, tw, mode), address_coordinate(bx + 1, tw, mode)}; \
+        const int32_t ys[2] = {address_coordinate(by, th, mode), address_coordinate(by + 1, th, mode)}; \
+        const REAL w[4] = {((REAL)1 - fx) * ((REAL)1 - fy), fx * ((REAL)1 - fy), ((REAL)1 - fx) * fy, fx * fy}; \
+        const uint64_t tx4[4] = {(uint64_t)ys[0] * tw + xs[0], (uint64_t)ys[0] * tw + xs[1],        \
+                                 (uint64_t)ys[1] * tw + xs[0], (uint64_t)ys[1] * tw + xs[1]};        \
+        for (int k = 0; k < 4; ++k)                                                                  \
+            for (uint32_t c = 0; c < C; ++c) grad_tex[tx4[k] * C + c] += w[k] * (REAL)grad[p * C + c]; \
+    }                                                                                                \
+    if (grad_uv) {                                                                                   \
+        for (uint64_t p = 0; p < P; ++p) {                                                           \
+            if (rid(raster[p * 4 + 3]) == 0) { grad_uv[p * 2] = grad_uv[p * 2 + 1] = 0; continue; } \
+            REAL tx, ty, fx, fy; int32_t bx, by;                                                     \
+            UVPOS;                                                                                   \
+            const int32_t x0 = address_coordinate(bx, tw, mode), x1 = address_coordinate(add1(bx), tw, mode); \
+            const int32_t y0 = address_coordinate(by, th, mode), y1 = address_coordinate(add1(by), th, mode); \
+            REAL gx = 0, gy = 0;                                                                     \
+            for (uint32_t c = 0; c < C; ++c) {                                                       \
+                const REAL c00 = tex[((uint64_t)(uint32_t)y0 * tw + (uint32_t)x0) * C + c];          \
+                const REAL c10 = tex[((uint64_t)(uint32_t)y0 * tw + (uint32_t)x1) * C + c];          \
+                const REAL c01 = tex[((uint64_t)(uint32_t)y1 * tw + (uint32_t)x0) * C + c];          \
+                const REAL c11 = tex[((uint64_t)(uint32_t)y1 * tw + (uint32_t)x1) * C + c];          \
+                const REAL g = grad[p * C + c];                                                      \
+                const REAL dx = ((REAL)1 - fy) * (c10 - c00) + fy * (c11 - c01);                     \
+                const REAL dy = ((REAL)1 - fx) * (c01 - c00) + fx * (c11 - c10);                     \
+                gx += g * (dx * (REAL)tw);                                                           \
+                gy += g * (dy * (REAL)th);                                                           \
+            }                                                                                        \
+            grad_uv[p * 2] = gx;                                                                     \
+            grad_uv[p * 2 + 1] = gy;                                                                 \
+        }                                                                                            \
+    }
+
+static int texture_validate(uint32_t tw, uint32_t th, uint32_t C) {
+    if (tw == 0 || th == 0 || C == 0) return ORA_INVALID;
+    if (tw > 1073741823u || th > 1073741823u) return ORA_RANGE;
+    return ORA_OK;
+}
+
+int ora_texture_backward(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
+                         const float* uv, const float* raster, uint64_t P, const float* grad,
+                         float* grad_tex, float* grad_uv) {
+    int rc = texture_validate(tw, th, C);
+    if (rc) return rc;
+#define UVPOS tx = uv[p * 2] * (float)tw - 0.5f; ty = uv[p * 2 + 1] * (float)th - 0.5f; \
+    bx = f2i_sat(floorf(tx)); by = f2i_sat(floorf(ty)); fx = tx - floorf(tx); fy = ty - floorf(ty)
+    TB_BODY(float)
+#undef UVPOS
+    return ORA_OK;
+}
+
+int ora_texture_backward_f64(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
+                             const float* uv, const float* raster, uint64_t P, const float* grad,
+                             double* grad_tex, double* grad_uv) {
+    int rc = texture_validate(tw, th, C);
+    if (rc) return rc;
+#define UVPOS tx = (double)uv[p * 2] * tw - 0.5; ty = (double)uv[p * 2 + 1] * th - 0.5; \
+    bx = d2i_sat(floor(tx)); by = d2i_sat(floor(ty)); fx = tx - floor(tx); fy = ty - floor(ty)
+    TB_BODY(double)
+#undef UVPOS
+    return ORA_OK;
+}
+
+/* ---- transforms and softmax scale ---------------------------------------------------- */
+
+void ora_transform_positions(const float* pos3, uint32_t V, const float m[16], float* clip4) {
+    for (uint64_t v = 0; v < V; ++v) {
+        const float x = pos3[v * 3], y = pos3[v * 3 + 1], z = pos3[v * 3 + 2];
+        for (int r = 0; r < 4; ++r)
+            clip4[v * 4 + r] = m[r * 4] * x + m[r * 4 + 1] * y + m[r * 4 + 2] * z + m[r * 4 + 3];
+    }
+}
+
+float ora_suggest_softmax_scale(const float* pos, uint32_t V, const float* cams, uint32_t ncam) {
+    if (V == 0 || ncam == 0) return 0.0f;
+    const uint64_t stride = V / 10000 > 1 ? V / 10000 : 1;
+    double best = INFINITY;
+    for (uint64_t v = 0; v < V; v += stride) {
+        const double x = pos[v * 3], y = pos[v * 3 + 1], z = pos[v * 3 + 2];
+        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) continue;
+        for (uint32_t c = 0; c < ncam; ++c) {
+            const double dx = cams[c * 3] - x, dy = cams[c * 3 + 1] - y, dz = cams[c * 3 + 2] - z;
+            const double sq = dx * dx + dy * dy + dz * dz;
+            best = sq < best ? sq : best;
+        }
+    }
+    if (!isfinite(best) || best <= 0.0) return 0.0f;
+    return (float)(20.0 * best);
+}
+
+/* ---- projection: shaders/project_texture.hlsl:26-247 --------------------------------- */
+
+static float load_channel(const ora_project_params* pp, const float* photo, int32_t cx, int32_t cy, uint32_t ch) {
+    const int32_t w = (int32_t)pp->image_width, h = (int32_t)pp->image_height;
+    cx = clampi(cx, 0, w - 1);
+    cy = clampi(cy, 0, h - 1);
+    return photo[((uint64_t)(uint32_t)cy * pp->image_width + (uint32_t)cx) * pp->channel_count + ch];
+}
+
+static float sample_photo(const ora_project_params* pp, const float* photo, float ppx, float ppy, uint32_t ch) {
+    const float tx = ppx - 0.5f, ty = ppy - 0.5f;
+    const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+    const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+    const float v00 = load_channel(pp, photo, bx, by, ch);
+    const float v10 = load_channel(pp, photo, add1(bx), by, ch);
+    const float v01 = load_channel(pp, photo, bx, add1(by), ch);
+    const float v11 = load_channel(pp, photo, add1(bx), add1(by), ch);
+    return lerpf_hlsl(lerpf_hlsl(v00, v10, fx), lerpf_hlsl(v01, v11, fx), fy);
+}
+
+static float sample_mask(const ora_project_params* pp, const float* mask, float ppx, float ppy) {
+    const int32_t w = (int32_t)pp->image_width, h = (int32_t)pp->image_height;
+    const float tx = ppx - 0.5f, ty = ppy - 0.5f;
+    const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+    const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+    const int32_t x0 = clampi(bx, 0, w - 1), x1 = clampi(add1(bx), 0, w - 1);
+    const int32_t y0 = clampi(by, 0, h - 1), y1 = clampi(add1(by), 0, h - 1);
+    const float v00 = mask[(uint64_t)y0 * pp->image_width + x0];
+    const float v10 = mask[(uint64_t)y0 * pp->image_width + x1];
+    const float v01 = mask[(uint64_t)y1 * pp->image_width + x0];
+    const float v11 = mask[(uint64_t)y1 * pp->image_width + x1];
+    return lerpf_hlsl(lerpf_hlsl(v00, v10, fx), lerpf_hlsl(v01, v11, fx), fy);
+}
+
+static float shadow_visibility(const ora_project_params* pp, const float* shadow, float ppx, float ppy,
+                               float depth) {
+    const int32_t w = (int32_t)pp->image_width, h = (int32_t)pp->image_height;
+    const int32_t cx = f2i_sat(floorf(ppx)), cy = f2i_sat(floorf(ppy));
+    const int32_t r = (int32_t)pp->pcf_radius;
+    float visible = 0.0f, count = 0.0f;
+    for (int32_t y = -r; y <= r; ++y) {
+        for (int32_t x = -r; x <= r; ++x) {
+            const int32_t X = cx + x, Y = cy + y;
+            if (X < 0 || Y < 0 || X >= w || Y >= h) continue;
+            const uint64_t off = ((uint64_t)Y * pp->image_width + (uint64_t)X) * 4;
+            if (rid(shadow[off + 3]) != 0) {
+                visible += depth <= shadow[off + 2] + pp->depth_bias ? 1.0f : 0.0f;
+                count += 1.0f;
+            }
+        }
+    }
+    return count > 0.0f ? visible / count : 0.0f;
+}
+
+void ora_project_texture(const ora_project_params* pp, const float* apos, const float* anrm,
+                         const float* araster, const float* shadow, const float* photo,
+                         const float* mask, const float* rayvis, float* acc_color, float* acc_weight,
+                         float* best_conf, uint32_t* source_view) {
+    const uint64_t N = (uint64_t)pp->atlas_width * pp->atlas_height;
+    const float* M = pp->world_to_clip;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)N; ++i) {
+        if (rid(araster[i * 4 + 3]) == 0) continue;
+        const float px = apos[i * 3], py = apos[i * 3 + 1], pz = apos[i * 3 + 2];
+        const float nx0 = anrm[i * 3], ny0 = anrm[i * 3 + 1], nz0 = anrm[i * 3 + 2];
+        const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
+        const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
+        const float cx = M[0] * px + M[1] * py + M[2] * pz + M[3] * 1.0f;
+        const float cy = M[4] * px + M[5] * py + M[6] * pz + M[7] * 1.0f;
+        const float cz = M[8] * px + M[9] * py + M[10] * pz + M[11] * 1.0f;
+        const float cw = M[12] * px + M[13] * py + M[14] * pz + M[15] * 1.0f;
+        if (cw <= 1e-8f) continue;
+        const float ndx = cx / cw, ndy = cy / cw, ndz = cz / cw;
+        if (ndx < -1.0f || ndy < -1.0f || ndx > 1.0f || ndy > 1.0f || ndz < -1.0f || ndz > 1.0f) continue;
+        const float ppx = pp->viewport[0] + (ndx * 0.5f + 0.5f) * pp->viewport[2];
+        const float ppy = pp->viewport[1] + (ndy * 0.5f + 0.5f) * pp->viewport[3];
+        if (ppx < pp->viewport[0] || ppy < pp->viewport[1] || ppx >= pp->viewport[0] + pp->viewport[2] ||
+            ppy >= pp->viewport[1] + pp->viewport[3])
+            continue;
+        float vis = rayvis[i];
+        if (pp->visibility_mode == 0) vis = shadow_visibility(pp, shadow, ppx, ppy, ndz);
+        else if (pp->visibility_mode == 1) vis *= shadow_visibility(pp, shadow, ppx, ppy, ndz);
+        if (pp->has_mask) vis *= clampf_hlsl(sample_mask(pp, mask, ppx, ppy), 0.0f, 1.0f);
+        const float vx0 = pp->camera_position[0] - px, vy0 = pp->camera_position[1] - py, vz0 = pp->camera_position[2] - pz;
+        const float vl = sqrtf(vx0 * vx0 + vy0 * vy0 + vz0 * vz0);
+        const float vx = vx0 / vl, vy = vy0 / vl, vz = vz0 / vl;
+        const float cosv = nx * vx + ny * vy + nz * vz;
+        if (cosv < pp->min_view_cosine || vis <= 0.0f) continue;
+        const float c0 = sample_photo(pp, photo, ppx, ppy, 0);
+        const float c1 = sample_photo(pp, photo, ppx, ppy, 1);
+        const float c2 = sample_photo(pp, photo, ppx, ppy, 2);
+        const float alpha = pp->channel_count == 4 ? sample_photo(pp, photo, ppx, ppy, 3) : 1.0f;
+        if (pp->blend_mode == 2) {
+            const float dist = fmaxf(sqrtf(vx0 * vx0 + vy0 * vy0 + vz0 * vz0), 1e-6f);
+            const float footprint = cosv / (dist * dist);
+            const float ex = clampf_hlsl(vis * alpha * footprint * pp->view_weight, 0.0f, 64.0f);
+            const float prev = best_conf[i];
+            const float cur = fmaxf(prev, ex);
+            if (cur > prev) {
+                const float rs = expf(prev - cur);
+                acc_color[i * 3] *= rs;
+                acc_color[i * 3 + 1] *= rs;
+                acc_color[i * 3 + 2] *= rs;
+                acc_weight[i] *= rs;
+                best_conf[i] = cur;
+            }
+            if (ex >= prev) source_view[i] = pp->view_index;
+            const float sw = expf(ex - cur);
+            if (sw <= 0.0f) continue;
+            acc_color[i * 3] += c0 * sw;
+            acc_color[i * 3 + 1] += c1 * sw;
+            acc_color[i * 3 + 2] += c2 * sw;
+            acc_weight[i] += sw;
+            continue;
+        }
+        const float conf = vis * alpha * cosv * pp->view_weight;
+        if (conf <= 0.0f) continue;
+        if (conf > best_conf[i]) {
+            best_conf[i] = conf;
+            source_view[i] = pp->view_index;
+        }
+        if (pp->blend_mode == 0) {
+            if (conf >= acc_weight[i]) {
+                acc_color[i * 3] = c0;
+                acc_color[i * 3 + 1] = c1;
+                acc_color[i * 3 + 2] = c2;
+                acc_weight[i] = conf;
+            }
+        } else {
+            acc_color[i * 3] += c0 * conf;
+            acc_color[i * 3 + 1] += c1 * conf;
+            acc_color[i * 3 + 2] += c2 * conf;
+            acc_weight[i] += conf;
+        }
+    }
+}
+
+/* ---- bake host: src/texture_baker.cpp:156-361 (shadow-map visibility) ----------------- */
+
+int ora_bake(const float* pos3, const float* nrm3, const float* uv2, uint32_t V, const uint32_t* idx,
+             uint32_t T, const ora_view* views, uint32_t nviews, uint32_t aw, uint32_t ah,
+             uint32_t blend_mode, uint32_t pcf_radius, float mask_floor, float softmax_scale,
+             float* color4, float* confidence, uint32_t* source_view, float* valid_mask,
+             float* coverage_mask, uint32_t* face_ids) {
+    if (V == 0 || T == 0 || nviews == 0) return ORA_INVALID;
+    for (uint64_t i = 0; i < (uint64_t)T * 3; ++i) if (idx[i] >= V) return ORA_RANGE;
+    if (aw == 0 || ah == 0 || pcf_radius > 4 || !isfinite(mask_floor) || mask_floor < 0.0f || mask_floor > 1.0f)
+        return ORA_INVALID;
+    const uint64_t N = (uint64_t)aw * ah;
+    float* aclip = (float*)malloc((size_t)V * 4 * sizeof(float));
+    for (uint64_t v = 0; v < V; ++v) {
+        aclip[v * 4 + 0] = uv2[v * 2 + 0] * 2.0f - 1.0f;
+        aclip[v * 4 + 1] = uv2[v * 2 + 1] * 2.0f - 1.0f;
+        aclip[v * 4 + 2] = 0.0f;
+        aclip[v * 4 + 3] = 1.0f;
+    }
+    const float avp[4] = {0.0f, 0.0f, (float)aw, (float)ah};
+    float* araster = (float*)malloc(N * 4 * sizeof(float));
+    int rc = ora_rasterize_forward(aclip, V, idx, T, aw, ah, 0, 0, avp, araster, NULL);
+    if (rc) { free(aclip); free(araster); return rc; }
+    float* apos = (float*)malloc(N * 3 * sizeof(float));
+    float* anrm = (float*)malloc(N * 3 * sizeof(float));
+    ora_interpolate_forward(pos3, V, 3, idx, T, araster, N, apos);
+    ora_interpolate_forward(nrm3, V, 3, idx, T, araster, N, anrm);
+    for (uint64_t i = 0; i < N; ++i) {
+        const float r = roundf(araster[i * 4 + 3]); /* std::round */
+        coverage_mask[i] = r != 0.0f ? 1.0f : 0.0f;
+        face_ids[i] = coverage_mask[i] > 0.5f ? (uint32_t)r - 1u : UINT32_MAX;
+    }
+    float scale = softmax_scale;
+    if (blend_mode == 2 && (!(scale > 0.0f) || !isfinite(scale))) {
+        float* cams = (float*)malloc((size_t)nviews * 3 * sizeof(float));
+        for (uint32_t k = 0; k < nviews; ++k) memcpy(cams + k * 3, views[k].camera_position, 3 * sizeof(float));
+        scale = ora_suggest_softmax_scale(pos3, V, cams, nviews);
+        free(cams);
+        if (!(scale > 0.0f) || !isfinite(scale)) scale = 1.0f;
+    }
+    float* acc = (float*)calloc(N * 3, sizeof(float));
+    float* accw = (float*)calloc(N, sizeof(float));
+    float* best = (float*)calloc(N, sizeof(float));
+    float* rayvis = (float*)malloc(N * sizeof(float));
+    for (uint64_t i = 0; i < N; ++i) { rayvis[i] = 1.0f; source_view[i] = UINT32_MAX; }
+    float* clip = (float*)malloc((size_t)V * 4 * sizeof(float));
+    for (uint32_t k = 0; k < nviews && rc == 0; ++k) {
+        const ora_view* vw = &views[k];
+        if (vw->width == 0 || vw->height == 0 || (vw->channel_count != 3 && vw->channel_count != 4)) { rc = ORA_INVALID; break; }
+        if (!isfinite(vw->weight) || vw->weight < 0.0f || !isfinite(vw->depth_bias) || vw->depth_bias < 0.0f ||
+            !isfinite(vw->min_view_cosine) || vw->min_view_cosine < -1.0f || vw->min_view_cosine > 1.0f) { rc = ORA_INVALID; break; }
+        const float vvp[4] = {vw->has_viewport ? vw->viewport[0] : 0.0f, vw->has_viewport ? vw->viewport[1] : 0.0f,
+                              vw->has_viewport ? vw->viewport[2] : (float)vw->width,
+                              vw->has_viewport ? vw->viewport[3] : (float)vw->height};
+        const uint64_t Pv = (uint64_t)vw->width * vw->height;
+        ora_transform_positions(pos3, V, vw->world_to_clip, clip);
+        float* shadow = (float*)malloc(Pv * 4 * sizeof(float));
+        rc = ora_rasterize_forward(clip, V, idx, T, vw->width, vw->height, 0, 0, vvp, shadow, NULL);
+        if (rc) { free(shadow); break; }
+        float* floored = NULL;
+        const float* mask = vw->visibility_mask;
+        if (mask_floor > 0.0f && mask) {
+            floored = (float*)malloc(Pv * sizeof(float));
+            for (uint64_t i = 0; i < Pv; ++i) floored[i] = mask[i] < mask_floor ? mask_floor : mask[i];
+            mask = floored;
+        }
+        ora_project_params pp;
+        memcpy(pp.world_to_clip, vw->world_to_clip, sizeof(pp.world_to_clip));
+        memcpy(pp.camera_position, vw->camera_position, sizeof(pp.camera_position));
+        pp.view_weight = blend_mode == 2 ? vw->weight * scale : vw->weight;
+        memcpy(pp.viewport, vvp, sizeof(vvp));
+        pp.atlas_width = aw;
+        pp.atlas_height = ah;
+        pp.image_width = vw->width;
+        pp.image_height = vw->height;
+        pp.depth_bias = vw->depth_bias;
+        pp.min_view_cosine = vw->min_view_cosine;
+        pp.channel_count = vw->channel_count;
+        pp.blend_mode = blend_mode;
+        pp.pcf_radius = pcf_radius;
+        pp.has_mask = vw->visibility_mask != NULL;
+        pp.visibility_mode = 0;
+        pp.view_index = k;
+        ora_project_texture(&pp, apos, anrm, araster, shadow, vw->image, mask, rayvis, acc, accw, best, source_view);
+        free(floored);
+        free(shadow);
+    }
+    if (rc == 0) {
+        for (uint64_t i = 0; i < N; ++i) {
+            const float w = accw[i];
+            confidence[i] = w;
+            valid_mask[i] = w > 0.0f ? 1.0f : 0.0f;
+            const float div = blend_mode != 0 && w > 0.0f ? w : 1.0f;
+            color4[i * 4 + 0] = acc[i * 3 + 0] / div;
+            color4[i * 4 + 1] = acc[i * 3 + 1] / div;
+            color4[i * 4 + 2] = acc[i * 3 + 2] / div;
+            color4[i * 4 + 3] = valid_mask[i];
+        }
+    }
+    free(clip); free(rayvis); free(best); free(accw); free(acc);
+    free(apos); free(anrm); free(araster); free(aclip);
+    return rc;
+}
+
+/* ---- atlas refinement kernels ------------------------------------------------------- */
+
+static void clamp_layout(float u, float v, uint32_t tw, uint32_t th, uint32_t tx[4], float w[4]) {
+    const float px = u * (float)tw - 0.5f, py = v * (float)th - 0.5f;
+    const int32_t bx = f2i_sat(floorf(px)), by = f2i_sat(floorf(py));
+    const float fx = px - floorf(px), fy = py - floorf(py);
+    const uint32_t x0 = (uint32_t)clampi(bx, 0, (int32_t)tw - 1), x1 = (uint32_t)clampi(add1(bx), 0, (int32_t)tw - 1);
+    const uint32_t y0 = (uint32_t)clampi(by, 0, (int32_t)th - 1), y1 = (uint32_t)clampi(add1(by), 0, (int32_t)th - 1);
+    tx[0] = y0 * tw + x0;
+    tx[1] = y0 * tw + x1;
+    tx[2] = y1 * tw + x0;
+    tx[3] = y1 * tw + x1;
+    w[0] = (1.0f - fx) * (1.0f - fy);
+    w[1] = fx * (1.0f - fy);
+    w[2] = (1.0f - fx) * fy;
+    w[3] = fx * fy;
+}
+
+/* atlas_photometric_gradient.hlsl:45-108: per-pixel math in pixel order; the loss is
+ * reduced per 64-pixel group with the shader's tree, then groups in order. */
+float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const float* uv,
+                               const float* target, const float* mask, uint32_t P, float eps,
+                               float norm, float* grad) {
+    float loss = 0.0f;
+    float group[64];
+    for (uint32_t g0 = 0; g0 < P; g0 += 64) {
+        for (uint32_t gi = 0; gi < 64; ++gi) {
+            const uint32_t p = g0 + gi;
+            float local = 0.0f;
+            if (p < P) {
+                const float m = mask[p];
+                if (m > 0.0f) {
+                    uint32_t tx[4];
+                    float w[4];
+                    clamp_layout(uv[(uint64_t)p * 2], uv[(uint64_t)p * 2 + 1], tw, th, tx, w);
+                    for (uint32_t c = 0; c < 3; ++c) {
+                        float rendered = 0.0f;
+                        for (int k = 0; k < 4; ++k) rendered += tex[(uint64_t)tx[k] * 3 + c] * w[k];
+                        const float d = rendered - target[(uint64_t)p * 3 + c];
+                        const float robust = sqrtf(d * d + eps * eps);
+                        const float og = d / robust * m * norm;
+                        local += robust * m * norm;
+                        for (int k = 0; k < 4; ++k) grad[(uint64_t)tx[k] * 3 + c] += og * w[k];
+                    }
+                }
+            }
+            group[gi] = local;
+        }
+        for (uint32_t stride = 32; stride > 0; stride >>= 1)
+            for (uint32_t gi = 0; gi < stride; ++gi) group[gi] += group[gi + stride];
+        if (group[0] != 0.0f) loss += group[0];
+    }
+    return loss;
+}
+
+float ora_seam_gradient(const float* tex, uint32_t tw, uint32_t th, const float* pairs,
+                        uint32_t npairs, float eps, float norm, float* grad) {
+    float loss = 0.0f;
+    float group[64];
+    for (uint32_t g0 = 0; g0 < npairs; g0 += 64) {
+        for (uint32_t gi = 0; gi < 64; ++gi) {
+            const uint32_t i = g0 + gi;
+            float local = 0.0f;
+            if (i < npairs) {
+                uint32_t t0[4], t1[4];
+                float w0[4], w1[4];
+                clamp_layout(pairs[(uint64_t)i * 4], pairs[(uint64_t)i * 4 + 1], tw, th, t0, w0);
+                clamp_layout(pairs[(uint64_t)i * 4 + 2], pairs[(uint64_t)i * 4 + 3], tw, th, t1, w1);
+                for (uint32_t c = 0; c < 3; ++c) {
+                    float c0 = 0.0f, c1 = 0.0f;
+                    for (int k = 0; k < 4; ++k) {
+                        c0 += tex[(uint64_t)t0[k] * 3 + c] * w0[k];
+                        c1 += tex[(uint64_t)t1[k] * 3 + c] * w1[k];
+                    }
+                    const float d = c0 - c1;
+                    const float robust = sqrtf(d * d + eps * eps);
+                    const float g = d / robust * norm;
+                    local += robust * norm;
+                    for (int k = 0; k < 4; ++k) {
+                        grad[(uint64_t)t0[k] * 3 + c] += g * w0[k];
+                        grad[(uint64_t)t1[k] * 3 + c] += -g * w1[k];
+                    }
+                }
+            }
+            group[gi] = local;
+        }
+        for (uint32_t stride = 32; stride > 0; stride >>= 1)
+            for (uint32_t gi = 0; gi < stride; ++gi) group[gi] += group[gi + stride];
+        if (group[0] != 0.0f) loss += group[0];
+    }
+    return loss;
+}
+
+/* atlas_adam_update.hlsl:20-43 */
+void ora_adam_update(float* tex, float* grad, float* m, float* v, uint64_t n, float lr, float b1,
+                     float b2, float eps, float bc1, float bc2, float cmin, float cmax) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const float g = grad[i];
+        const float m1 = b1 * m[i] + (1.0f - b1) * g;
+        const float m2 = b2 * v[i] + (1.0f - b2) * g * g;
+        m[i] = m1;
+        v[i] = m2;
+        const float c1 = m1 / bc1, c2 = m2 / bc2;
+        tex[i] = clampf_hlsl(tex[i] - lr * c1 / (sqrtf(c2) + eps), cmin, cmax);
+        grad[i] = 0.0f;
+    }
+}
+
+/* texture_refiner.cpp:219-242 */
+int ora_refine_view_cache(const float* pos3, const float* uv2, uint32_t V, const uint32_t* idx,
+                          uint32_t T, const ora_view* vw, float* uv_out, float* target, float* mask,
+                          double* valid_weight) {
+    const uint64_t P = (uint64_t)vw->width * vw->height;
+    const float vvp[4] = {vw->has_viewport ? vw->viewport[0] : 0.0f, vw->has_viewport ? vw->viewport[1] : 0.0f,
+                          vw->has_viewport ? vw->viewport[2] : (float)vw->width,
+                          vw->has_viewport ? vw->viewport[3] : (float)vw->height};
+    float* clip = (float*)malloc((size_t)V * 4 * sizeof(float));
+    ora_transform_positions(pos3, V, vw->world_to_clip, clip);
+    float* raster = (float*)malloc(P * 4 * sizeof(float));
+    int rc = ora_rasterize_forward(clip, V, idx, T, vw->width, vw->height, 0, 0, vvp, raster, NULL);
+    if (rc) { free(clip); free(raster); return rc; }
+    ora_interpolate_forward(uv2, V, 2, idx, T, raster, P, uv_out);
+    double vwsum = 0.0;
+    for (uint64_t p = 0; p < P; ++p) {
+        target[p * 3] = vw->image[p * vw->channel_count];
+        target[p * 3 + 1] = vw->image[p * vw->channel_count + 1];
+        target[p * 3 + 2] = vw->image[p * vw->channel_count + 2];
+        mask[p] = 0.0f;
+        if (raster[p * 4 + 3] != 0.0f) {
+            float ext = 1.0f;
+            if (vw->visibility_mask) {
+                const float m = vw->visibility_mask[p];
+                ext = m < 0.0f ? 0.0f : (1.0f < m ? 1.0f : m); /* std::clamp */
+            }
+            mask[p] = ext;
+            vwsum += ext;
+        }
+    }
+    *valid_weight = vwsum;
+    free(clip);
+    free(raster);
+    return ORA_OK;
+}
+
+int ora_refine(const float* init, const float* pos3, const float* uv2, uint32_t V, const uint32_t* idx,
+               uint32_t T, const ora_view* views, uint32_t nviews, const float* pairs, uint32_t npairs,
+               const ora_refine_options* o, float* out, float* loss_hist, float* seam_hist) {
+    if (V == 0 || T == 0 || nviews == 0) return ORA_INVALID;
+    for (uint64_t i = 0; i < (uint64_t)T * 3; ++i) if (idx[i] >= V) return ORA_INVALID;
+    const uint64_t n = (uint64_t)o->width * o->height * 3;
+    if (o->width == 0 || o->height == 0 || o->steps == 0 || o->batch_size == 0 ||
+        !isfinite(o->learning_rate) || o->learning_rate <= 0.0f || !isfinite(o->minimum_learning_rate) ||
+        o->minimum_learning_rate < 0.0f || o->minimum_learning_rate > o->learning_rate ||
+        !isfinite(o->photometric_epsilon) || o->photometric_epsilon <= 0.0f ||
+        !(o->adam_beta1 > 0.0f && o->adam_beta1 < 1.0f) || !(o->adam_beta2 > 0.0f && o->adam_beta2 < 1.0f) ||
+        !(o->clamp_min < o->clamp_max) || !isfinite(o->seam_learning_rate) || o->seam_learning_rate <= 0.0f ||
+        !isfinite(o->seam_epsilon) || o->seam_epsilon <= 0.0f)
+        return ORA_INVALID;
+    if (n > UINT32_MAX) return ORA_OVERFLOW;
+    float** cuv = (float**)calloc(nviews, sizeof(float*));
+    float** ctg = (float**)calloc(nviews, sizeof(float*));
+    float** cmk = (float**)calloc(nviews, sizeof(float*));
+    double* cvw = (double*)calloc(nviews, sizeof(double));
+    int rc = ORA_OK;
+    for (uint32_t k = 0; k < nviews && rc == 0; ++k) {
+        const ora_view* vw = &views[k];
+        if (vw->width == 0 || vw->height == 0 || (vw->channel_count != 3 && vw->channel_count != 4)) { rc = ORA_INVALID; break; }
+        const uint64_t P = (uint64_t)vw->width * vw->height;
+        cuv[k] = (float*)malloc(P * 2 * sizeof(float));
+        ctg[k] = (float*)malloc(P * 3 * sizeof(float));
+        cmk[k] = (float*)malloc(P * sizeof(float));
+        rc = ora_refine_view_cache(pos3, uv2, V, idx, T, vw, cuv[k], ctg[k], cmk[k], &cvw[k]);
+    }
+    if (rc == 0) {
+        memcpy(out, init, n * sizeof(float));
+        float* g = (float*)calloc(n, sizeof(float));
+        float* m = (float*)calloc(n, sizeof(float));
+        float* v = (float*)calloc(n, sizeof(float));
+        const float pi = acosf(-1.0f);
+        for (uint32_t s = 0; s < o->steps; ++s) {
+            double bvw = 0.0;
+            for (uint32_t b = 0; b < o->batch_size; ++b) bvw += cvw[((uint64_t)s * o->batch_size + b) % nviews];
+            const float norm = bvw > 0.0 ? (float)(1.0 / (bvw * 3.0)) : 0.0f;
+            float loss = 0.0f;
+            for (uint32_t b = 0; b < o->batch_size; ++b) {
+                const uint32_t k = (uint32_t)(((uint64_t)s * o->batch_size + b) % nviews);
+                loss += ora_photometric_gradient(out, o->width, o->height, cuv[k], ctg[k], cmk[k],
+                                                 views[k].width * views[k].height, o->photometric_epsilon, norm, g);
+            }
+            loss_hist[s] = loss;
+            const float phase = (float)s / (float)o->steps;
+            const float lr = o->minimum_learning_rate +
+                             0.5f * (o->learning_rate - o->minimum_learning_rate) * (1.0f + cosf(pi * phase));
+            ora_adam_update(out, g, m, v, n, lr, o->adam_beta1, o->adam_beta2, o->adam_epsilon,
+                            1.0f - powf(o->adam_beta1, (float)(s + 1)), 1.0f - powf(o->adam_beta2, (float)(s + 1)),
+                            o->clamp_min, o->clamp_max);
+        }
+        const uint32_t seam_steps = npairs == 0 ? 0 : o->seam_polish_steps;
+        if (seam_steps) {
+            memset(g, 0, n * sizeof(float));
+            memset(m, 0, n * sizeof(float));
+            memset(v, 0, n * sizeof(float));
+            for (uint32_t s = 0; s < seam_steps; ++s) {
+                seam_hist[s] = ora_seam_gradient(out, o->width, o->height, pairs, npairs, o->seam_epsilon,
+                                                 1.0f / (float)(npairs * 3u), g);
+                ora_adam_update(out, g, m, v, n, o->seam_learning_rate, o->adam_beta1, o->adam_beta2, o->adam_epsilon,
+                                1.0f - powf(o->adam_beta1, (float)(s + 1)), 1.0f - powf(o->adam_beta2, (float)(s + 1)),
+                                o->clamp_min, o->clamp_max);
+            }
+        }
+        free(g); free(m); free(v);
+    }
+    for (uint32_t k = 0; k < nviews; ++k) { free(cuv[k]); free(ctg[k]); free(cmk[k]); }
+    free(cuv); free(ctg); free(cmk); free(cvw);
+    return rc;
+}
+
+/* ---- chart-aware total variation: python/photara_drender/atlas.py:84-115 --------------- */
+
+double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C, const uint8_t* valid,
+                       const int32_t* chart, float eps, float weight, float* grad) {
+    uint64_t pairs = 0;
+    for (uint32_t y = 0; y < th; ++y)
+        for (uint32_t x = 0; x < tw; ++x) {
+            const uint64_t i = (uint64_t)y * tw + x;
+            if (x + 1 < tw && valid[i] && valid[i + 1] && (!chart || chart[i] == chart[i + 1])) pairs++;
+            if (y + 1 < th && valid[i] && valid[i + tw] && (!chart || chart[i] == chart[i + tw])) pairs++;
+        }
+    const double denom = (double)(pairs > 0 ? pairs : 1) * C;
+    const float scale = (float)((double)weight / denom);
+    double loss = 0.0;
+    for (uint32_t y = 0; y < th; ++y)
+        for (uint32_t x = 0; x < tw; ++x) {
+            const uint64_t i = (uint64_t)y * tw + x;
+            for (int dir = 0; dir < 2; ++dir) {
+                uint64_t j;
+                if (dir == 0) { if (x + 1 >= tw) continue; j = i + 1; }
+                else { if (y + 1 >= th) continue; j = i + tw; }
+                if (!(valid[i] && valid[j] && (!chart || chart[i] == chart[j]))) continue;
+                for (uint32_t c = 0; c < C; ++c) {
+                    const float d = tex[j * C + c] - tex[i * C + c];
+                    const float r = sqrtf(d * d + eps * eps);
+                    loss += r;
+                    const float gg = d / r * scale;
+                    grad[j * C + c] += gg;
+                    grad[i * C + c] -= gg;
+                }
+            }
+        }
+    return loss * (double)weight / denom;
+}

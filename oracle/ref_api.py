@@ -1,0 +1,204 @@
+"""NumPy face of ``libpdr_ref.so``: the reference's own HLSL shaders (and its CPU
+``texture_padding.cpp``) compiled for the CPU. TEST INFRASTRUCTURE ONLY.
+
+The reference's host-side table builders cannot be compiled here (``src/rasterizer.cpp`` needs
+the absent Vulkan wrapper), so this module restates the two small ones it needs in NumPy:
+the vertex->corner table (src/rasterizer.cpp:145-162) and the texel->sample table with
+double-precision weights (src/rasterizer.cpp:187-258). Tile bins come from the oracle's
+restatement of build_tile_bins (src/rasterizer.cpp:61-138).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import api
+
+_f32p = C.POINTER(C.c_float)
+_u32p = C.POINTER(C.c_uint32)
+
+
+def available() -> bool:
+    return api.ref() is not None
+
+
+def _L():
+    L = api.ref()
+    if L is None:
+        raise RuntimeError("reference sources are not available on this machine")
+    L.ref_suggest_softmax_scale.restype = C.c_float
+    return L
+
+
+def _p(a, t=_f32p):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def rasterize_forward(pos, idx, resolution, cull_mode=0, output_derivatives=True, viewport=None):
+    pos, idx = api._f(pos), api._u(idx)
+    h, w = resolution
+    vp = api._vp(viewport, w, h)
+    offsets, lst = api.bin_tiles(pos, idx, resolution, vp)
+    lst = np.ascontiguousarray(lst if lst.size else np.zeros(1, np.uint32))
+    raster = np.zeros((h, w, 4), np.float32)
+    deriv = np.zeros((h, w, 4), np.float32)
+    _L().ref_rasterize_forward(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, cull_mode,
+                               int(bool(output_derivatives)), _p(vp), (w + 15) // 16, _p(offsets, _u32p),
+                               _p(lst, _u32p), _p(raster), _p(deriv))
+    return raster, (deriv if output_derivatives else None)
+
+
+def vertex_corner_table(idx, V):
+    """src/rasterizer.cpp:145-162: CSR of corners per vertex, corners ascending."""
+    flat = np.asarray(idx, dtype=np.uint32).reshape(-1)
+    offsets = np.zeros(V + 1, np.uint32)
+    np.add.at(offsets, flat.astype(np.int64) + 1, 1)
+    offsets = np.cumsum(offsets).astype(np.uint32)
+    corners = np.argsort(flat, kind="stable").astype(np.uint32)
+    return offsets, corners
+
+
+def rasterize_backward(pos, idx, raster, grad_raster, viewport=None):
+    pos, idx, raster, grad_raster = api._f(pos), api._u(idx), api._f(raster), api._f(grad_raster)
+    h, w = raster.shape[:2]
+    vp = api._vp(viewport, w, h)
+    T, V = idx.shape[0], pos.shape[0]
+    corner = np.zeros((T * 3, 4), np.float32)
+    L = _L()
+    L.ref_rasterize_backward(_p(pos), V, _p(idx, _u32p), T, w, h, _p(vp), _p(raster), _p(grad_raster), _p(corner))
+    off, corners = vertex_corner_table(idx, V)
+    out = np.zeros((V, 4), np.float32)
+    L.ref_reduce_vertex_gradients(_p(off, _u32p), _p(corners, _u32p), _p(corner), V, _p(out))
+    return out
+
+
+def interpolate_forward(attr, idx, raster):
+    attr, idx, raster = api._f(attr), api._u(idx), api._f(raster)
+    h, w = raster.shape[:2]
+    V, A = attr.shape
+    out = np.zeros((h, w, A), np.float32)
+    _L().ref_interpolate_forward(_p(attr), V, A, _p(idx, _u32p), idx.shape[0], _p(raster), h * w, _p(out))
+    return out
+
+
+def interpolate_backward(attr, idx, raster, grad):
+    attr, idx, raster, grad = api._f(attr), api._u(idx), api._f(raster), api._f(grad)
+    h, w = raster.shape[:2]
+    V, A = attr.shape
+    ga = np.zeros((V, A), np.float32)
+    gr = np.zeros((h, w, 4), np.float32)
+    L = _L()
+    L.ref_interpolate_grad_attributes(_p(idx, _u32p), V, A, idx.shape[0], _p(raster), h * w, _p(grad), _p(ga))
+    L.ref_interpolate_grad_raster(_p(attr), V, A, _p(idx, _u32p), idx.shape[0], _p(raster), h * w, _p(grad), _p(gr))
+    return ga, gr
+
+
+def texture_forward(tex, uv, raster, address_mode="clamp"):
+    tex, uv, raster = api._f(tex), api._f(uv), api._f(raster)
+    th, tw, Cc = tex.shape
+    h, w = raster.shape[:2]
+    out = np.zeros((h, w, Cc), np.float32)
+    _L().ref_texture_forward(_p(tex), tw, th, Cc, api.ADDRESS[address_mode], _p(uv), _p(raster), h * w, _p(out))
+    return out
+
+
+def _address(c, size, mode):
+    c = c.astype(np.int64)
+    if mode == 0:
+        return np.clip(c, 0, size - 1)
+    if mode == 1:
+        return np.mod(c, size)
+    period = 2 * size
+    m = np.mod(c, period)
+    return np.where(m < size, m, period - 1 - m)
+
+
+def texture_sample_table(uv, raster, tw, th, mode):
+    """src/rasterizer.cpp:187-258 restated: texel CSR of sample entries and float weights from
+    double-precision texel positions."""
+    uv = np.asarray(uv, np.float32).reshape(-1, 2)
+    r3 = np.asarray(raster, np.float32).reshape(-1, 4)[:, 3]
+    P = uv.shape[0]
+    covered = r3 != 0.0
+    tx = uv[:, 0].astype(np.float64) * tw - 0.5
+    ty = uv[:, 1].astype(np.float64) * th - 0.5
+    bx, by = np.floor(tx), np.floor(ty)
+    fx = (tx - bx).astype(np.float32)
+    fy = (ty - by).astype(np.float32)
+    one = np.float32(1.0)
+    weights = np.stack([(one - fx) * (one - fy), fx * (one - fy), (one - fx) * fy, fx * fy], axis=1)
+    weights[~covered] = 0.0
+    bx = np.where(covered, bx, 0).astype(np.int64)
+    by = np.where(covered, by, 0).astype(np.int64)
+    xs = [_address(bx, tw, mode), _address(bx + 1, tw, mode)]
+    ys = [_address(by, th, mode), _address(by + 1, th, mode)]
+    texels = np.stack([ys[0] * tw + xs[0], ys[0] * tw + xs[1], ys[1] * tw + xs[0], ys[1] * tw + xs[1]], axis=1)
+    entries = np.arange(P * 4, dtype=np.int64)
+    valid = np.repeat(covered, 4)
+    tex_of_entry = texels.reshape(-1)[valid]
+    ent = entries[valid]
+    order = np.argsort(tex_of_entry, kind="stable")
+    offsets = np.zeros(tw * th + 1, np.int64)
+    np.add.at(offsets, tex_of_entry + 1, 1)
+    offsets = np.cumsum(offsets)
+    return (offsets.astype(np.uint32), np.ascontiguousarray(ent[order].astype(np.uint32)),
+            np.ascontiguousarray(weights.reshape(-1).astype(np.float32)))
+
+
+def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gradient=True):
+    tex, uv, raster, grad = api._f(tex), api._f(uv), api._f(raster), api._f(grad)
+    th, tw, Cc = tex.shape
+    h, w = raster.shape[:2]
+    mode = api.ADDRESS[address_mode]
+    off, ent, wts = texture_sample_table(uv, raster, tw, th, mode)
+    ent = ent if ent.size else np.zeros(1, np.uint32)
+    gt = np.zeros(tex.shape, np.float32)
+    L = _L()
+    L.ref_texture_grad_texture(_p(grad), _p(off, _u32p), _p(ent, _u32p), _p(wts), tw * th, h * w, Cc, _p(gt))
+    gu = None
+    if compute_uv_gradient:
+        gu = np.zeros((h, w, 2), np.float32)
+        L.ref_texture_grad_uv(_p(tex), tw, th, Cc, mode, _p(uv), _p(raster), h * w, _p(grad), _p(gu))
+    return gt, gu
+
+
+def project_texture(m16, cam_weight4, vp4, dims4, depth_bias, min_cos, packed, view_index, apos, anrm, araster,
+                    shadow, photo, mask, rayvis, acc_color, acc_weight, best_conf, source_view):
+    a = [api._f(x) for x in (m16, cam_weight4, vp4)]
+    dims = np.ascontiguousarray(dims4, dtype=np.uint32)
+    _L().ref_project_texture(_p(a[0]), _p(a[1]), _p(a[2]), _p(dims, _u32p), C.c_float(depth_bias),
+                             C.c_float(min_cos), C.c_uint32(packed), C.c_uint32(view_index), _p(apos), _p(anrm),
+                             _p(araster), _p(shadow), _p(photo), _p(mask), _p(rayvis), _p(acc_color), _p(acc_weight),
+                             _p(best_conf), _p(source_view, _u32p))
+
+
+def photometric_gradient(tex3, uv, target, mask, eps, normalization, grad=None):
+    tex3, uv, target, mask = api._f(tex3), api._f(uv), api._f(target), api._f(mask)
+    th, tw, _ = tex3.shape
+    g = np.zeros_like(tex3) if grad is None else grad
+    loss = np.zeros(1, np.float32)
+    P = int(np.prod(mask.shape))
+    _L().ref_atlas_photometric_gradient(_p(tex3), _p(uv), _p(target), _p(mask), P, tw, th, 0, C.c_float(eps),
+                                        C.c_float(normalization), _p(g), _p(loss))
+    return g, float(loss[0])
+
+
+def seam_gradient(tex3, pairs, eps, normalization, grad=None):
+    tex3, pairs = api._f(tex3), api._f(pairs)
+    th, tw, _ = tex3.shape
+    g = np.zeros_like(tex3) if grad is None else grad
+    loss = np.zeros(1, np.float32)
+    _L().ref_atlas_seam_gradient(_p(tex3), _p(pairs), pairs.shape[0], tw, th, 0, C.c_float(eps),
+                                 C.c_float(normalization), _p(g), _p(loss))
+    return g, float(loss[0])
+
+
+def adam_update(tex, grad, m, v, lr, b1, b2, eps, bc1, bc2, cmin, cmax):
+    _L().ref_atlas_adam_update(_p(tex), _p(grad), _p(m), _p(v), tex.size, C.c_float(lr), C.c_float(b1), C.c_float(b2),
+                               C.c_float(eps), C.c_float(bc1), C.c_float(bc2), C.c_float(cmin), C.c_float(cmax))
+
+
+def suggest_softmax_scale(positions, camera_positions):
+    pos, cams = api._f(positions), api._f(camera_positions)
+    return float(_L().ref_suggest_softmax_scale(_p(pos), pos.shape[0], _p(cams), cams.shape[0]))
