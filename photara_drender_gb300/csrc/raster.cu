@@ -1,0 +1,604 @@
+// Tile binning and rasterization (forward and backward) for many views in one launch.
+//
+// Reference path: src/rasterizer.cpp:61-138 (CPU tile binning), shaders/rasterize_forward.hlsl,
+// shaders/rasterize_backward.hlsl + reduce_vertex_gradients.hlsl.
+//
+// Layout in HBM: clip positions [views][V][4] fp32, indices [T][3] u32 (shared by all views),
+// viewports [views][4], tile bins as one CSR over (view, tile) keys: offsets [views*tiles+1]
+// and triangle ids sorted ascending inside every tile, raster/derivatives [views][H][W][4].
+#include <cuda_runtime.h>
+#include <float.h>
+
+#include "pdr_common.cuh"
+#include "pdr_internal.h"
+
+namespace pdr {
+namespace {
+
+constexpr uint32_t kNoRect = 0xffffffffu;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr uint32_t kScanBlock = kScanThreads * kScanItems;
+constexpr uint32_t kSmallSort = 1024;   // tiles up to this many entries sort in one warp
+constexpr uint32_t kWindowBits = 8192 * 32;  // id window of the large-tile bitmap sort (32 KB)
+
+struct TriRect {
+    uint32_t x;  // tx0 | tx1 << 16, or kNoRect
+    uint32_t y;  // ty0 | ty1 << 16
+};
+
+// src/rasterizer.cpp:73-125 for one triangle: pixel bounding box of the NDC bounds, clamped.
+__device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__ pos, const uint3 vi,
+                                                      uint32_t W, uint32_t H, float4 vp) {
+    TriRect r{kNoRect, 0};
+    float min_x = INFINITY, min_y = INFINITY, max_x = -INFINITY, max_y = -INFINITY;
+    const uint32_t v[3] = {vi.x, vi.y, vi.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float4 p = pos[v[c]];
+        if (!(p.w > 1e-8f) || !isfinite(p.w)) return r;
+        const float x = p.x / p.w;
+        const float y = p.y / p.w;
+        if (!isfinite(x) || !isfinite(y)) return r;
+        min_x = x < min_x ? x : min_x;
+        min_y = y < min_y ? y : min_y;
+        max_x = max_x < x ? x : max_x;
+        max_y = max_y < y ? y : max_y;
+    }
+    if (max_x < -1.0f || min_x > 1.0f || max_y < -1.0f || min_y > 1.0f) return r;
+    const int64_t px0 = f2i_sat(floorf((min_x * 0.5f + 0.5f) * vp.z + vp.x));
+    const int64_t px1 = (int64_t)f2i_sat(ceilf((max_x * 0.5f + 0.5f) * vp.z + vp.x)) - 1;
+    const int64_t py0 = f2i_sat(floorf((min_y * 0.5f + 0.5f) * vp.w + vp.y));
+    const int64_t py1 = (int64_t)f2i_sat(ceilf((max_y * 0.5f + 0.5f) * vp.w + vp.y)) - 1;
+    const int64_t wm = (int64_t)W - 1, hm = (int64_t)H - 1;
+    const uint32_t x0 = (uint32_t)(px0 < 0 ? 0 : (px0 > wm ? wm : px0));
+    const uint32_t x1 = (uint32_t)(px1 < 0 ? 0 : (px1 > wm ? wm : px1));
+    const uint32_t y0 = (uint32_t)(py0 < 0 ? 0 : (py0 > hm ? hm : py0));
+    const uint32_t y1 = (uint32_t)(py1 < 0 ? 0 : (py1 > hm ? hm : py1));
+    r.x = (x0 / kTile) | ((x1 / kTile) << 16);
+    r.y = (y0 / kTile) | ((y1 / kTile) << 16);
+    return r;
+}
+
+// Pass 1: per (view, triangle) tile rectangle and per-tile counts (warp-aggregated when the
+// lanes of a warp land in the same single tile).
+__global__ void bin_count_kernel(const float4* __restrict__ clip, uint32_t V, const uint3* __restrict__ idx,
+                                 uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports,
+                                 uint32_t tcx, uint32_t tiles, TriRect* __restrict__ rects,
+                                 uint32_t* __restrict__ counts) {
+    const uint32_t view = blockIdx.y;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = t < T;
+    TriRect r{kNoRect, 0};
+    if (live) {
+        const uint3 vi = idx[t];
+        if (vi.x < V && vi.y < V && vi.z < V) r = triangle_tile_rect(clip + (size_t)view * V, vi, W, H, viewports[view]);
+        rects[(size_t)view * T + t] = r;
+    }
+    uint32_t* cnt = counts + (size_t)view * tiles;
+    const bool has = live && r.x != kNoRect;
+    const uint32_t tx0 = r.x & 0xffffu, tx1 = r.x >> 16, ty0 = r.y & 0xffffu, ty1 = r.y >> 16;
+    const bool single = has && tx0 == tx1 && ty0 == ty1;
+    const uint32_t key = single ? ty0 * tcx + tx0 : 0xffffffffu - (threadIdx.x & 31u);
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (single && (__ffs(peers) - 1) == (int)(threadIdx.x & 31u)) atomicAdd(cnt + key, (uint32_t)__popc(peers));
+    if (has && !single) {
+        for (uint32_t ty = ty0; ty <= ty1; ++ty)
+            for (uint32_t tx = tx0; tx <= tx1; ++tx) atomicAdd(cnt + ty * tcx + tx, 1u);
+    }
+}
+
+// Exclusive scan over the (view, tile) counts in three phases.
+// Block-wide exclusive scan of one value per thread; returns the block total in *total.
+__device__ __forceinline__ unsigned long long block_exclusive_u64(unsigned long long v, unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long n = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += n;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        unsigned long long s = lane < nw ? warp_sums[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long n = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += n;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const unsigned long long warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0ull;
+    *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + inc - v;
+}
+
+__global__ void scan_local_kernel(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ out,
+                                  unsigned long long* __restrict__ block_sums) {
+    const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    unsigned long long s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        v[i] = base + i < n ? in[base + i] : 0u;
+        s += v[i];
+    }
+    unsigned long long total;
+    unsigned long long pre = block_exclusive_u64(s, &total);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        if (base + i < n) out[base + i] = (uint32_t)pre;
+        pre += v[i];
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void scan_blocks_kernel(unsigned long long* __restrict__ block_sums, uint32_t nblocks,
+                                   uint32_t* __restrict__ out, uint32_t n, uint32_t* __restrict__ status,
+                                   unsigned long long capacity) {
+    // single block: exclusive scan of the block totals, chunk by chunk
+    unsigned long long carry = 0;
+    for (uint32_t c = 0; c < nblocks; c += blockDim.x) {
+        const uint32_t i = c + threadIdx.x;
+        const unsigned long long v = i < nblocks ? block_sums[i] : 0ull;
+        unsigned long long total;
+        const unsigned long long pre = block_exclusive_u64(v, &total);
+        if (i < nblocks) block_sums[i] = carry + pre;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const bool overflow = carry > 0xffffffffull;
+        out[n] = overflow ? 0xffffffffu : (uint32_t)carry;
+        status[kStatusTotal] = overflow ? 0xffffffffu : (uint32_t)carry;
+        status[kStatusTotalHi] = (uint32_t)(carry >> 32);
+        status[kStatusOverflow] = (overflow || carry > capacity) ? 1u : 0u;
+        status[kStatusLargeTiles] = 0u;
+    }
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ out, uint32_t n, const unsigned long long* __restrict__ block_sums,
+                                uint32_t* __restrict__ cursor) {
+    const size_t base = (size_t)blockIdx.x * kScanBlock;
+    const uint32_t add = (uint32_t)block_sums[blockIdx.x];
+    for (uint32_t i = threadIdx.x; i < kScanBlock; i += blockDim.x) {
+        const size_t k = base + i;
+        if (k < n) {
+            const uint32_t v = out[k] + add;
+            out[k] = v;
+            cursor[k] = v;
+        }
+    }
+}
+
+// Pass 2: scatter triangle ids into their tiles (unordered inside a tile).
+__global__ void bin_fill_kernel(const TriRect* __restrict__ rects, uint32_t T, uint32_t tcx, uint32_t tiles,
+                                uint32_t* __restrict__ cursor, uint32_t* __restrict__ unsorted,
+                                unsigned long long capacity) {
+    const uint32_t view = blockIdx.y;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = t < T;
+    TriRect r{kNoRect, 0};
+    if (live) r = rects[(size_t)view * T + t];
+    uint32_t* cur = cursor + (size_t)view * tiles;
+    const bool has = live && r.x != kNoRect;
+    const uint32_t tx0 = r.x & 0xffffu, tx1 = r.x >> 16, ty0 = r.y & 0xffffu, ty1 = r.y >> 16;
+    const bool single = has && tx0 == tx1 && ty0 == ty1;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t key = single ? ty0 * tcx + tx0 : 0xffffffffu - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (single) {
+        const int leader = __ffs(peers) - 1;
+        uint32_t slot = 0;
+        if ((int)lane == leader) slot = atomicAdd(cur + key, (uint32_t)__popc(peers));
+        slot = __shfl_sync(peers, slot, leader);
+        slot += __popc(peers & ((1u << lane) - 1u));
+        if (slot < capacity) unsorted[slot] = t;
+    }
+    if (has && !single) {
+        for (uint32_t ty = ty0; ty <= ty1; ++ty)
+            for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+                const uint32_t slot = atomicAdd(cur + ty * tcx + tx, 1u);
+                if (slot < capacity) unsorted[slot] = t;
+            }
+    }
+}
+
+// Pass 3a: sort every tile with at most kSmallSort entries inside one warp (bitonic in shared
+// memory); larger tiles are queued for pass 3b.
+__global__ void bin_sort_small_kernel(const uint32_t* __restrict__ offsets, uint32_t segments,
+                                      const uint32_t* __restrict__ unsorted, uint32_t* __restrict__ sorted,
+                                      uint32_t* __restrict__ large_queue, uint32_t* __restrict__ status,
+                                      unsigned long long capacity) {
+    __shared__ uint32_t buf[8][kSmallSort];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t seg = blockIdx.x * 8 + warp;
+    if (seg >= segments) return;
+    const uint32_t b = offsets[seg];
+    uint32_t e = offsets[seg + 1];
+    if (e > capacity) e = (uint32_t)capacity;
+    if (b >= e) return;
+    const uint32_t n = e - b;
+    if (n > kSmallSort) {
+        if (lane == 0) {
+            const uint32_t q = atomicAdd(status + kStatusLargeTiles, 1u);
+            large_queue[q] = seg;
+        }
+        return;
+    }
+    if (n <= 32) {
+        const uint32_t v = lane < n ? unsorted[b + lane] : 0xffffffffu;
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < 32; ++j) {
+            const uint32_t o = __shfl_sync(0xffffffffu, v, j);
+            rank += (o < v) ? 1u : 0u;
+        }
+        if (lane < n) sorted[b + rank] = v;
+        return;
+    }
+    uint32_t m = 64;
+    while (m < n) m <<= 1;
+    uint32_t* s = buf[warp];
+    for (uint32_t i = lane; i < m; i += 32) s[i] = i < n ? unsorted[b + i] : 0xffffffffu;
+    __syncwarp();
+    for (uint32_t k = 2; k <= m; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < m; i += 32) {
+                const uint32_t l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = s[i], c = s[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > c) == up) {
+                        s[i] = c;
+                        s[l] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    for (uint32_t i = lane; i < n; i += 32) sorted[b + i] = s[i];
+}
+
+// Pass 3b: tiles with more than kSmallSort entries. Triangle ids inside a tile are distinct, so a
+// bitmap over an id window orders them; windows ascend over [min id, max id] of the tile.
+__global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ unsorted,
+                                      uint32_t* __restrict__ sorted, const uint32_t* __restrict__ large_queue,
+                                      const uint32_t* __restrict__ status, unsigned long long capacity) {
+    __shared__ uint32_t bitmap[kWindowBits / 32];
+    __shared__ unsigned int lo_s, hi_s;
+    const uint32_t count = status[kStatusLargeTiles];
+    for (uint32_t q = blockIdx.x; q < count; q += gridDim.x) {
+        const uint32_t seg = large_queue[q];
+        const uint32_t b = offsets[seg];
+        uint32_t e = offsets[seg + 1];
+        if (e > capacity) e = (uint32_t)capacity;
+        if (threadIdx.x == 0) {
+            lo_s = 0xffffffffu;
+            hi_s = 0u;
+        }
+        __syncthreads();
+        uint32_t lo = 0xffffffffu, hi = 0u;
+        for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+            const uint32_t v = unsorted[i];
+            lo = v < lo ? v : lo;
+            hi = v > hi ? v : hi;
+        }
+        atomicMin(&lo_s, lo);
+        atomicMax(&hi_s, hi);
+        __syncthreads();
+        const uint32_t first = lo_s, last = hi_s;
+        uint32_t written = 0;
+        for (unsigned long long w0 = first; w0 <= last; w0 += kWindowBits) {
+            for (uint32_t i = threadIdx.x; i < kWindowBits / 32; i += blockDim.x) bitmap[i] = 0u;
+            __syncthreads();
+            for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+                const unsigned long long v = unsorted[i];
+                if (v >= w0 && v < w0 + kWindowBits) {
+                    const uint32_t o = (uint32_t)(v - w0);
+                    atomicOr(&bitmap[o >> 5], 1u << (o & 31u));
+                }
+            }
+            __syncthreads();
+            // each thread owns a contiguous run of words
+            const uint32_t words = kWindowBits / 32;
+            const uint32_t per = (words + blockDim.x - 1) / blockDim.x;
+            const uint32_t w_begin = threadIdx.x * per;
+            uint32_t cnt = 0;
+            for (uint32_t w = w_begin; w < w_begin + per && w < words; ++w) cnt += __popc(bitmap[w]);
+            unsigned long long total;
+            const uint32_t pre = (uint32_t)block_exclusive_u64(cnt, &total);
+            uint32_t outp = b + written + pre;
+            for (uint32_t w = w_begin; w < w_begin + per && w < words; ++w) {
+                uint32_t bits = bitmap[w];
+                while (bits) {
+                    const int bit = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    sorted[outp++] = (uint32_t)(w0 + w * 32u + (uint32_t)bit);
+                }
+            }
+            written += (uint32_t)total;
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+}
+
+// ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ----------------------------
+
+struct TriSetup {
+    float s0x, s0y, s1x, s1y, s2x, s2y;
+    float4 p0, p1, p2;
+    float sign;  // coverage sign, or 0 when the triangle is skipped for every pixel
+    uint32_t t;
+};
+
+constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA
+
+template <bool kDeriv>
+__global__ void __launch_bounds__(kRasterThreads)
+raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
+                      uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
+                      uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
+                      const uint32_t* __restrict__ list, unsigned long long capacity, float4* __restrict__ raster,
+                      float4* __restrict__ deriv) {
+    __shared__ TriSetup tri[kRasterThreads];
+    const uint32_t view = blockIdx.y;
+    const uint32_t tile = blockIdx.x;
+    const float4* __restrict__ clip = clip_all + (size_t)view * V;
+    const float4 vp = viewports[view];
+    const uint32_t px = (tile % tcx) * kTile + (threadIdx.x & 15u);
+    const uint32_t py = (tile / tcx) * kTile + (threadIdx.x >> 4);
+    const float sx = sample_ndc(px, vp.x, vp.z);
+    const float sy = sample_ndc(py, vp.y, vp.w);
+    const uint32_t seg = view * tiles + tile;
+    const uint32_t b = offsets[seg];
+    uint32_t e = offsets[seg + 1];
+    if (e > capacity) e = (uint32_t)capacity;
+    if (b > e) e = b;
+
+    float best_depth = 3.402823466e+38f;
+    uint32_t best_tri = 0;
+    float bb0 = 0.0f, bb1 = 0.0f, binv = 0.0f;
+    for (uint32_t chunk = b; chunk < e; chunk += kRasterThreads) {
+        __syncthreads();
+        const uint32_t i = chunk + threadIdx.x;
+        if (i < e) {
+            TriSetup s;
+            s.t = list[i];
+            s.sign = 0.0f;
+            const uint3 vi = idx[s.t];
+            if (vi.x < V && vi.y < V && vi.z < V) {
+                s.p0 = clip[vi.x];
+                s.p1 = clip[vi.y];
+                s.p2 = clip[vi.z];
+                if (!(s.p0.w <= 1e-8f || s.p1.w <= 1e-8f || s.p2.w <= 1e-8f)) {
+                    s.s0x = s.p0.x / s.p0.w; s.s0y = s.p0.y / s.p0.w;
+                    s.s1x = s.p1.x / s.p1.w; s.s1y = s.p1.y / s.p1.w;
+                    s.s2x = s.p2.x / s.p2.w; s.s2y = s.p2.y / s.p2.w;
+                    const float area = cross2(s.s1x - s.s0x, s.s1y - s.s0y, s.s2x - s.s0x, s.s2y - s.s0y);
+                    const bool skip = fabsf(area) <= 1e-12f || (cull == 1 && area <= 0.0f) || (cull == 2 && area >= 0.0f);
+                    if (!skip) s.sign = area > 0.0f ? 1.0f : -1.0f;
+                }
+            }
+            tri[threadIdx.x] = s;
+        }
+        __syncthreads();
+        const uint32_t n = min(e - chunk, (uint32_t)kRasterThreads);
+        for (uint32_t j = 0; j < n; ++j) {
+            const TriSetup& s = tri[j];
+            if (s.sign == 0.0f) continue;
+            const float e0 = cross2(s.s1x - sx, s.s1y - sy, s.s2x - sx, s.s2y - sy);
+            const float e1 = cross2(s.s2x - sx, s.s2y - sy, s.s0x - sx, s.s0y - sy);
+            const float e2 = cross2(s.s0x - sx, s.s0y - sy, s.s1x - sx, s.s1y - sy);
+            const float ceps = -1e-7f;
+            if (e0 * s.sign < ceps || e1 * s.sign < ceps || e2 * s.sign < ceps) continue;
+            const float q0x = s.p0.x - sx * s.p0.w, q0y = s.p0.y - sy * s.p0.w;
+            const float q1x = s.p1.x - sx * s.p1.w, q1y = s.p1.y - sy * s.p1.w;
+            const float q2x = s.p2.x - sx * s.p2.w, q2y = s.p2.y - sy * s.p2.w;
+            const float a0 = cross2(q1x, q1y, q2x, q2y);
+            const float a1 = cross2(q2x, q2y, q0x, q0y);
+            const float a2 = cross2(q0x, q0y, q1x, q1y);
+            const float ha = a0 + a1 + a2;
+            if (fabsf(ha) <= 1e-12f) continue;
+            const float inv = 1.0f / ha;
+            const float iz = s.p0.z * a0 + s.p1.z * a1 + s.p2.z * a2;
+            const float iw = s.p0.w * a0 + s.p1.w * a1 + s.p2.w * a2;
+            if (fabsf(iw) <= 1e-12f) continue;
+            const float depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
+            // nearest depth wins; ties go to the lowest triangle id (rasterize_forward.hlsl:136-140)
+            if (depth > best_depth || (depth == best_depth && best_tri != 0 && s.t + 1 >= best_tri)) continue;
+            best_depth = depth;
+            best_tri = s.t + 1;
+            bb0 = clamp_hlsl(a0 * inv, 0.0f, 1.0f);
+            bb1 = clamp_hlsl(a1 * inv, 0.0f, 1.0f);
+            binv = inv;
+        }
+    }
+    if (px >= W || py >= H) return;
+    const size_t pix = ((size_t)view * H + py) * W + px;
+    if (best_tri == 0) {
+        raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (kDeriv) deriv[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
+    if (kDeriv) {
+        const uint3 vi = idx[best_tri - 1];
+        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+        const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
+        const float da0_dy = -p1.x * p2.w + p1.w * p2.x;
+        const float da1_dx = -p2.w * p0.y + p2.y * p0.w;
+        const float da1_dy = -p2.x * p0.w + p2.w * p0.x;
+        const float da2_dx = -p0.w * p1.y + p0.y * p1.w;
+        const float da2_dy = -p0.x * p1.w + p0.w * p1.x;
+        const float dadx = da0_dx + da1_dx + da2_dx;
+        const float dady = da0_dy + da1_dy + da2_dy;
+        deriv[pix] = make_float4((da0_dx - bb0 * dadx) * binv * 2.0f / vp.z, (da0_dy - bb0 * dady) * binv * 2.0f / vp.w,
+                                 (da1_dx - bb1 * dadx) * binv * 2.0f / vp.z, (da1_dy - bb1 * dady) * binv * 2.0f / vp.w);
+    }
+}
+
+// ---- rasterize backward: shaders/rasterize_backward.hlsl:36-158 -------------------------
+// One thread per pixel. A pixel contributes to triangle t exactly when the reference's
+// per-triangle loop would visit it: raster id == t+1, inside t's clamped pixel bounds
+// (rasterize_backward.hlsl:78-90) and a non-zero (u, v) gradient. Corner sums use atomics.
+__global__ void raster_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
+                                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports,
+                                       const float4* __restrict__ raster, const float4* __restrict__ grad_raster,
+                                       float* __restrict__ grad_clip) {
+    const uint32_t view = blockIdx.y;
+    const size_t P = (size_t)W * H;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const size_t pix = (size_t)view * P + p;
+    const float rw = raster[pix].w;
+    const uint32_t id = raster_id(rw);
+    if (id == 0 || id > T) return;
+    const float4 g = grad_raster[pix];
+    if (g.x == 0.0f && g.y == 0.0f) return;
+    const uint3 vi = idx[id - 1];
+    if (vi.x >= V || vi.y >= V || vi.z >= V) return;
+    const float4* __restrict__ clip = clip_all + (size_t)view * V;
+    const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+    if (p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f) return;
+    const float4 vp = viewports[view];
+    const uint32_t x = (uint32_t)(p % W), y = (uint32_t)(p / W);
+    {
+        const float s0x = p0.x / p0.w, s0y = p0.y / p0.w;
+        const float s1x = p1.x / p1.w, s1y = p1.y / p1.w;
+        const float s2x = p2.x / p2.w, s2y = p2.y / p2.w;
+        const float mnx = fminf(s0x, fminf(s1x, s2x)), mny = fminf(s0y, fminf(s1y, s2y));
+        const float mxx = fmaxf(s0x, fmaxf(s1x, s2x)), mxy = fmaxf(s0y, fmaxf(s1y, s2y));
+        const int32_t x0 = clampi(f2i_sat(floorf((mnx * 0.5f + 0.5f) * vp.z + vp.x)), 0, (int32_t)W);
+        const int32_t x1 = clampi(f2i_sat(ceilf((mxx * 0.5f + 0.5f) * vp.z + vp.x)), 0, (int32_t)W);
+        const int32_t y0 = clampi(f2i_sat(floorf((mny * 0.5f + 0.5f) * vp.w + vp.y)), 0, (int32_t)H);
+        const int32_t y1 = clampi(f2i_sat(ceilf((mxy * 0.5f + 0.5f) * vp.w + vp.y)), 0, (int32_t)H);
+        if ((int32_t)x < x0 || (int32_t)x >= x1 || (int32_t)y < y0 || (int32_t)y >= y1) return;
+    }
+    const float sx = sample_ndc(x, vp.x, vp.z);
+    const float sy = sample_ndc(y, vp.y, vp.w);
+    const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+    const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+    const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+    const float area = cross2(q1x, q1y, q2x, q2y) + cross2(q2x, q2y, q0x, q0y) + cross2(q0x, q0y, q1x, q1y);
+    if (fabsf(area) <= 1e-12f) return;
+    const float eps = area >= 0.0f ? 1e-6f : -1e-6f;
+    const float inv = 1.0f / (area + eps);
+    const float a0 = cross2(q1x, q1y, q2x, q2y);
+    const float a1 = cross2(q2x, q2y, q0x, q0y);
+    const float b0 = a0 * inv, b1 = a1 * inv;
+    const float gb0 = g.x * inv, gb1 = g.y * inv;
+    const float gc = gb0 * b0 + gb1 * b1;
+    const float g0x = gc * (q2y - q1y) - gb1 * q2y;
+    const float g1x = gc * (q0y - q2y) + gb0 * q2y;
+    const float g2x = gc * (q1y - q0y) - gb0 * q1y + gb1 * q0y;
+    const float g0y = gc * (q1x - q2x) + gb1 * q2x;
+    const float g1y = gc * (q2x - q0x) - gb0 * q2x;
+    const float g2y = gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x;
+    float* gv = grad_clip + (size_t)view * V * 4;
+    atomicAdd(gv + (size_t)vi.x * 4 + 0, g0x);
+    atomicAdd(gv + (size_t)vi.x * 4 + 1, g0y);
+    atomicAdd(gv + (size_t)vi.x * 4 + 3, -sx * g0x - sy * g0y);
+    atomicAdd(gv + (size_t)vi.y * 4 + 0, g1x);
+    atomicAdd(gv + (size_t)vi.y * 4 + 1, g1y);
+    atomicAdd(gv + (size_t)vi.y * 4 + 3, -sx * g1x - sy * g1y);
+    atomicAdd(gv + (size_t)vi.z * 4 + 0, g2x);
+    atomicAdd(gv + (size_t)vi.z * 4 + 1, g2y);
+    atomicAdd(gv + (size_t)vi.z * 4 + 3, -sx * g2x - sy * g2y);
+}
+
+}  // namespace
+
+// ---- host launchers -----------------------------------------------------------------------
+
+size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity) {
+    const size_t tiles = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+    const size_t segs = tiles * views;
+    const size_t nblocks = (segs + 1 + kScanBlock - 1) / kScanBlock;
+    size_t bytes = 0;
+    bytes += align_up((size_t)views * T * sizeof(TriRect));  // rects
+    bytes += align_up((segs + 1) * sizeof(uint32_t));          // counts
+    bytes += align_up((segs + 1) * sizeof(uint32_t));          // cursor
+    bytes += align_up(nblocks * sizeof(unsigned long long));   // scan block sums
+    bytes += align_up(segs * sizeof(uint32_t));                // large-tile queue
+    bytes += align_up((size_t)capacity * sizeof(uint32_t));    // unsorted list
+    return bytes;
+}
+
+cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
+                             uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
+                             unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream) {
+    const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
+    const uint32_t tiles = tcx * tcy;
+    const size_t segs = (size_t)tiles * views;
+    const uint32_t nblocks = (uint32_t)((segs + 1 + kScanBlock - 1) / kScanBlock);
+    char* ws = static_cast<char*>(workspace);
+    TriRect* rects = reinterpret_cast<TriRect*>(ws);
+    ws += align_up((size_t)views * T * sizeof(TriRect));
+    uint32_t* counts = reinterpret_cast<uint32_t*>(ws);
+    ws += align_up((segs + 1) * sizeof(uint32_t));
+    uint32_t* cursor = reinterpret_cast<uint32_t*>(ws);
+    ws += align_up((segs + 1) * sizeof(uint32_t));
+    unsigned long long* block_sums = reinterpret_cast<unsigned long long*>(ws);
+    ws += align_up((size_t)nblocks * sizeof(unsigned long long));
+    uint32_t* large_queue = reinterpret_cast<uint32_t*>(ws);
+    ws += align_up(segs * sizeof(uint32_t));
+    uint32_t* unsorted = reinterpret_cast<uint32_t*>(ws);
+
+    cudaError_t err = cudaMemsetAsync(counts, 0, (segs + 1) * sizeof(uint32_t), stream);
+    if (err != cudaSuccess) return err;
+    const dim3 tgrid((T + 255) / 256, views);
+    bin_count_kernel<<<tgrid, 256, 0, stream>>>(reinterpret_cast<const float4*>(clip), V,
+                                                reinterpret_cast<const uint3*>(idx), T, W, H,
+                                                reinterpret_cast<const float4*>(viewports), tcx, tiles, rects, counts);
+    scan_local_kernel<<<nblocks, kScanThreads, 0, stream>>>(counts, (uint32_t)segs, offsets, block_sums);
+    scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(block_sums, nblocks, offsets, (uint32_t)segs, status, capacity);
+    scan_add_kernel<<<nblocks, kScanThreads, 0, stream>>>(offsets, (uint32_t)segs, block_sums, cursor);
+    bin_fill_kernel<<<tgrid, 256, 0, stream>>>(rects, T, tcx, tiles, cursor, unsorted, capacity);
+    bin_sort_small_kernel<<<(uint32_t)((segs + 7) / 8), 256, 0, stream>>>(offsets, (uint32_t)segs, unsorted, list,
+                                                                           large_queue, status, capacity);
+    bin_sort_large_kernel<<<num_sms() * 2, 512, 0, stream>>>(offsets, unsorted, list, large_queue, status, capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
+                                  uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
+                                  const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
+                                  float* raster, float* deriv, cudaStream_t stream) {
+    const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
+    const dim3 grid(tcx * tcy, views);
+    if (deriv) {
+        raster_forward_kernel<true><<<grid, kRasterThreads, 0, stream>>>(
+            reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
+            reinterpret_cast<const float4*>(viewports), cull, tcx, tcx * tcy, offsets, list, capacity,
+            reinterpret_cast<float4*>(raster), reinterpret_cast<float4*>(deriv));
+    } else {
+        raster_forward_kernel<false><<<grid, kRasterThreads, 0, stream>>>(
+            reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
+            reinterpret_cast<const float4*>(viewports), cull, tcx, tcx * tcy, offsets, list, capacity,
+            reinterpret_cast<float4*>(raster), nullptr);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
+                                   uint32_t W, uint32_t H, const float* viewports, const float* raster,
+                                   const float* grad_raster, float* grad_clip, cudaStream_t stream) {
+    cudaError_t err = cudaMemsetAsync(grad_clip, 0, (size_t)views * V * 4 * sizeof(float), stream);
+    if (err != cudaSuccess) return err;
+    const size_t P = (size_t)W * H;
+    const dim3 grid((uint32_t)((P + 255) / 256), views);
+    raster_backward_kernel<<<grid, 256, 0, stream>>>(
+        reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
+        reinterpret_cast<const float4*>(viewports), reinterpret_cast<const float4*>(raster),
+        reinterpret_cast<const float4*>(grad_raster), grad_clip);
+    return cudaGetLastError();
+}
+
+}  // namespace pdr
