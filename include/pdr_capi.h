@@ -108,6 +108,16 @@ PDR_API pdr_status pdr_interpolate_backward(const float* attributes, uint64_t at
                                             uint32_t views, uint64_t pixels_per_view, const float* grad_interpolated,
                                             float* grad_attributes, float* grad_raster, void* stream);
 
+/* As pdr_interpolate_backward, but grad_raster is accumulated into (+=) instead of overwritten, so the
+ * raster gradients of several interpolations of one raster sum in place (what autograd does when
+ * one raster feeds several interpolate() calls, python/photara_drender/torch.py:121-123). */
+PDR_API pdr_status pdr_interpolate_backward_accumulate(const float* attributes, uint64_t attribute_view_stride,
+                                                       uint32_t vertex_count, uint32_t attribute_count,
+                                                       const uint32_t* indices, uint32_t triangle_count,
+                                                       const float* raster, uint32_t views, uint64_t pixels_per_view,
+                                                       const float* grad_interpolated, float* grad_attributes,
+                                                       float* grad_raster, void* stream);
+
 /* Rasterizer::texture_forward (src/rasterizer.cpp:685-735 + shaders/texture_forward.hlsl).
  * address_mode: 0 clamp, 1 wrap, 2 mirror (types.hpp AddressMode). */
 PDR_API pdr_status pdr_texture_forward(const float* texture, uint64_t texture_view_stride, uint32_t texture_width,
@@ -124,6 +134,109 @@ PDR_API pdr_status pdr_texture_backward(const float* texture, uint64_t texture_v
                                         const float* uv, const float* raster, uint32_t views,
                                         uint64_t pixels_per_view, const float* grad_sampled, float* grad_texture,
                                         float* grad_uv, uint32_t* status, void* stream);
+
+
+/* ---- bake: src/texture_baker.cpp + shaders/project_texture.hlsl ------------------------------ */
+
+/* One projection view (types.hpp ProjectionView plus the device buffers the projection reads).
+ * 160 bytes; the array passed to pdr_project_views lives in device memory. */
+typedef struct {
+    float world_to_clip[16];     /* row-major, clip = M [p, 1] */
+    float camera_position[3];
+    float weight;                /* ProjectionView::weight (times the softmax scale when blending softmax) */
+    float viewport[4];           /* x, y, width, height in image pixels */
+    uint32_t width, height, channel_count, has_mask;
+    float depth_bias, min_view_cosine, mask_floor, reserved;
+    const float* image;          /* [height][width][channel_count] */
+    const float* visibility_mask;/* [height][width] when has_mask */
+    const float* shadow_raster;  /* [height][width][4] raster of this view (visibility modes 0 and 1) */
+    const float* ray_visibility; /* [atlas texels] visibility for modes 1 and 2, or NULL for 1.0 */
+} pdr_projection_view;
+
+/* texture_baker.cpp:92-106: clip [views][V][4] = world_to_clip[views] (row-major 4x4) * [p, 1]. */
+PDR_API pdr_status pdr_transform_positions(const float* positions, uint32_t vertex_count, const float* world_to_clip,
+                                           uint32_t views, float* clip_positions, void* stream);
+/* texture_baker.cpp:81-90: clip [V][4] = (2u - 1, 2v - 1, 0, 1). */
+PDR_API pdr_status pdr_atlas_clip_positions(const float* uv, uint32_t vertex_count, float* clip_positions,
+                                            void* stream);
+/* All views of a bake in one launch (project_texture.hlsl per view, in view order, per atlas texel)
+ * with the host normalisation of texture_baker.cpp:334-358 fused: color [N][4] (rgb, valid),
+ * confidence [N], source_view [N] (UINT32_MAX when unseen), valid_mask [N], coverage_mask [N] and
+ * face_ids [N] (the last two may be NULL). blend_mode: 0 best_view, 1 weighted_average, 2 softmax;
+ * visibility_mode: 0 shadow map, 1 ray visibility times shadow map, 2 ray visibility. */
+PDR_API pdr_status pdr_project_views(const float* atlas_positions, const float* atlas_normals, const float* atlas_raster,
+                                     uint32_t atlas_texels, const pdr_projection_view* views, uint32_t view_count,
+                                     uint32_t blend_mode, uint32_t pcf_radius, uint32_t visibility_mode, float* color,
+                                     float* confidence, uint32_t* source_view, float* valid_mask, float* coverage_mask,
+                                     uint32_t* face_ids, void* stream);
+
+/* ---- refine: src/texture_refiner.cpp + atlas_* shaders ---------------------------------------- */
+
+/* Cached per-view refinement inputs (texture_refiner.cpp:79-85), device pointers; 32 bytes. */
+typedef struct {
+    const float* uv;      /* [P][2] interpolated atlas uv */
+    const float* target;  /* [P][3] */
+    const float* mask;    /* [P] */
+    uint64_t pixel_count;
+} pdr_refine_view;
+
+/* types.hpp TextureRefineOptions plus the optional chart-aware total variation term
+ * (python/photara_drender/atlas.py:84-115): tv_scale = weight / (valid pairs * 3), 0 disables. */
+typedef struct {
+    uint32_t width, height, steps, batch_size;
+    float learning_rate, minimum_learning_rate, photometric_epsilon;
+    float adam_beta1, adam_beta2, adam_epsilon, clamp_min, clamp_max;
+    uint32_t seam_polish_steps;
+    float seam_learning_rate, seam_epsilon;
+    float tv_scale, tv_epsilon;
+} pdr_refine_options;
+
+/* texture_refiner.cpp:228-242 for one view: target [P][3] and mask [P] from the image and raster. */
+PDR_API pdr_status pdr_refine_prepare_view(const float* image, uint32_t channel_count, const float* visibility_mask,
+                                           const float* raster, uint64_t pixel_count, float* target, float* mask,
+                                           void* stream);
+/* One photometric dispatch set (all batch views of `step`) accumulating into gradient and loss[step]. */
+PDR_API pdr_status pdr_refine_photometric(const float* texture, uint32_t width, uint32_t height,
+                                          const pdr_refine_view* views, uint32_t view_count,
+                                          uint64_t max_view_pixels, uint32_t step, uint32_t batch_size,
+                                          float epsilon, float normalization, float* gradient, float* loss_history,
+                                          void* stream);
+PDR_API pdr_status pdr_refine_seam(const float* texture, uint32_t width, uint32_t height, const float* seam_uv_pairs,
+                                   uint32_t pair_count, float epsilon, float normalization, float* gradient,
+                                   float* loss_history, uint32_t loss_index, void* stream);
+PDR_API pdr_status pdr_refine_total_variation(const float* texture, uint32_t width, uint32_t height,
+                                              const uint8_t* valid, const int32_t* chart_ids, float epsilon,
+                                              float scale, float* gradient, void* stream);
+PDR_API pdr_status pdr_refine_adam(float* texture, float* gradient, float* moment1, float* moment2, uint64_t count,
+                                   float learning_rate, float beta1, float beta2, float epsilon,
+                                   float bias_correction1, float bias_correction2, float clamp_min, float clamp_max,
+                                   void* stream);
+/* The per-step learning rate and bias corrections of texture_refiner.cpp:343-353, in float. */
+PDR_API pdr_status pdr_refine_schedule(const pdr_refine_options* options, uint32_t step, float* learning_rate,
+                                       float* bias_correction1, float* bias_correction2);
+
+/* The whole TextureRefiner::refine optimisation (texture_refiner.cpp:256-415): `steps` photometric
+ * + Adam steps with the cosine learning rate, then (when pair_count > 0) the seam polish with reset
+ * moments. view_valid_weights is a host array of the views' valid weights (double, as the reference
+ * keeps them); texture is updated in place; gradient/moment buffers are overwritten;
+ * loss_history has steps + seam steps floats. With use_graph != 0 the sequence is recorded once
+ * into a CUDA graph and launched as a single unit. */
+PDR_API pdr_status pdr_refine_run(const pdr_refine_options* options, const pdr_refine_view* views, uint32_t view_count,
+                                  const double* view_valid_weights, uint64_t max_view_pixels,
+                                  const float* seam_uv_pairs, uint32_t pair_count, const uint8_t* tv_valid,
+                                  const int32_t* tv_chart_ids, float* texture, float* gradient, float* moment1,
+                                  float* moment2, float* loss_history, int32_t use_graph, void* stream);
+
+/* A recorded refinement (same arguments as pdr_refine_run) that can be launched many times. */
+typedef struct pdr_refine_graph_t* pdr_refine_graph;
+PDR_API pdr_status pdr_refine_graph_create(pdr_refine_graph* graph, const pdr_refine_options* options,
+                                           const pdr_refine_view* views, uint32_t view_count,
+                                           const double* view_valid_weights, uint64_t max_view_pixels,
+                                           const float* seam_uv_pairs, uint32_t pair_count, const uint8_t* tv_valid,
+                                           const int32_t* tv_chart_ids, float* texture, float* gradient,
+                                           float* moment1, float* moment2, float* loss_history, void* stream);
+PDR_API pdr_status pdr_refine_graph_launch(pdr_refine_graph graph, void* stream);
+PDR_API pdr_status pdr_refine_graph_destroy(pdr_refine_graph graph);
 
 #ifdef __cplusplus
 }

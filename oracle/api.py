@@ -114,7 +114,7 @@ def rasterize_forward_f64(pos, idx, raster, viewport=None):
     return r64
 
 
-def rasterize_backward(pos, idx, raster, grad_raster, viewport=None, f64=False):
+def rasterize_backward(pos, idx, raster, grad_raster, viewport=None, f64=False, abs_terms=False):
     pos, idx, raster, grad_raster = _f(pos), _u(idx), _f(raster), _f(grad_raster)
     h, w = raster.shape[:2]
     vp = _vp(viewport, w, h)
@@ -124,8 +124,9 @@ def rasterize_backward(pos, idx, raster, grad_raster, viewport=None, f64=False):
     else:
         out = np.zeros((pos.shape[0], 4), dtype=np.float32)
         fn, t = lib().ora_rasterize_backward, _f32p
+    extra = (int(abs_terms),) if f64 else ()
     _check(fn(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp), _p(raster), _p(grad_raster),
-              _p(out, t)))
+              _p(out, t), *extra))
     return out
 
 
@@ -141,7 +142,7 @@ def interpolate_forward(attr, idx, raster):
     return out
 
 
-def interpolate_backward(attr, idx, raster, grad, f64=False):
+def interpolate_backward(attr, idx, raster, grad, f64=False, abs_terms=False):
     attr, idx, raster, grad = _f(attr), _u(idx), _f(raster), _f(grad)
     h, w = raster.shape[:2]
     V, A = attr.shape
@@ -149,8 +150,9 @@ def interpolate_backward(attr, idx, raster, grad, f64=False):
     ga = np.zeros((V, A), dtype=dt)
     gr = np.zeros((h, w, 4), dtype=dt)
     fn = lib().ora_interpolate_backward_f64 if f64 else lib().ora_interpolate_backward
+    extra = (int(abs_terms),) if f64 else ()
     _check(fn(_p(attr), V, A, _p(idx, _u32p), idx.shape[0], _p(raster), C.c_uint64(h * w), _p(grad), _p(ga, t),
-              _p(gr, t)))
+              _p(gr, t), *extra))
     return ga, gr
 
 
@@ -169,7 +171,8 @@ def texture_forward(tex, uv, raster, address_mode="clamp"):
     return out
 
 
-def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gradient=True, f64=False):
+def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gradient=True, f64=False,
+                     abs_terms=False):
     tex, uv, raster, grad = _f(tex), _f(uv), _f(raster), _f(grad)
     th, tw, Cc = tex.shape
     h, w = raster.shape[:2]
@@ -177,8 +180,9 @@ def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gra
     gt = np.zeros(tex.shape, dtype=dt)
     gu = np.zeros((h, w, 2), dtype=dt) if compute_uv_gradient else None
     fn = lib().ora_texture_backward_f64 if f64 else lib().ora_texture_backward
+    extra = (int(abs_terms),) if f64 else ()
     _check(fn(_p(tex), tw, th, Cc, ADDRESS[address_mode], _p(uv), _p(raster), C.c_uint64(h * w), _p(grad),
-              _p(gt, t), _p(gu, t)))
+              _p(gt, t), _p(gu, t), *extra))
     return gt, gu
 
 

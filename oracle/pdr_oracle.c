@@ -314,6 +314,8 @@ int ora_rasterize_forward_f64(const float* pos, uint32_t V, const uint32_t* idx,
 /* ---- rasterize backward: rasterize_backward.hlsl:36-158, reduce_vertex_gradients.hlsl,
  *      rasterizer.cpp:145-162 (vertex CSR over corners, ascending corner order) ---------- */
 
+/* ACC(x) is the identity, or |x| in the FP64 twins' abs_terms mode (sum of absolute terms,
+ * the scale against which summation-order error is stated). */
 #define RB_BODY(REAL, CROSS, EPS_AREA, SAMPLE)                                                       \
     for (uint32_t t = 0; t < T; ++t) {                                                               \
         REAL g[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};                                  \
@@ -358,9 +360,9 @@ int ora_rasterize_forward_f64(const float* pos, uint32_t V, const uint32_t* idx,
                         const REAL g0y = gc * (q1x - q2x) + gb1 * q2x;                               \
                         const REAL g1y = gc * (q2x - q0x) - gb0 * q2x;                               \
                         const REAL g2y = gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x;                   \
-                        g[0][0] += g0x; g[0][1] += g0y; g[0][2] += (REAL)0; g[0][3] += -sx * g0x - sy * g0y; \
-                        g[1][0] += g1x; g[1][1] += g1y; g[1][2] += (REAL)0; g[1][3] += -sx * g1x - sy * g1y; \
-                        g[2][0] += g2x; g[2][1] += g2y; g[2][2] += (REAL)0; g[2][3] += -sx * g2x - sy * g2y; \
+                        g[0][0] += ACC(g0x); g[0][1] += ACC(g0y); g[0][2] += (REAL)0; g[0][3] += ACC(-sx * g0x - sy * g0y); \
+                        g[1][0] += ACC(g1x); g[1][1] += ACC(g1y); g[1][2] += (REAL)0; g[1][3] += ACC(-sx * g1x - sy * g1y); \
+                        g[2][0] += ACC(g2x); g[2][1] += ACC(g2y); g[2][2] += (REAL)0; g[2][3] += ACC(-sx * g2x - sy * g2y); \
                     }                                                                                \
                 }                                                                                    \
             }                                                                                        \
@@ -389,7 +391,9 @@ int ora_rasterize_backward(const float* pos, uint32_t V, const uint32_t* idx, ui
     if (rc) return rc;
     float* corner = (float*)malloc((size_t)T * 12 * sizeof(float));
 #define SAMPLE_F sx = sample_ndc((uint32_t)x, vp[0], vp[2]); sy = sample_ndc((uint32_t)y, vp[1], vp[3])
+#define ACC(x) (x)
     RB_BODY(float, cross2, 1e-6f, SAMPLE_F)
+#undef ACC
     uint32_t *off, *corners;
     vertex_csr(idx, T, V, &off, &corners);
     for (uint32_t v = 0; v < V; ++v) {
@@ -406,12 +410,14 @@ int ora_rasterize_backward(const float* pos, uint32_t V, const uint32_t* idx, ui
 
 int ora_rasterize_backward_f64(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
                                uint32_t W, uint32_t H, const float vp[4], const float* raster,
-                               const float* grad_raster, double* grad_pos) {
+                               const float* grad_raster, double* grad_pos, int abs_terms) {
     int rc = validate_mesh(pos, V, idx, T);
     if (rc) return rc;
     double* corner = (double*)malloc((size_t)T * 12 * sizeof(double));
 #define SAMPLE_D sx = ((double)x - vp[0] + 0.5) * 2.0 / vp[2] - 1.0; sy = ((double)y - vp[1] + 0.5) * 2.0 / vp[3] - 1.0
+#define ACC(x) (abs_terms ? fabs(x) : (x))
     RB_BODY(double, cross2d, 1e-6f, SAMPLE_D)
+#undef ACC
     uint32_t *off, *corners;
     vertex_csr(idx, T, V, &off, &corners);
     for (uint32_t v = 0; v < V; ++v) {
@@ -475,7 +481,7 @@ int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uin
             if (i0 == vx) wgt += (REAL)u;                                                            \
             if (i1 == vx) wgt += (REAL)v;                                                            \
             if (i2 == vx) wgt += (REAL)1 - (REAL)u - (REAL)v;                                        \
-            for (uint32_t a = 0; a < A; ++a) grad_attr[(uint64_t)vx * A + a] += wgt * (REAL)grad_out[p * A + a]; \
+            for (uint32_t a = 0; a < A; ++a) grad_attr[(uint64_t)vx * A + a] += ACC(wgt * (REAL)grad_out[p * A + a]); \
         }                                                                                            \
         if (i0 < V && i1 < V && i2 < V) {                                                            \
             REAL gx = 0, gy = 0;                                                                     \
@@ -494,14 +500,18 @@ int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uin
 int ora_interpolate_backward(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
                              uint32_t T, const float* raster, uint64_t P, const float* grad_out,
                              float* grad_attr, float* grad_raster) {
+#define ACC(x) (x)
     IB_BODY(float)
+#undef ACC
     return ORA_OK;
 }
 
 int ora_interpolate_backward_f64(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
                                  uint32_t T, const float* raster, uint64_t P, const float* grad_out,
-                                 double* grad_attr, double* grad_raster) {
+                                 double* grad_attr, double* grad_raster, int abs_terms) {
+#define ACC(x) (abs_terms ? fabs(x) : (x))
     IB_BODY(double)
+#undef ACC
     return ORA_OK;
 }
 
@@ -554,7 +564,7 @@ int ora_texture_forward(const float* tex, uint32_t tw, uint32_t th, uint32_t C, 
         const uint64_t tx4[4] = {(uint64_t)ys[0] * tw + xs[0], (uint64_t)ys[0] * tw + xs[1],        \
                                  (uint64_t)ys[1] * tw + xs[0], (uint64_t)ys[1] * tw + xs[1]};        \
         for (int k = 0; k < 4; ++k)                                                                  \
-            for (uint32_t c = 0; c < C; ++c) grad_tex[tx4[k] * C + c] += w[k] * (REAL)grad[p * C + c]; \
+            for (uint32_t c = 0; c < C; ++c) grad_tex[tx4[k] * C + c] += ACC(w[k] * (REAL)grad[p * C + c]); \
     }                                                                                                \
     if (grad_uv) {                                                                                   \
         for (uint64_t p = 0; p < P; ++p) {                                                           \
@@ -593,19 +603,23 @@ int ora_texture_backward(const float* tex, uint32_t tw, uint32_t th, uint32_t C,
     if (rc) return rc;
 #define UVPOS tx = uv[p * 2] * (float)tw - 0.5f; ty = uv[p * 2 + 1] * (float)th - 0.5f; \
     bx = f2i_sat(floorf(tx)); by = f2i_sat(floorf(ty)); fx = tx - floorf(tx); fy = ty - floorf(ty)
+#define ACC(x) (x)
     TB_BODY(float)
+#undef ACC
 #undef UVPOS
     return ORA_OK;
 }
 
 int ora_texture_backward_f64(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
                              const float* uv, const float* raster, uint64_t P, const float* grad,
-                             double* grad_tex, double* grad_uv) {
+                             double* grad_tex, double* grad_uv, int abs_terms) {
     int rc = texture_validate(tw, th, C);
     if (rc) return rc;
 #define UVPOS tx = (double)uv[p * 2] * tw - 0.5; ty = (double)uv[p * 2 + 1] * th - 0.5; \
     bx = d2i_sat(floor(tx)); by = d2i_sat(floor(ty)); fx = tx - floor(tx); fy = ty - floor(ty)
+#define ACC(x) (abs_terms ? fabs(x) : (x))
     TB_BODY(double)
+#undef ACC
 #undef UVPOS
     return ORA_OK;
 }

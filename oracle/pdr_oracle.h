@@ -7,7 +7,8 @@
  * Every function restates one routine of the reference (fenghuayumo/photara_drender
  * v0.4.0) in plain C with the same fp32 operation order, compiled with
  * -ffp-contract=off so no multiply-add is fused. The "_f64" functions are FP64
- * twins used only to state the error of fp32 results.
+ * twins used only to state the error of fp32 results; with abs_terms they accumulate |term|
+ * instead (the sum of absolute terms that bounds summation-order error).
  *
  * Return codes mirror the reference's exception types:
  *   0 ok, -1 std::invalid_argument, -2 std::out_of_range, -3 std::overflow_error.
@@ -49,7 +50,7 @@ int ora_rasterize_backward(const float* pos, uint32_t V, const uint32_t* idx, ui
                            const float* raster, const float* grad_raster, float* grad_pos);
 int ora_rasterize_backward_f64(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
                                uint32_t width, uint32_t height, const float viewport[4],
-                               const float* raster, const float* grad_raster, double* grad_pos);
+                               const float* raster, const float* grad_raster, double* grad_pos, int abs_terms);
 
 /* shaders/interpolate_forward.hlsl */
 int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
@@ -60,7 +61,7 @@ int ora_interpolate_backward(const float* attr, uint32_t V, uint32_t A, const ui
                              float* grad_attr, float* grad_raster);
 int ora_interpolate_backward_f64(const float* attr, uint32_t V, uint32_t A, const uint32_t* idx,
                                  uint32_t T, const float* raster, uint64_t P, const float* grad_out,
-                                 double* grad_attr, double* grad_raster);
+                                 double* grad_attr, double* grad_raster, int abs_terms);
 
 /* shaders/texture_forward.hlsl */
 int ora_texture_forward(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
@@ -72,7 +73,7 @@ int ora_texture_backward(const float* tex, uint32_t tw, uint32_t th, uint32_t C,
                          float* grad_tex, float* grad_uv);
 int ora_texture_backward_f64(const float* tex, uint32_t tw, uint32_t th, uint32_t C, uint32_t mode,
                              const float* uv, const float* raster, uint64_t P, const float* grad,
-                             double* grad_tex, double* grad_uv);
+                             double* grad_tex, double* grad_uv, int abs_terms);
 
 /* texture_baker.cpp:92-106 / texture_refiner.cpp:36-50 */
 void ora_transform_positions(const float* pos3, uint32_t V, const float m[16], float* clip4);

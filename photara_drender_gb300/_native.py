@@ -46,9 +46,27 @@ _SIGNATURES = {
     "pdr_rasterize_backward": (_i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     "pdr_interpolate_forward": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp]),
     "pdr_interpolate_backward": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp, _vp, _vp]),
+    "pdr_interpolate_backward_accumulate": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp,
+                                                   _vp, _vp]),
     "pdr_texture_forward": (_i32, [_vp, _u64, _u32, _u32, _u32, _u32, _vp, _vp, _u32, _u64, _vp, _vp]),
     "pdr_texture_backward": (_i32, [_vp, _u64, _u32, _u32, _u32, _u32, _vp, _vp, _u32, _u64, _vp, _vp, _vp, _vp,
                                     _vp]),
+    "pdr_transform_positions": (_i32, [_vp, _u32, _vp, _u32, _vp, _vp]),
+    "pdr_atlas_clip_positions": (_i32, [_vp, _u32, _vp, _vp]),
+    "pdr_project_views": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp,
+                                 _vp]),
+    "pdr_refine_prepare_view": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
+    "pdr_refine_photometric": (_i32, [_vp, _u32, _u32, _vp, _u32, _u64, _u32, _u32, C.c_float, C.c_float, _vp, _vp,
+                                      _vp]),
+    "pdr_refine_seam": (_i32, [_vp, _u32, _u32, _vp, _u32, C.c_float, C.c_float, _vp, _vp, _u32, _vp]),
+    "pdr_refine_total_variation": (_i32, [_vp, _u32, _u32, _vp, _vp, C.c_float, C.c_float, _vp, _vp]),
+    "pdr_refine_adam": (_i32, [_vp, _vp, _vp, _vp, _u64] + [C.c_float] * 8 + [_vp]),
+    "pdr_refine_schedule": (_i32, [_vp, _u32, _vp, _vp, _vp]),
+    "pdr_refine_run": (_i32, [_vp, _vp, _u32, _vp, _u64, _vp, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp]),
+    "pdr_refine_graph_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u64, _vp, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                       _vp]),
+    "pdr_refine_graph_launch": (_i32, [_vp, _vp]),
+    "pdr_refine_graph_destroy": (_i32, [_vp]),
 }
 
 OPTIONAL_SIGNATURES: dict = {}

@@ -1,0 +1,231 @@
+// Texture projection (bake) for all views in one launch, plus the small per-view transforms the
+// bake and refine hosts need.
+//
+// Reference path: src/texture_baker.cpp:156-361 and shaders/project_texture.hlsl. The reference
+// dispatches project_texture once per view and keeps the per-texel accumulators in device
+// buffers between dispatches; here one thread owns one atlas texel, walks the views in order
+// with the accumulators in registers, and writes the host-side normalisation of
+// texture_baker.cpp:334-358 directly (colour / weight, valid mask, confidence, source view,
+// coverage and face ids). Per-texel results equal the reference's view-by-view sequence.
+#include <cuda_runtime.h>
+
+#include "../../include/pdr_capi.h"
+#include "pdr_common.cuh"
+#include "pdr_internal.h"
+
+namespace pdr {
+namespace {
+
+__device__ __forceinline__ float lerp_hlsl(float x, float y, float s) { return x * (1.0f - s) + y * s; }
+
+__device__ __forceinline__ float load_channel(const pdr_projection_view& v, int32_t cx, int32_t cy, uint32_t ch) {
+    cx = clampi(cx, 0, (int32_t)v.width - 1);
+    cy = clampi(cy, 0, (int32_t)v.height - 1);
+    return __ldg(v.image + ((size_t)(uint32_t)cy * v.width + (uint32_t)cx) * v.channel_count + ch);
+}
+
+// project_texture.hlsl:46-56
+__device__ __forceinline__ float sample_photo(const pdr_projection_view& v, float ppx, float ppy, uint32_t ch) {
+    const float tx = ppx - 0.5f, ty = ppy - 0.5f;
+    const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+    const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+    const float v00 = load_channel(v, bx, by, ch), v10 = load_channel(v, add1(bx), by, ch);
+    const float v01 = load_channel(v, bx, add1(by), ch), v11 = load_channel(v, add1(bx), add1(by), ch);
+    return lerp_hlsl(lerp_hlsl(v00, v10, fx), lerp_hlsl(v01, v11, fx), fy);
+}
+
+// project_texture.hlsl:58-74, with the host-side mask floor of texture_baker.cpp:283-292
+// (std::max(mask, floor) on every mask texel) applied to the four taps.
+__device__ __forceinline__ float mask_tap(const pdr_projection_view& v, int32_t x, int32_t y, float floor_value) {
+    const float m = __ldg(v.visibility_mask + (size_t)y * v.width + x);
+    return floor_value > 0.0f && m < floor_value ? floor_value : m;
+}
+
+__device__ __forceinline__ float sample_mask(const pdr_projection_view& v, float ppx, float ppy, float floor_value) {
+    const int32_t w = (int32_t)v.width, h = (int32_t)v.height;
+    const float tx = ppx - 0.5f, ty = ppy - 0.5f;
+    const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+    const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+    const int32_t x0 = clampi(bx, 0, w - 1), x1 = clampi(add1(bx), 0, w - 1);
+    const int32_t y0 = clampi(by, 0, h - 1), y1 = clampi(add1(by), 0, h - 1);
+    const float v00 = mask_tap(v, x0, y0, floor_value), v10 = mask_tap(v, x1, y0, floor_value);
+    const float v01 = mask_tap(v, x0, y1, floor_value), v11 = mask_tap(v, x1, y1, floor_value);
+    return lerp_hlsl(lerp_hlsl(v00, v10, fx), lerp_hlsl(v01, v11, fx), fy);
+}
+
+// project_texture.hlsl:76-101
+__device__ __forceinline__ float shadow_visibility(const pdr_projection_view& v, float ppx, float ppy, float depth,
+                                                   int32_t r) {
+    const int32_t w = (int32_t)v.width, h = (int32_t)v.height;
+    const int32_t cx = f2i_sat(floorf(ppx)), cy = f2i_sat(floorf(ppy));
+    float visible = 0.0f, count = 0.0f;
+    const float4* shadow = reinterpret_cast<const float4*>(v.shadow_raster);
+    for (int32_t y = -r; y <= r; ++y) {
+        for (int32_t x = -r; x <= r; ++x) {
+            const int32_t X = cx + x, Y = cy + y;
+            if (X < 0 || Y < 0 || X >= w || Y >= h) continue;
+            const float4 s = __ldg(shadow + (size_t)Y * v.width + (size_t)X);
+            if (raster_id(s.w) != 0) {
+                visible += depth <= s.z + v.depth_bias ? 1.0f : 0.0f;
+                count += 1.0f;
+            }
+        }
+    }
+    return count > 0.0f ? visible / count : 0.0f;
+}
+
+__global__ void project_views_kernel(const float* __restrict__ apos, const float* __restrict__ anrm,
+                                     const float4* __restrict__ araster, uint32_t N,
+                                     const pdr_projection_view* __restrict__ views, uint32_t nviews,
+                                     uint32_t blend_mode, uint32_t pcf_radius, uint32_t visibility_mode,
+                                     float* __restrict__ color4, float* __restrict__ confidence,
+                                     uint32_t* __restrict__ source_view, float* __restrict__ valid_mask,
+                                     float* __restrict__ coverage_mask, uint32_t* __restrict__ face_ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float rw = araster[i].w;
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, accw = 0.0f, best = 0.0f;
+    uint32_t src = 0xffffffffu;
+    if (raster_id(rw) != 0) {
+        const float px = apos[(size_t)i * 3], py = apos[(size_t)i * 3 + 1], pz = apos[(size_t)i * 3 + 2];
+        const float nx0 = anrm[(size_t)i * 3], ny0 = anrm[(size_t)i * 3 + 1], nz0 = anrm[(size_t)i * 3 + 2];
+        const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
+        const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
+        for (uint32_t k = 0; k < nviews; ++k) {
+            const pdr_projection_view& v = views[k];
+            const float* M = v.world_to_clip;
+            const float cw = M[12] * px + M[13] * py + M[14] * pz + M[15] * 1.0f;
+            if (cw <= 1e-8f) continue;
+            const float cx = M[0] * px + M[1] * py + M[2] * pz + M[3] * 1.0f;
+            const float cy = M[4] * px + M[5] * py + M[6] * pz + M[7] * 1.0f;
+            const float cz = M[8] * px + M[9] * py + M[10] * pz + M[11] * 1.0f;
+            const float ndx = cx / cw, ndy = cy / cw, ndz = cz / cw;
+            if (ndx < -1.0f || ndy < -1.0f || ndx > 1.0f || ndy > 1.0f || ndz < -1.0f || ndz > 1.0f) continue;
+            const float ppx = v.viewport[0] + (ndx * 0.5f + 0.5f) * v.viewport[2];
+            const float ppy = v.viewport[1] + (ndy * 0.5f + 0.5f) * v.viewport[3];
+            if (ppx < v.viewport[0] || ppy < v.viewport[1] || ppx >= v.viewport[0] + v.viewport[2] ||
+                ppy >= v.viewport[1] + v.viewport[3])
+                continue;
+            // view direction first: the facing test rejects half of all texel-views before the
+            // visibility work, with the same outcome as the reference's order
+            const float vx0 = v.camera_position[0] - px, vy0 = v.camera_position[1] - py;
+            const float vz0 = v.camera_position[2] - pz;
+            const float vl = sqrtf(vx0 * vx0 + vy0 * vy0 + vz0 * vz0);
+            const float cosv = nx * (vx0 / vl) + ny * (vy0 / vl) + nz * (vz0 / vl);
+            if (cosv < v.min_view_cosine) continue;
+            float vis = v.ray_visibility ? __ldg(v.ray_visibility + i) : 1.0f;
+            if (visibility_mode == 0) vis = shadow_visibility(v, ppx, ppy, ndz, (int32_t)pcf_radius);
+            else if (visibility_mode == 1) vis *= shadow_visibility(v, ppx, ppy, ndz, (int32_t)pcf_radius);
+            if (v.has_mask) vis *= clamp_hlsl(sample_mask(v, ppx, ppy, v.mask_floor), 0.0f, 1.0f);
+            if (vis <= 0.0f) continue;
+            const float c0 = sample_photo(v, ppx, ppy, 0), c1 = sample_photo(v, ppx, ppy, 1);
+            const float c2 = sample_photo(v, ppx, ppy, 2);
+            const float alpha = v.channel_count == 4 ? sample_photo(v, ppx, ppy, 3) : 1.0f;
+            if (blend_mode == 2) {
+                const float dist = fmaxf(vl, 1e-6f);
+                const float footprint = cosv / (dist * dist);
+                const float ex = clamp_hlsl(vis * alpha * footprint * v.weight, 0.0f, 64.0f);
+                const float prev = best;
+                const float cur = fmaxf(prev, ex);
+                if (cur > prev) {
+                    const float rs = expf(prev - cur);
+                    acc0 *= rs;
+                    acc1 *= rs;
+                    acc2 *= rs;
+                    accw *= rs;
+                    best = cur;
+                }
+                if (ex >= prev) src = k;
+                const float sw = expf(ex - cur);
+                if (sw <= 0.0f) continue;
+                acc0 += c0 * sw;
+                acc1 += c1 * sw;
+                acc2 += c2 * sw;
+                accw += sw;
+                continue;
+            }
+            const float conf = vis * alpha * cosv * v.weight;
+            if (conf <= 0.0f) continue;
+            if (conf > best) {
+                best = conf;
+                src = k;
+            }
+            if (blend_mode == 0) {
+                if (conf >= accw) {
+                    acc0 = c0;
+                    acc1 = c1;
+                    acc2 = c2;
+                    accw = conf;
+                }
+            } else {
+                acc0 += c0 * conf;
+                acc1 += c1 * conf;
+                acc2 += c2 * conf;
+                accw += conf;
+            }
+        }
+    }
+    // texture_baker.cpp:192-204 and 347-358
+    const float valid = accw > 0.0f ? 1.0f : 0.0f;
+    const float div = blend_mode != 0 && accw > 0.0f ? accw : 1.0f;
+    reinterpret_cast<float4*>(color4)[i] = make_float4(acc0 / div, acc1 / div, acc2 / div, valid);
+    confidence[i] = accw;
+    source_view[i] = src;
+    valid_mask[i] = valid;
+    const float r = roundf(rw);
+    const float cov = r != 0.0f ? 1.0f : 0.0f;
+    if (coverage_mask) coverage_mask[i] = cov;
+    if (face_ids) face_ids[i] = cov > 0.5f ? (uint32_t)r - 1u : 0xffffffffu;
+}
+
+// texture_baker.cpp:92-106 / texture_refiner.cpp:36-50 for every view: [views][V][4].
+__global__ void transform_positions_kernel(const float* __restrict__ pos3, uint32_t V,
+                                           const float* __restrict__ mats, float4* __restrict__ clip) {
+    const uint32_t view = blockIdx.y;
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const float* m = mats + (size_t)view * 16;
+    const float x = pos3[(size_t)v * 3], y = pos3[(size_t)v * 3 + 1], z = pos3[(size_t)v * 3 + 2];
+    float4 o;
+    o.x = m[0] * x + m[1] * y + m[2] * z + m[3];
+    o.y = m[4] * x + m[5] * y + m[6] * z + m[7];
+    o.z = m[8] * x + m[9] * y + m[10] * z + m[11];
+    o.w = m[12] * x + m[13] * y + m[14] * z + m[15];
+    clip[(size_t)view * V + v] = o;
+}
+
+// texture_baker.cpp:81-90
+__global__ void atlas_clip_kernel(const float2* __restrict__ uv, uint32_t V, float4* __restrict__ clip) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const float2 t = uv[v];
+    clip[v] = make_float4(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, 0.0f, 1.0f);
+}
+
+}  // namespace
+
+cudaError_t launch_project_views(const float* apos, const float* anrm, const float* araster, uint32_t N,
+                                 const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,
+                                 uint32_t pcf_radius, uint32_t visibility_mode, float* color4, float* confidence,
+                                 uint32_t* source_view, float* valid_mask, float* coverage_mask, uint32_t* face_ids,
+                                 cudaStream_t stream) {
+    project_views_kernel<<<(N + 127) / 128, 128, 0, stream>>>(
+        apos, anrm, reinterpret_cast<const float4*>(araster), N, views, nviews, blend_mode, pcf_radius,
+        visibility_mode, color4, confidence, source_view, valid_mask, coverage_mask, face_ids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transform_positions(const float* pos3, uint32_t V, const float* mats, uint32_t views, float* clip,
+                                       cudaStream_t stream) {
+    const dim3 grid((V + 255) / 256, views);
+    transform_positions_kernel<<<grid, 256, 0, stream>>>(pos3, V, mats, reinterpret_cast<float4*>(clip));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_atlas_clip(const float* uv, uint32_t V, float* clip, cudaStream_t stream) {
+    atlas_clip_kernel<<<(V + 255) / 256, 256, 0, stream>>>(reinterpret_cast<const float2*>(uv), V,
+                                                           reinterpret_cast<float4*>(clip));
+    return cudaGetLastError();
+}
+
+}  // namespace pdr

@@ -36,6 +36,9 @@ __global__ void validate_indices_kernel(const uint32_t* __restrict__ idx, uint64
 }
 }  // namespace
 
+pdr_status set_error(pdr_status code, const char* msg) { return fail(code, msg); }
+pdr_status set_cuda_error(cudaError_t err, const char* what) { return cuda_status(err, what); }
+
 int num_sms() {
     static int sms = 0;
     if (sms == 0) {
@@ -163,9 +166,30 @@ pdr_status pdr_interpolate_forward(const float* attr, uint64_t stride, uint32_t 
                        "interpolate_forward");
 }
 
+static pdr_status interpolate_backward_impl(const float* attr, uint64_t stride, uint32_t V, uint32_t A,
+                                            const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,
+                                            uint64_t P, const float* grad_out, float* grad_attr, float* grad_raster,
+                                            void* stream, bool accumulate);
+
 pdr_status pdr_interpolate_backward(const float* attr, uint64_t stride, uint32_t V, uint32_t A, const uint32_t* idx,
                                     uint32_t T, const float* raster, uint32_t views, uint64_t P, const float* grad_out,
                                     float* grad_attr, float* grad_raster, void* stream) {
+    return interpolate_backward_impl(attr, stride, V, A, idx, T, raster, views, P, grad_out, grad_attr, grad_raster,
+                                     stream, false);
+}
+
+pdr_status pdr_interpolate_backward_accumulate(const float* attr, uint64_t stride, uint32_t V, uint32_t A,
+                                               const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,
+                                               uint64_t P, const float* grad_out, float* grad_attr, float* grad_raster,
+                                               void* stream) {
+    return interpolate_backward_impl(attr, stride, V, A, idx, T, raster, views, P, grad_out, grad_attr, grad_raster,
+                                     stream, true);
+}
+
+static pdr_status interpolate_backward_impl(const float* attr, uint64_t stride, uint32_t V, uint32_t A,
+                                            const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,
+                                            uint64_t P, const float* grad_out, float* grad_attr, float* grad_raster,
+                                            void* stream, bool accumulate) {
     if (!attr || !idx || !raster || !grad_out) return fail(PDR_INVALID_ARGUMENT, "attributes, indices, raster and grad_interpolated are required");
     if (A == 0 || V == 0) return fail(PDR_INVALID_ARGUMENT, "vertex_attributes must have shape [vertex_count, attribute_count]");
     if (T == 0) return fail(PDR_INVALID_ARGUMENT, "triangle_indices is incompatible with vertex_attributes");
@@ -173,7 +197,7 @@ pdr_status pdr_interpolate_backward(const float* attr, uint64_t stride, uint32_t
     if (P > 0xffffffffull) return fail(PDR_OVERFLOW, "Interpolation pixel count exceeds backend limits");
     if (!aligned(raster, 16) || (grad_raster && !aligned(grad_raster, 16))) return fail(PDR_INVALID_ARGUMENT, "raster buffers must be 16-byte aligned");
     return cuda_status(launch_interpolate_backward(attr, stride, V, A, idx, T, raster, views, P, grad_out, grad_attr,
-                                                   grad_raster, (cudaStream_t)stream),
+                                                   grad_raster, (cudaStream_t)stream, accumulate),
                        "interpolate_backward");
 }
 

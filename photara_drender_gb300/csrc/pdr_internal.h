@@ -43,7 +43,7 @@ cudaError_t launch_interpolate_forward(const float* attr, size_t attr_view_strid
 cudaError_t launch_interpolate_backward(const float* attr, size_t attr_view_stride, uint32_t V, uint32_t A,
                                         const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,
                                         size_t P, const float* grad_out, float* grad_attr, float* grad_raster,
-                                        cudaStream_t stream);
+                                        cudaStream_t stream, bool accumulate_raster = false);
 
 cudaError_t launch_texture_forward(const float* tex, size_t tex_view_stride, uint32_t tw, uint32_t th, uint32_t C,
                                    uint32_t mode, const float* uv, const float* raster, uint32_t views, size_t P,
@@ -53,5 +53,33 @@ cudaError_t launch_texture_backward(const float* tex, size_t tex_view_stride, ui
                                     uint32_t mode, const float* uv, const float* raster, uint32_t views, size_t P,
                                     const float* grad, float* grad_tex, float* grad_uv, uint32_t* status,
                                     cudaStream_t stream);
+
+
+}  // namespace pdr
+
+#include "../../include/pdr_capi.h"
+
+namespace pdr {
+
+cudaError_t launch_project_views(const float* apos, const float* anrm, const float* araster, uint32_t N,
+                                 const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,
+                                 uint32_t pcf_radius, uint32_t visibility_mode, float* color4, float* confidence,
+                                 uint32_t* source_view, float* valid_mask, float* coverage_mask, uint32_t* face_ids,
+                                 cudaStream_t stream);
+cudaError_t launch_transform_positions(const float* pos3, uint32_t V, const float* mats, uint32_t views, float* clip,
+                                       cudaStream_t stream);
+cudaError_t launch_atlas_clip(const float* uv, uint32_t V, float* clip, cudaStream_t stream);
+cudaError_t launch_prepare_view(const float* image, uint32_t C, const float* ext_mask, const float* raster, size_t P,
+                                float* target, float* mask, cudaStream_t stream);
+cudaError_t launch_photometric(const float* tex, uint32_t tw, uint32_t th, const pdr_refine_view* views,
+                               uint32_t nviews, uint64_t max_pixels, uint32_t step, uint32_t batch, float eps,
+                               float norm, float* grad, float* loss, cudaStream_t stream);
+cudaError_t launch_seam(const float* tex, uint32_t tw, uint32_t th, const float* pairs, uint32_t npairs, float eps,
+                        float norm, float* grad, float* loss, uint32_t loss_index, cudaStream_t stream);
+cudaError_t launch_tv(const float* tex, uint32_t tw, uint32_t th, const uint8_t* valid, const int32_t* chart, float eps,
+                      float scale, float* grad, cudaStream_t stream);
+cudaError_t launch_adam(float* tex, float* grad, float* m, float* v, size_t n, float lr, float b1, float b2, float eps,
+                        float bc1, float bc2, float cmin, float cmax, cudaStream_t stream);
+void refine_schedule(const pdr_refine_options* o, uint32_t step, float* lr, float* bc1, float* bc2);
 
 }  // namespace pdr

@@ -49,7 +49,7 @@ __global__ void interpolate_backward_kernel(const float* __restrict__ attr_all, 
                                             uint32_t A, const uint3* __restrict__ idx, uint32_t T,
                                             const float4* __restrict__ raster, size_t P,
                                             const float* __restrict__ grad_out, float* __restrict__ grad_attr_all,
-                                            float4* __restrict__ grad_raster) {
+                                            float4* __restrict__ grad_raster, bool accumulate) {
     const uint32_t view = blockIdx.y;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
@@ -57,7 +57,7 @@ __global__ void interpolate_backward_kernel(const float* __restrict__ attr_all, 
     const float4 r = raster[pix];
     const uint32_t id = raster_id(r.w);
     if (id == 0 || id > T) {
-        if (grad_raster) grad_raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (grad_raster && !accumulate) grad_raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
     const uint3 vi = idx[id - 1];
@@ -90,7 +90,12 @@ __global__ void interpolate_backward_kernel(const float* __restrict__ attr_all, 
                 gy += g[a] * (a1 - a2);
             }
         }
-        grad_raster[pix] = make_float4(gx, gy, 0.0f, 0.0f);
+        if (accumulate) {
+            const float4 o = grad_raster[pix];
+            grad_raster[pix] = make_float4(o.x + gx, o.y + gy, o.z, o.w);
+        } else {
+            grad_raster[pix] = make_float4(gx, gy, 0.0f, 0.0f);
+        }
     }
 }
 
@@ -244,7 +249,7 @@ cudaError_t launch_interpolate_forward(const float* attr, size_t attr_view_strid
 cudaError_t launch_interpolate_backward(const float* attr, size_t attr_view_stride, uint32_t V, uint32_t A,
                                         const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,
                                         size_t P, const float* grad_out, float* grad_attr, float* grad_raster,
-                                        cudaStream_t stream) {
+                                        cudaStream_t stream, bool accumulate_raster) {
     if (grad_attr) {
         const size_t n = attr_view_stride == 0 ? (size_t)V * A : attr_view_stride * views;
         cudaError_t err = cudaMemsetAsync(grad_attr, 0, n * sizeof(float), stream);
@@ -254,7 +259,8 @@ cudaError_t launch_interpolate_backward(const float* attr, size_t attr_view_stri
     interpolate_backward_kernel<<<grid, 256, 0, stream>>>(attr, attr_view_stride, V, A,
                                                           reinterpret_cast<const uint3*>(idx), T,
                                                           reinterpret_cast<const float4*>(raster), P, grad_out,
-                                                          grad_attr, reinterpret_cast<float4*>(grad_raster));
+                                                          grad_attr, reinterpret_cast<float4*>(grad_raster),
+                                                          accumulate_raster);
     return cudaGetLastError();
 }
 

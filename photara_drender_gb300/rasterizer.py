@@ -136,10 +136,20 @@ class _Io:
         return t
 
 
+def _single_viewport(vp) -> bool:
+    """True for one (x, y, width, height) viewport, False for a per-view sequence of them."""
+    if isinstance(vp, (list, tuple)) and any(v is None or hasattr(v, "__len__") for v in vp):
+        return False
+    try:
+        a = np.asarray(vp, dtype=np.float64)
+    except (TypeError, ValueError):
+        return False
+    return a.ndim == 1 and a.shape[0] == 4
+
+
 def _viewports(viewport, views: int, width: int, height: int, device) -> Tuple[torch.Tensor, list]:
     """src/rasterizer.cpp:48-59 resolve_viewport, per view."""
-    if viewport is None or (isinstance(viewport, (list, tuple)) and len(viewport) == 4
-                            and not isinstance(viewport[0], (list, tuple, np.ndarray)) and viewport[0] is not None):
+    if viewport is None or _single_viewport(viewport):
         per = [viewport] * views
     else:
         per = list(viewport)
@@ -384,4 +394,6 @@ class Rasterizer:
 
 
 def _is_batched(positions) -> bool:
-    return getattr(positions, "ndim", np.asarray(positions).ndim) == 3
+    if isinstance(positions, (np.ndarray, torch.Tensor)):
+        return positions.ndim == 3
+    return np.asarray(positions).ndim == 3

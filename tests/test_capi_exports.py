@@ -1,0 +1,50 @@
+"""The C-ABI library builds, loads without a GPU, and exports every entry point include/*.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            with open(os.path.join(inc, f)) as fh:
+                text = fh.read()
+            names += re.findall(r"PDR_API\s+[\w\s\*]+?\b(pdr_\w+)\s*\(", text)
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert len(names) >= 25
+    for required in ("pdr_bin_tiles", "pdr_rasterize_forward", "pdr_rasterize_backward", "pdr_interpolate_forward",
+                     "pdr_interpolate_backward", "pdr_texture_forward", "pdr_texture_backward", "pdr_project_views",
+                     "pdr_refine_run", "pdr_refine_graph_create"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    from photara_drender_gb300 import build
+
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.pdr_version.restype = ctypes.c_int32
+    assert lib.pdr_version() >= 100
+
+
+def test_status_codes_without_gpu():
+    """Argument checks run before any CUDA call, so they answer on a machine without a GPU."""
+    from photara_drender_gb300 import _native
+
+    L = _native.lib()
+    with pytest.raises(ValueError):
+        _native.check(L.pdr_rasterize_forward(None, 1, 3, None, 1, 8, 8, None, 0, None, None, 0, None, None, None))
+    with pytest.raises(ValueError):
+        _native.check(L.pdr_texture_forward(None, 0, 4, 4, 3, 0, None, None, 1, 16, None, None))

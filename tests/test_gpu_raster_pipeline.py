@@ -77,7 +77,9 @@ def test_adversarial_raster(rast, cull):
         g = np.random.default_rng(1).normal(size=o_r.shape).astype(np.float32)
         gp = rast.backward(pos, idx, o_r, g, viewport=vp)
         grad_check(gp, api.rasterize_backward(pos, idx, o_r, g, viewport=vp),
-                   api.rasterize_backward(pos, idx, o_r, g, viewport=vp, f64=True), name="adversarial grad_pos")
+                   api.rasterize_backward(pos, idx, o_r, g, viewport=vp, f64=True),
+                   api.rasterize_backward(pos, idx, o_r, g, viewport=vp, f64=True, abs_terms=True),
+                   name="adversarial grad_pos")
 
 
 def test_large_tiles_sorted(rast):
@@ -114,8 +116,9 @@ def test_backward_chain_vs_oracle(rast):
         ga, gr = rast.interpolate_backward(attrs, idx, o_r, gi)
         o_ga, o_gr = api.interpolate_backward(attrs, idx, o_r, gi)
         o64_ga, _ = api.interpolate_backward(attrs, idx, o_r, gi, f64=True)
+        abs_ga, _ = api.interpolate_backward(attrs, idx, o_r, gi, f64=True, abs_terms=True)
         assert same_bits(gr, o_gr), "interpolate grad_raster"
-        grad_check(ga, o_ga, o64_ga, name="grad_attributes")
+        grad_check(ga, o_ga, o64_ga, abs_ga, name="grad_attributes")
         uv = api.interpolate_forward(uvv, idx, o_r) * 1.3 - 0.1
         for mode in ("clamp", "wrap", "mirror"):
             s = rast.texture_forward(tex, uv, o_r, mode)
@@ -124,12 +127,14 @@ def test_backward_chain_vs_oracle(rast):
             gt, gu = rast.texture_backward(tex, uv, o_r, gs, mode)
             o_gt, o_gu = api.texture_backward(tex, uv, o_r, gs, mode)
             o64_gt, _ = api.texture_backward(tex, uv, o_r, gs, mode, f64=True)
+            abs_gt, _ = api.texture_backward(tex, uv, o_r, gs, mode, f64=True, abs_terms=True)
             assert same_bits(gu, o_gu), f"grad_uv {mode}"
-            grad_check(gt, o_gt, o64_gt, name=f"grad_texture {mode}")
+            grad_check(gt, o_gt, o64_gt, abs_gt, name=f"grad_texture {mode}")
         g = rng.normal(size=o_r.shape).astype(np.float32)
         gp = rast.backward(clip[k], idx, o_r, g)
         grad_check(gp, api.rasterize_backward(clip[k], idx, o_r, g),
-                   api.rasterize_backward(clip[k], idx, o_r, g, f64=True), name="grad_positions")
+                   api.rasterize_backward(clip[k], idx, o_r, g, f64=True),
+                   api.rasterize_backward(clip[k], idx, o_r, g, f64=True, abs_terms=True), name="grad_positions")
 
 
 def test_texture_channels_not_four(rast):
@@ -145,7 +150,8 @@ def test_texture_channels_not_four(rast):
         gt, gu = rast.texture_backward(tex, uv, o_r, gs)
         o_gt, o_gu = api.texture_backward(tex, uv, o_r, gs)
         assert same_bits(gu, o_gu)
-        grad_check(gt, o_gt, api.texture_backward(tex, uv, o_r, gs, f64=True)[0], name=f"grad_texture C={C}")
+        grad_check(gt, o_gt, api.texture_backward(tex, uv, o_r, gs, f64=True)[0],
+                   api.texture_backward(tex, uv, o_r, gs, f64=True, abs_terms=True)[0], name=f"grad_texture C={C}")
 
 
 def test_golden_fixtures_on_gpu(rast):

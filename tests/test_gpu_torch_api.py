@@ -1,0 +1,121 @@
+"""The reference's Python surface on the GPU: tests/python_smoke.py restated (shapes, finiteness,
+autograd through rasterize -> interpolate -> texture, the atlas helpers, the native refiner) plus
+autograd-vs-direct-adjoint equality."""
+import numpy as np
+import pytest
+import torch
+
+import photara_drender_gb300 as pdr
+from oracle import api
+from photara_drender_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+TRI = np.array([[-0.75, -0.75, 0.0, 1.0], [0.75, -0.75, 0.0, 1.0], [0.0, 0.75, 0.0, 1.0]], np.float32)
+IDX = np.array([[0, 1, 2]], np.uint32)
+
+
+@pytest.fixture(scope="module")
+def rast():
+    return pdr.Rasterizer()
+
+
+def test_python_smoke_numpy_surface(rast):
+    raster, derivatives = rast.forward(TRI, IDX, (16, 20))
+    assert raster.shape == (16, 20, 4) and derivatives.shape == raster.shape
+    assert np.count_nonzero(raster[..., 3]) > 0
+    grad_raster = np.zeros_like(raster)
+    grad_raster[..., 0] = 1.0
+    gp = rast.backward(TRI, IDX, raster, grad_raster)
+    assert gp.shape == TRI.shape and np.isfinite(gp).all()
+    attributes = np.eye(3, dtype=np.float32)
+    interp = rast.interpolate_forward(attributes, IDX, raster)
+    assert interp.shape == (16, 20, 3)
+    ga, gr = rast.interpolate_backward(attributes, IDX, raster, np.ones_like(interp))
+    assert ga.shape == attributes.shape and gr.shape == raster.shape and np.isfinite(ga).all()
+    uva = np.array([[0.2, 0.2], [0.8, 0.2], [0.5, 0.8]], np.float32)
+    uv = rast.interpolate_forward(uva, IDX, raster)
+    tex = np.arange(4 * 4 * 3, dtype=np.float32).reshape(4, 4, 3) / 48.0
+    sampled = rast.texture_forward(tex, uv, raster)
+    assert sampled.shape == (16, 20, 3)
+    gt, gu = rast.texture_backward(tex, uv, raster, np.ones_like(sampled))
+    assert gt.shape == tex.shape and gu.shape == uv.shape and np.isfinite(gt).all() and np.isfinite(gu).all()
+    gt2, gu2 = rast.texture_backward(tex, uv, raster, np.ones_like(sampled), compute_uv_gradient=False)
+    assert gu2 is None
+    for mode in ("wrap", "mirror"):
+        assert np.isfinite(rast.texture_forward(tex, uv + 1.25, raster, mode)).all()
+    vr, _ = rast.forward(TRI, IDX, (20, 24), viewport=(4.0, 3.0, 16.0, 12.0))
+    assert np.count_nonzero(vr[:3, ..., 3]) == 0 and np.count_nonzero(vr[15:, ..., 3]) == 0
+    assert rast.device_info.name
+
+
+def test_python_smoke_torch_surface(rast):
+    dev = torch.device("cuda", 0)
+    positions = torch.tensor(TRI, device=dev, requires_grad=True)
+    indices = torch.tensor(IDX.astype(np.int64), device=dev)
+    raster, _ = pdr.rasterize(positions, indices, (16, 20), rasterizer=rast)
+    attrs = torch.eye(3, dtype=torch.float32, device=dev, requires_grad=True)
+    image = pdr.interpolate(attrs, raster, indices, rasterizer=rast)
+    uva = torch.tensor([[0.2, 0.2], [0.8, 0.2], [0.5, 0.8]], device=dev, requires_grad=True)
+    uv = pdr.interpolate(uva, raster, indices, rasterizer=rast)
+    tex = torch.tensor(np.arange(48, dtype=np.float32).reshape(4, 4, 3) / 48.0, device=dev, requires_grad=True)
+    sampled = pdr.texture(tex, uv, raster, rasterizer=rast)
+    (image[..., 0].sum() + sampled.square().sum()).backward()
+    for t in (positions, attrs, uva, tex):
+        assert t.grad is not None and torch.isfinite(t.grad).all()
+    render = pdr.render_textured_mesh(positions.detach(), indices, uva.detach(), tex.detach(), (16, 20),
+                                      rasterizer=rast)
+    assert render.image.shape == (16, 20, 3)
+    assert torch.isfinite(pdr.masked_charbonnier_loss(render.image, sampled.detach(), render.valid_mask))
+    assert torch.isfinite(pdr.atlas_total_variation(tex.detach()))
+    opts = pdr.AtlasOptimizationOptions(steps=2, learning_rate=1e-2, total_variation_weight=0.0, seam_weight=0.0,
+                                        cache_view_rasters=True)
+    out, hist = pdr.optimize_texture_atlas(tex.detach() * 0.9, positions.detach()[None], indices, uva.detach(),
+                                           [sampled.detach()], rasterizer=rast, options=opts)
+    assert out.shape == tex.shape and len(hist) == 2 and np.isfinite(hist).all()
+
+
+def test_autograd_equals_direct_adjoints(rast):
+    rng = np.random.default_rng(0)
+    pos3, idx = S.icosphere(3)
+    mats, _ = S.orbit_cameras(2)
+    clip = S.clip_positions(pos3, mats)
+    dev = torch.device("cuda", 0)
+    tclip = torch.tensor(clip, device=dev, requires_grad=True)
+    tidx = torch.tensor(idx.astype(np.int64), device=dev)
+    uva = torch.tensor(S.spherical_uv(pos3), device=dev, requires_grad=True)
+    tex = torch.tensor(rng.uniform(size=(32, 32, 4)).astype(np.float32), device=dev, requires_grad=True)
+    raster, _ = pdr.rasterize(tclip, tidx, (64, 64), rasterizer=rast, recompute_in_backward=True)
+    uv = pdr.interpolate(uva, raster, tidx, rasterizer=rast)
+    img = pdr.texture(tex, uv, raster, rasterizer=rast)
+    g = torch.tensor(rng.normal(size=img.shape).astype(np.float32), device=dev)
+    img.backward(g)
+    gt, gu = rast.texture_backward(tex.detach(), uv.detach(), raster.detach(), g)
+    ga, gr = rast.interpolate_backward(uva.detach(), tidx, raster.detach(), gu)
+    gp = rast.backward(tclip.detach(), tidx, raster.detach(), gr)
+    assert torch.allclose(tex.grad, gt, rtol=1e-5, atol=1e-6)
+    assert torch.allclose(uva.grad, ga, rtol=1e-5, atol=1e-5)
+    assert torch.allclose(tclip.grad, gp, rtol=1e-4, atol=1e-5)
+
+
+def test_native_refine_smoke(rast):
+    # tests/python_smoke.py:83-100
+    baker = pdr.TextureBaker()
+    wp = TRI[:, :3].copy()
+    buv = np.array([[0.125, 0.125], [0.875, 0.125], [0.5, 0.875]], np.float32)
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (3, 1))
+    image = np.zeros((16, 16, 4), np.float32)
+    image[..., 0], image[..., 1], image[..., 3] = 0.75, 0.25, 1.0
+    mats = np.eye(4, dtype=np.float32)[None]
+    baked = pdr.project_texture_atlas(pdr.UnwrappedMesh(wp, nrm, buv, IDX, np.arange(3), np.zeros(1), 1, 0.0),
+                                      [image], mats, np.array([[0, 0, 2]], np.float32), resolution=(16, 16),
+                                      baker=baker)
+    assert baked.color.shape == (16, 16, 4) and baked.valid_mask.any()
+    refined, hist, seam, pre, opt = baker.refine_texture(np.ascontiguousarray(baked.color[..., :3] * 0.5), wp, buv, IDX,
+                                                         [image], mats, steps=3, batch_size=1, learning_rate=0.05,
+                                                         minimum_learning_rate=0.01, seam_polish_steps=0)
+    assert refined.shape == (16, 16, 3) and hist.shape == (3,) and np.isfinite(hist).all()
+    assert hist[-1] < hist[0] and seam.shape == (0,) and pre >= 0 and opt >= 0
+    o_ref, o_hist, _ = api.refine(baked.color[..., :3] * 0.5, wp, buv, IDX, [image], mats, steps=3, batch_size=1,
+                                  learning_rate=0.05, minimum_learning_rate=0.01, seam_polish_steps=0)
+    assert np.allclose(hist, o_hist, rtol=1e-5) and np.abs(refined - o_ref).max() < 1e-5
