@@ -198,27 +198,25 @@ def run_reference(args, world, rank):
 
 # ---- GPU arm ------------------------------------------------------------------------------------------
 
-STAGES = ["bin_tiles", "rasterize_forward", "interpolate_forward(attr)", "interpolate_forward(uv)",
-          "texture_forward", "texture_backward", "interpolate_backward(uv)", "interpolate_backward(attr)",
-          "rasterize_backward"]
+STAGES = ["bin_tiles", "rasterize_forward+shade", "render_backward"]
 
 
 def stage_bytes(w, T, V, entries):
-    """Algorithmic bytes per launch of each stage: API-boundary tensors, each read or written once."""
+    """Algorithmic bytes per launch of each timed stage: API-boundary tensors, each read or written
+    once (tile lists count for binning only, where they are the output)."""
     P = w["views"] * w["height"] * w["width"]
     A, Cc = w["attributes"], w["channels"]
     tex = w["atlas"] * w["atlas"] * Cc * 4
     mesh = w["views"] * V * 16 + T * 12
+    tiles = w["views"] * ((w["height"] + 15) // 16) * ((w["width"] + 15) // 16)
     return {
-        "bin_tiles": mesh + entries * 4 + w["views"] * (w["height"] // 16) * (w["width"] // 16) * 4,
-        "rasterize_forward": mesh + entries * 4 + P * 32,
-        "interpolate_forward(attr)": V * A * 4 + T * 12 + P * (16 + A * 4),
-        "interpolate_forward(uv)": V * 2 * 4 + T * 12 + P * (16 + 8),
-        "texture_forward": tex + P * (16 + 8 + Cc * 4),
-        "texture_backward": 2 * tex + P * (16 + 8 + Cc * 4 + 8),
-        "interpolate_backward(uv)": V * 2 * 4 * 2 + T * 12 + P * (16 + 8 + 16),
-        "interpolate_backward(attr)": V * A * 4 * 2 + T * 12 + P * (16 + A * 4 + 16),
-        "rasterize_backward": mesh * 2 + P * (16 + 16),
+        "bin_tiles": mesh + entries * 4 + (tiles + 1) * 4,
+        # inputs: clip, indices, attributes, uv attributes, texture; outputs raster, derivatives,
+        # attributes, uv, sampled
+        "rasterize_forward+shade": mesh + V * (A + 2) * 4 + tex + P * (16 + 16 + A * 4 + 8 + Cc * 4),
+        # inputs: raster, uv, grad_interpolated, grad_sampled, texture, clip, attributes;
+        # outputs: grad_texture, grad_clip, grad_attributes, grad_uv_attributes
+        "render_backward": P * (16 + 8 + A * 4 + Cc * 4) + 2 * tex + 2 * mesh + 2 * V * (A + 2) * 4,
     }
 
 
@@ -279,25 +277,29 @@ def run_gpu(args, world, rank, local):
     ms = max_over_ranks(ms, world)
     value = world * P / 1e6 / (ms / 1e3)
 
-    # ---- per-stage attribution (one more step, events between stages) ------------------------------
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(STAGES) + 1)]
+    # ---- per-stage attribution: replay each stage between events --------------------------------
     L = _native.lib()
     reps = 3
     stage_ms = np.zeros(len(STAGES))
+    a = pipe._args(clip, t_attrs, t_uv, tex, g_attr, g_samp)
+    timed = [
+        lambda: _native.check(L.pdr_bin_tiles(_ptr(clip), views, V, _ptr(pipe.idx), T, W, H, _ptr(pipe.vps),
+                                              _ptr(pipe.offsets), _ptr(pipe.list), pipe.capacity, _ptr(pipe.ws),
+                                              pipe.ws_bytes, _ptr(pipe.status), stream)),
+        lambda: _native.check(L.pdr_render_forward(C.addressof(a), stream)),
+        lambda: _native.check(L.pdr_render_backward(C.addressof(a), stream)),
+    ]
     for _ in range(reps):
-        ev[0].record()
-        pipe.forward(clip, t_attrs, t_uv, tex, stream)  # bin + raster + 3 forwards
-        torch.cuda.synchronize(dev)
-        # time each stage separately by replaying it
-        calls = stage_calls(pipe, L, clip, t_attrs, t_uv, tex, g_attr, g_samp, stream)
-        for i, fn in enumerate(calls):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            fn()
-            b.record()
+        for i, fn in enumerate(timed):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize(dev)
-            stage_ms[i] += a.elapsed_time(b)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            stage_ms[i] += e0.elapsed_time(e1)
     stage_ms /= reps
+    stage_ms[1] = max(stage_ms[1] - stage_ms[0], 1e-6)  # render_forward includes the binning
     hbm, peak_kind = load_peaks()
     sbytes = stage_bytes(w, T, V, entries)
     dom = int(np.argmax(stage_ms))
@@ -306,7 +308,7 @@ def run_gpu(args, world, rank, local):
     step_bytes = P * 96 + 2 * w["atlas"] ** 2 * w["channels"] * 4
 
     # ---- e2e: public autograd API with host buffers ---------------------------------------------------
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = 0 if args.skip_e2e else max(1, min(args.steps, 3))
     host = {k: v.cpu().pin_memory() for k, v in dict(clip=clip, attrs=t_attrs, uv=t_uv, tex=tex, g_attr=g_attr,
                                                      g_samp=g_samp).items()}
     h_idx = torch.tensor(idx.astype(np.int64)).pin_memory()
@@ -330,15 +332,18 @@ def run_gpu(args, world, rank, local):
         out_host = [o.to("cpu", non_blocking=True) for o in outs]
         return sum(o.numel() * o.element_size() for o in outs)
 
-    d2h = e2e_step()
-    torch.cuda.synchronize(dev)
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    torch.cuda.synchronize(dev)
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world)
-    e2e_value = world * P / 1e6 / (e2e_ms / 1e3)
+    e2e_value = e2e_ms = None
+    d2h = 0
+    if e2e_steps:
+        d2h = e2e_step()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world)
+        e2e_value = world * P / 1e6 / (e2e_ms / 1e3)
 
     # ---- CPU baseline (oracle restatement, bounded sample) --------------------------------------------
     cpu = None
@@ -364,11 +369,12 @@ def run_gpu(args, world, rank, local):
                        "attributes": w["attributes"], "tile_entries": entries,
                        "l2": "inputs larger than L2 (6.5 GB of per-view buffers per step)",
                        "parallelism": f"replicas x{world}"},
-            "gpu_launches": RenderFwdBwd.KERNELS_PER_STEP * args.steps,
+            "gpu_launches": pipe.kernels_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                          "algorithmic_bytes": sbytes[dom_name], "ms": float(stage_ms[dom])},
             "stages_ms": {n: float(t) for n, t in zip(STAGES, stage_ms)},
+            "pipeline": "fused" if pipe.fused else "separate kernels",
             "step_roofline": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
                               "frac": step_bytes / (ms / 1e3) / 1e9 / hbm},
             "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
@@ -380,36 +386,6 @@ def run_gpu(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def stage_calls(pipe, L, clip, attrs, uvs, tex, g_attr, g_samp, stream):
-    from photara_drender_gb300 import _native
-    from photara_drender_gb300.rasterizer import _ptr
-
-    p = pipe
-    v, V, T, W, H = p.views, p.V, p.T, p.W, p.H
-    ck = _native.check
-    return [
-        lambda: ck(L.pdr_bin_tiles(_ptr(clip), v, V, _ptr(p.idx), T, W, H, _ptr(p.vps), _ptr(p.offsets),
-                                   _ptr(p.list), p.capacity, _ptr(p.ws), p.ws_bytes, _ptr(p.status), stream)),
-        lambda: ck(L.pdr_rasterize_forward(_ptr(clip), v, V, _ptr(p.idx), T, W, H, _ptr(p.vps), 0, _ptr(p.offsets),
-                                           _ptr(p.list), p.capacity, _ptr(p.raster), _ptr(p.deriv), stream)),
-        lambda: ck(L.pdr_interpolate_forward(_ptr(attrs), 0, V, p.A, _ptr(p.idx), T, _ptr(p.raster), v, p.P,
-                                             _ptr(p.attr_out), stream)),
-        lambda: ck(L.pdr_interpolate_forward(_ptr(uvs), 0, V, 2, _ptr(p.idx), T, _ptr(p.raster), v, p.P, _ptr(p.uv),
-                                             stream)),
-        lambda: ck(L.pdr_texture_forward(_ptr(tex), 0, p.tw, p.th, p.C, p.mode, _ptr(p.uv), _ptr(p.raster), v, p.P,
-                                         _ptr(p.sampled), stream)),
-        lambda: ck(L.pdr_texture_backward(_ptr(tex), 0, p.tw, p.th, p.C, p.mode, _ptr(p.uv), _ptr(p.raster), v, p.P,
-                                          _ptr(g_samp), _ptr(p.grad_tex), _ptr(p.grad_uv), _ptr(p.status), stream)),
-        lambda: ck(L.pdr_interpolate_backward(_ptr(uvs), 0, V, 2, _ptr(p.idx), T, _ptr(p.raster), v, p.P,
-                                              _ptr(p.grad_uv), _ptr(p.grad_uv_attr), _ptr(p.grad_raster), stream)),
-        lambda: ck(L.pdr_interpolate_backward_accumulate(_ptr(attrs), 0, V, p.A, _ptr(p.idx), T, _ptr(p.raster), v,
-                                                         p.P, _ptr(g_attr), _ptr(p.grad_attr), _ptr(p.grad_raster),
-                                                         stream)),
-        lambda: ck(L.pdr_rasterize_backward(_ptr(clip), v, V, _ptr(p.idx), T, W, H, _ptr(p.vps), _ptr(p.raster),
-                                            _ptr(p.grad_raster), _ptr(p.grad_clip), stream)),
-    ]
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -417,7 +393,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
+    ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
+    ap.add_argument("--views", type=int, default=None, help="override the view count (small profiling cases)")
     args = ap.parse_args()
+    if args.views:
+        WORKLOAD["views"] = args.views
+        WORKLOAD["name"] = WORKLOAD["name"].replace("64x", f"{args.views}x")
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))

@@ -238,6 +238,54 @@ PDR_API pdr_status pdr_refine_graph_create(pdr_refine_graph* graph, const pdr_re
 PDR_API pdr_status pdr_refine_graph_launch(pdr_refine_graph graph, void* stream);
 PDR_API pdr_status pdr_refine_graph_destroy(pdr_refine_graph graph);
 
+
+/* ---- fused many-view rendering: rasterize -> interpolate -> texture forward and backward ------- */
+
+/* Arguments of pdr_render_forward / pdr_render_backward (device pointers). Attributes, uv attributes
+ * and the texture are optional (NULL); the texture needs uv attributes and has 4 channels. */
+typedef struct {
+    const float* clip_positions;  /* [views][V][4] */
+    uint32_t views, vertex_count;
+    const uint32_t* indices;      /* [T][3] */
+    uint32_t triangle_count, width, height;
+    const float* viewports;       /* [views][4] */
+    uint32_t cull_mode;
+    const float* attributes;      /* [V][A], A <= 8, shared by all views */
+    uint32_t attribute_count;
+    const float* uv_attributes;   /* [V][2] */
+    const float* texture;         /* [texture_height][texture_width][4] */
+    uint32_t texture_width, texture_height, address_mode;
+    uint32_t* tile_offsets;       /* [views*tiles + 1] */
+    uint32_t* tile_triangles;     /* [capacity] */
+    uint64_t capacity;
+    void* workspace;              /* pdr_render_workspace_bytes() bytes */
+    size_t workspace_bytes;
+    uint32_t* status;             /* PDR_STATUS_WORDS words */
+    float* raster;                /* [views][H][W][4] */
+    float* barycentric_derivatives; /* [views][H][W][4] or NULL */
+    float* interpolated;          /* [views][H][W][A] */
+    float* uv;                    /* [views][H][W][2] */
+    float* sampled;               /* [views][H][W][4] */
+    const float* grad_interpolated; /* [views][H][W][A] */
+    const float* grad_sampled;    /* [views][H][W][4] */
+    float* grad_clip_positions;   /* [views][V][4] */
+    float* grad_attributes;       /* [V][A] summed over views */
+    float* grad_uv_attributes;    /* [V][2] summed over views */
+    float* grad_texture;          /* [texture_height][texture_width][4] summed over views */
+} pdr_render_args;
+
+PDR_API size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
+                                          uint64_t capacity);
+/* Tile binning and one raster launch whose epilogue interpolates both attribute sets and samples the
+ * texture for every pixel: the outputs of Rasterizer::forward + interpolate_forward (x2) +
+ * texture_forward, bit-identical to the separate calls. */
+PDR_API pdr_status pdr_render_forward(const pdr_render_args* args, void* stream);
+/* The adjoints of the forward in one pixel pass: texture_backward, interpolate_backward for both
+ * attribute sets (raster gradients summed) and rasterize_backward. */
+PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream);
+
+
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,9 @@ _SIGNATURES = {
     "pdr_texture_forward": (_i32, [_vp, _u64, _u32, _u32, _u32, _u32, _vp, _vp, _u32, _u64, _vp, _vp]),
     "pdr_texture_backward": (_i32, [_vp, _u64, _u32, _u32, _u32, _u32, _vp, _vp, _u32, _u64, _vp, _vp, _vp, _vp,
                                     _vp]),
+    "pdr_render_workspace_bytes": (_sz, [_u32, _u32, _u32, _u32, _u64]),
+    "pdr_render_forward": (_i32, [_vp, _vp]),
+    "pdr_render_backward": (_i32, [_vp, _vp]),
     "pdr_transform_positions": (_i32, [_vp, _u32, _vp, _u32, _vp, _vp]),
     "pdr_atlas_clip_positions": (_i32, [_vp, _u32, _vp, _vp]),
     "pdr_project_views": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp,

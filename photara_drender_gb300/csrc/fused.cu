@@ -1,0 +1,336 @@
+// Fused forward and backward of rasterize -> interpolate(attributes), interpolate(uv) -> texture for
+// many views (the chain python/photara_drender/atlas.py:36-62 render_textured_mesh runs as three
+// autograd functions, each a separate synchronous call in the reference).
+//
+// Forward: tile binning + one raster launch whose epilogue interpolates and samples for the winner.
+// Backward: one thread per pixel runs, in the reference's order and arithmetic, texture_grad_texture
+// (double-exact weights, vector atomics), texture_grad_uv, interpolate_grad_attributes /
+// interpolate_grad_raster for both attribute sets, and rasterize_backward for the summed raster
+// gradient. Per-vertex gradients of a 16x16 tile are first summed in a shared-memory hash table and
+// flushed with one atomic per (vertex, component); intermediate grad_uv / grad_raster never leave
+// registers.
+#include <cuda_runtime.h>
+
+#include "../../include/pdr_capi.h"
+#include "pdr_common.cuh"
+#include "pdr_internal.h"
+
+namespace pdr {
+namespace {
+
+constexpr int kFusedThreads = 256;
+constexpr uint32_t kSlots = 512;         // hash slots per CTA
+constexpr uint32_t kMaxVals = 2 + 8 + 3; // uv attributes, up to 8 attributes, clip x/y/w
+constexpr uint32_t kEmpty = 0xffffffffu;
+
+__device__ __forceinline__ void red_v4(float* addr, float4 v) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+struct VertexTable {
+    uint32_t key[kSlots];
+    float val[kSlots * kMaxVals];
+};
+
+// Finds or claims the slot of vertex v; returns kSlots when the table is full.
+__device__ __forceinline__ uint32_t table_slot(VertexTable& tb, uint32_t v) {
+    uint32_t s = (v * 2654435761u) >> 23;  // top 9 bits
+    for (uint32_t probe = 0; probe < kSlots; ++probe) {
+        const uint32_t prev = atomicCAS(&tb.key[s], kEmpty, v);
+        if (prev == kEmpty || prev == v) return s;
+        s = (s + 1) & (kSlots - 1);
+    }
+    return kSlots;
+}
+
+struct VertexSink {
+    VertexTable* tb;
+    uint32_t nv;  // values per vertex in the table: uv (2), attributes (A), clip x/y/w (3)
+};
+
+// Adds n values at offset `off` of vertex v's table entry; false when the table is full (the caller
+// then adds to global memory directly).
+__device__ __forceinline__ bool sink_add(const VertexSink& s, uint32_t v, uint32_t off, const float* vals, uint32_t n) {
+    const uint32_t slot = table_slot(*s.tb, v);
+    if (slot >= kSlots) return false;
+    float* dst = s.tb->val + (size_t)slot * s.nv + off;
+    for (uint32_t i = 0; i < n; ++i)
+        if (vals[i] != 0.0f) atomicAdd(dst + i, vals[i]);
+    return true;
+}
+
+__global__ void __launch_bounds__(kFusedThreads)
+render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
+                       uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
+                       const float* __restrict__ attrs, uint32_t A, const float2* __restrict__ uv_attrs,
+                       const float4* __restrict__ tex, uint32_t tw, uint32_t th, uint32_t mode,
+                       const float4* __restrict__ raster, const float2* __restrict__ uv,
+                       const float* __restrict__ grad_attr_out, const float4* __restrict__ grad_sampled,
+                       float* __restrict__ g_clip_all, float* __restrict__ g_attr, float* __restrict__ g_uv,
+                       float* __restrict__ g_tex, uint32_t* __restrict__ status) {
+    __shared__ VertexTable tb;
+    const uint32_t view = blockIdx.y;
+    const uint32_t tile = blockIdx.x;
+    const uint32_t nv = 2 + A + 3;
+    for (uint32_t i = threadIdx.x; i < kSlots; i += kFusedThreads) tb.key[i] = kEmpty;
+    for (uint32_t i = threadIdx.x; i < kSlots * nv; i += kFusedThreads) tb.val[i] = 0.0f;
+    __syncthreads();
+    float* g_clip = g_clip_all + (size_t)view * V * 4;
+    VertexSink sink{&tb, nv};
+
+    const uint32_t px = (tile % tcx) * kTile + (threadIdx.x & 15u);
+    const uint32_t py = (tile / tcx) * kTile + (threadIdx.x >> 4);
+    if (px < W && py < H) {
+        const size_t pix = ((size_t)view * H + py) * W + px;
+        const float4 r = raster[pix];
+        const uint32_t id = raster_id(r.w);
+        const float2 u = uv ? uv[pix] : make_float2(0.0f, 0.0f);
+        float4 gs = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float gux = 0.0f, guy = 0.0f;
+        if (tex) {
+            gs = grad_sampled[pix];
+            // texture_grad_texture: pixels with raster.w != 0, double-exact weights (rasterizer.cpp:198-229)
+            if (r.w != 0.0f) {
+                int32_t bx, by;
+                float fx, fy;
+                const int ex = exact_texel_coordinate(u.x, tw, &bx, &fx);
+                const int ey = exact_texel_coordinate(u.y, th, &by, &fy);
+                if (ex | ey) {
+                    atomicMax(status + kStatusTexelError, ((ex | ey) & kTexelNonFinite) ? (uint32_t)kTexelNonFinite
+                                                                                       : (uint32_t)kTexelRange);
+                } else {
+                    const int32_t xs0 = address_coordinate(bx, tw, mode), xs1 = address_coordinate(bx + 1, tw, mode);
+                    const int32_t ys0 = address_coordinate(by, th, mode), ys1 = address_coordinate(by + 1, th, mode);
+                    const float w0 = (1.0f - fx) * (1.0f - fy), w1 = fx * (1.0f - fy), w2 = (1.0f - fx) * fy,
+                                w3 = fx * fy;
+                    red_v4(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs0) * 4, make_float4(w0 * gs.x, w0 * gs.y, w0 * gs.z, w0 * gs.w));
+                    red_v4(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs1) * 4, make_float4(w1 * gs.x, w1 * gs.y, w1 * gs.z, w1 * gs.w));
+                    red_v4(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs0) * 4, make_float4(w2 * gs.x, w2 * gs.y, w2 * gs.z, w2 * gs.w));
+                    red_v4(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs1) * 4, make_float4(w3 * gs.x, w3 * gs.y, w3 * gs.z, w3 * gs.w));
+                }
+            }
+            // texture_grad_uv (fp32)
+            if (id != 0) {
+                const float tx = u.x * (float)tw - 0.5f, ty = u.y * (float)th - 0.5f;
+                const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+                const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+                const int32_t x0 = address_coordinate(bx, tw, mode), x1 = address_coordinate(add1(bx), tw, mode);
+                const int32_t y0 = address_coordinate(by, th, mode), y1 = address_coordinate(add1(by), th, mode);
+                const float4 c00 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x0);
+                const float4 c10 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x1);
+                const float4 c01 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x0);
+                const float4 c11 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x1);
+                const float cs00[4] = {c00.x, c00.y, c00.z, c00.w}, cs10[4] = {c10.x, c10.y, c10.z, c10.w};
+                const float cs01[4] = {c01.x, c01.y, c01.z, c01.w}, cs11[4] = {c11.x, c11.y, c11.z, c11.w};
+                const float g4[4] = {gs.x, gs.y, gs.z, gs.w};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float dx = (1.0f - fy) * (cs10[c] - cs00[c]) + fy * (cs11[c] - cs01[c]);
+                    const float dy = (1.0f - fx) * (cs01[c] - cs00[c]) + fx * (cs11[c] - cs10[c]);
+                    gux += g4[c] * (dx * (float)tw);
+                    guy += g4[c] * (dy * (float)th);
+                }
+            }
+        }
+        if (id != 0 && id <= T) {
+            const uint3 vi = idx[id - 1];
+            const float bu = r.x, bv = r.y;
+            const uint32_t vs[3] = {vi.x, vi.y, vi.z};
+            const bool inside = vi.x < V && vi.y < V && vi.z < V;
+            // interpolate_grad_attributes for uv and attributes (distinct vertices, accumulated weight)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t vx = vs[k];
+                bool first = true;
+                for (int j = 0; j < k; ++j) first = first && vs[j] != vx;
+                if (!first || vx >= V) continue;
+                float wgt = 0.0f;
+                if (vi.x == vx) wgt += bu;
+                if (vi.y == vx) wgt += bv;
+                if (vi.z == vx) wgt += 1.0f - bu - bv;
+                if (uv_attrs) {
+                    const float vals[2] = {wgt * gux, wgt * guy};
+                    if (!sink_add(sink, vx, 0, vals, 2)) {
+                        atomicAdd(g_uv + (size_t)vx * 2, vals[0]);
+                        atomicAdd(g_uv + (size_t)vx * 2 + 1, vals[1]);
+                    }
+                }
+                if (attrs) {
+                    float vals[8];
+                    for (uint32_t a = 0; a < A; ++a) vals[a] = wgt * grad_attr_out[pix * A + a];
+                    if (!sink_add(sink, vx, 2, vals, A))
+                        for (uint32_t a = 0; a < A; ++a) atomicAdd(g_attr + (size_t)vx * A + a, vals[a]);
+                }
+            }
+            // interpolate_grad_raster: uv attributes first, then attributes accumulated on top
+            float grx = 0.0f, gry = 0.0f;
+            if (inside) {
+                if (uv_attrs) {
+                    const float2 t0 = __ldg(uv_attrs + vi.x), t1 = __ldg(uv_attrs + vi.y), t2 = __ldg(uv_attrs + vi.z);
+                    grx += gux * (t0.x - t2.x);
+                    gry += gux * (t1.x - t2.x);
+                    grx += guy * (t0.y - t2.y);
+                    gry += guy * (t1.y - t2.y);
+                }
+                if (attrs) {
+                    float ax = 0.0f, ay = 0.0f;
+                    for (uint32_t a = 0; a < A; ++a) {
+                        const float g = grad_attr_out[pix * A + a];
+                        const float a0 = __ldg(attrs + (size_t)vi.x * A + a), a1 = __ldg(attrs + (size_t)vi.y * A + a);
+                        const float a2 = __ldg(attrs + (size_t)vi.z * A + a);
+                        ax += g * (a0 - a2);
+                        ay += g * (a1 - a2);
+                    }
+                    grx = grx + ax;
+                    gry = gry + ay;
+                }
+            }
+            // rasterize_backward for this pixel (same visit rule as the per-triangle loop)
+            if (inside && !(grx == 0.0f && gry == 0.0f)) {
+                const float4* __restrict__ clip = clip_all + (size_t)view * V;
+                const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+                const float4 vp = viewports[view];
+                bool visit = !(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f);
+                if (visit) {
+                    const float s0x = p0.x / p0.w, s0y = p0.y / p0.w;
+                    const float s1x = p1.x / p1.w, s1y = p1.y / p1.w;
+                    const float s2x = p2.x / p2.w, s2y = p2.y / p2.w;
+                    const float mnx = fminf(s0x, fminf(s1x, s2x)), mny = fminf(s0y, fminf(s1y, s2y));
+                    const float mxx = fmaxf(s0x, fmaxf(s1x, s2x)), mxy = fmaxf(s0y, fmaxf(s1y, s2y));
+                    const int32_t x0 = clampi(f2i_sat(floorf((mnx * 0.5f + 0.5f) * vp.z + vp.x)), 0, (int32_t)W);
+                    const int32_t x1 = clampi(f2i_sat(ceilf((mxx * 0.5f + 0.5f) * vp.z + vp.x)), 0, (int32_t)W);
+                    const int32_t y0 = clampi(f2i_sat(floorf((mny * 0.5f + 0.5f) * vp.w + vp.y)), 0, (int32_t)H);
+                    const int32_t y1 = clampi(f2i_sat(ceilf((mxy * 0.5f + 0.5f) * vp.w + vp.y)), 0, (int32_t)H);
+                    visit = (int32_t)px >= x0 && (int32_t)px < x1 && (int32_t)py >= y0 && (int32_t)py < y1;
+                }
+                if (visit) {
+                    const float sx = sample_ndc(px, vp.x, vp.z);
+                    const float sy = sample_ndc(py, vp.y, vp.w);
+                    const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+                    const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+                    const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+                    const float area = cross2(q1x, q1y, q2x, q2y) + cross2(q2x, q2y, q0x, q0y) + cross2(q0x, q0y, q1x, q1y);
+                    if (!(fabsf(area) <= 1e-12f)) {
+                        const float eps = area >= 0.0f ? 1e-6f : -1e-6f;
+                        const float inv = 1.0f / (area + eps);
+                        const float a0 = cross2(q1x, q1y, q2x, q2y);
+                        const float a1 = cross2(q2x, q2y, q0x, q0y);
+                        const float b0 = a0 * inv, b1 = a1 * inv;
+                        const float gb0 = grx * inv, gb1 = gry * inv;
+                        const float gc = gb0 * b0 + gb1 * b1;
+                        const float g0x = gc * (q2y - q1y) - gb1 * q2y;
+                        const float g1x = gc * (q0y - q2y) + gb0 * q2y;
+                        const float g2x = gc * (q1y - q0y) - gb0 * q1y + gb1 * q0y;
+                        const float g0y = gc * (q1x - q2x) + gb1 * q2x;
+                        const float g1y = gc * (q2x - q0x) - gb0 * q2x;
+                        const float g2y = gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x;
+                        const float c0[3] = {g0x, g0y, -sx * g0x - sy * g0y};
+                        const float c1[3] = {g1x, g1y, -sx * g1x - sy * g1y};
+                        const float c2[3] = {g2x, g2y, -sx * g2x - sy * g2y};
+                        // table layout x, y, w; clip gradients are components 0, 1 and 3 (z stays 0)
+                        const uint32_t corners[3] = {vi.x, vi.y, vi.z};
+                        const float* cg[3] = {c0, c1, c2};
+                        for (int k = 0; k < 3; ++k) {
+                            if (!sink_add(sink, corners[k], 2 + A, cg[k], 3)) {
+                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 0, cg[k][0]);
+                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 1, cg[k][1]);
+                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 3, cg[k][2]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // flush: one atomic per non-zero (vertex, component)
+    for (uint32_t s = threadIdx.x; s < kSlots; s += kFusedThreads) {
+        const uint32_t v = tb.key[s];
+        if (v == kEmpty) continue;
+        const float* src = tb.val + (size_t)s * nv;
+        if (g_uv) {
+            if (src[0] != 0.0f) atomicAdd(g_uv + (size_t)v * 2, src[0]);
+            if (src[1] != 0.0f) atomicAdd(g_uv + (size_t)v * 2 + 1, src[1]);
+        }
+        if (g_attr)
+            for (uint32_t a = 0; a < A; ++a)
+                if (src[2 + a] != 0.0f) atomicAdd(g_attr + (size_t)v * A + a, src[2 + a]);
+        const float* pc = src + 2 + A;
+        if (pc[0] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 0, pc[0]);
+        if (pc[1] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 1, pc[1]);
+        if (pc[2] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 3, pc[2]);
+    }
+}
+
+}  // namespace
+
+}  // namespace pdr
+
+using namespace pdr;
+
+extern "C" {
+
+size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
+                                  uint64_t capacity) {
+    return bins_workspace_bytes(views, triangle_count, width, height, capacity);
+}
+
+pdr_status pdr_render_forward(const pdr_render_args* a, void* stream) {
+    if (!a || !a->clip_positions || !a->indices || !a->viewports || !a->raster || !a->tile_offsets ||
+        !a->tile_triangles || !a->workspace || !a->status)
+        return set_error(PDR_INVALID_ARGUMENT, "render arguments are incomplete");
+    if (a->views == 0 || a->vertex_count == 0 || a->triangle_count == 0 || a->width == 0 || a->height == 0)
+        return set_error(PDR_INVALID_ARGUMENT, "render dimensions must be positive");
+    if (a->attributes && (a->attribute_count == 0 || a->attribute_count > 8 || !a->interpolated))
+        return set_error(PDR_INVALID_ARGUMENT, "fused rendering supports 1..8 attributes with an output buffer");
+    if (a->texture && (!a->uv_attributes || !a->uv || !a->sampled || a->texture_width == 0 || a->texture_height == 0 ||
+                       a->address_mode > 2))
+        return set_error(PDR_INVALID_ARGUMENT, "texture sampling needs uv attributes and uv/sampled outputs");
+    if (a->workspace_bytes < bins_workspace_bytes(a->views, a->triangle_count, a->width, a->height, a->capacity))
+        return set_error(PDR_INVALID_ARGUMENT, "workspace is smaller than pdr_render_workspace_bytes()");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = launch_bin_tiles(a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count,
+                                       a->width, a->height, a->viewports, a->tile_offsets, a->tile_triangles,
+                                       a->capacity, a->workspace, a->status, s);
+    if (err != cudaSuccess) return set_cuda_error(err, "render_forward(bins)");
+    RasterShade shade{a->attributes, a->attribute_count, a->interpolated, a->uv_attributes, a->uv, a->texture,
+                      a->texture_width, a->texture_height, a->address_mode, a->sampled};
+    err = launch_raster_forward(a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count, a->width,
+                                a->height, a->viewports, a->cull_mode, a->tile_offsets, a->tile_triangles, a->capacity,
+                                a->raster, a->barycentric_derivatives, s,
+                                (a->attributes || a->uv_attributes) ? &shade : nullptr);
+    return set_cuda_error(err, "render_forward");
+}
+
+pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
+    if (!a || !a->clip_positions || !a->indices || !a->viewports || !a->raster || !a->grad_clip_positions || !a->status)
+        return set_error(PDR_INVALID_ARGUMENT, "render arguments are incomplete");
+    if (a->attributes && (!a->grad_interpolated || !a->grad_attributes || a->attribute_count == 0 ||
+                          a->attribute_count > 8))
+        return set_error(PDR_INVALID_ARGUMENT, "attribute gradients need grad_interpolated and grad_attributes");
+    if (a->texture && (!a->uv || !a->grad_sampled || !a->grad_texture || !a->grad_uv_attributes || !a->uv_attributes))
+        return set_error(PDR_INVALID_ARGUMENT, "texture gradients need uv, grad_sampled and gradient outputs");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaMemsetAsync(a->grad_clip_positions, 0, (size_t)a->views * a->vertex_count * 4 * sizeof(float), s);
+    if (err == cudaSuccess && a->grad_attributes)
+        err = cudaMemsetAsync(a->grad_attributes, 0, (size_t)a->vertex_count * a->attribute_count * sizeof(float), s);
+    if (err == cudaSuccess && a->grad_uv_attributes)
+        err = cudaMemsetAsync(a->grad_uv_attributes, 0, (size_t)a->vertex_count * 2 * sizeof(float), s);
+    if (err == cudaSuccess && a->grad_texture)
+        err = cudaMemsetAsync(a->grad_texture, 0, (size_t)a->texture_width * a->texture_height * 4 * sizeof(float), s);
+    if (err != cudaSuccess) return set_cuda_error(err, "render_backward(memset)");
+    const uint32_t tcx = (a->width + kTile - 1) / kTile, tcy = (a->height + kTile - 1) / kTile;
+    const dim3 grid(tcx * tcy, a->views);
+    render_backward_kernel<<<grid, kFusedThreads, 0, s>>>(
+        reinterpret_cast<const float4*>(a->clip_positions), a->vertex_count, reinterpret_cast<const uint3*>(a->indices),
+        a->triangle_count, a->width, a->height, reinterpret_cast<const float4*>(a->viewports), tcx, a->attributes,
+        a->attributes ? a->attribute_count : 0, reinterpret_cast<const float2*>(a->uv_attributes),
+        reinterpret_cast<const float4*>(a->texture), a->texture_width, a->texture_height, a->address_mode,
+        reinterpret_cast<const float4*>(a->raster), reinterpret_cast<const float2*>(a->uv), a->grad_interpolated,
+        reinterpret_cast<const float4*>(a->grad_sampled), a->grad_clip_positions, a->grad_attributes,
+        a->grad_uv_attributes, a->grad_texture, a->status);
+    return set_cuda_error(cudaGetLastError(), "render_backward");
+}
+
+}  // extern "C"

@@ -27,10 +27,24 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
                              unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream);
 
+// Optional fused forward epilogue: interpolate attributes and uv for the winning triangle and sample
+// a 4-channel texture at that uv, with the same arithmetic as the separate kernels.
+struct RasterShade {
+    const float* attrs;
+    uint32_t attribute_count;
+    float* attr_out;
+    const float* uv_attrs;
+    float* uv_out;
+    const float* texture;
+    uint32_t texture_width, texture_height, address_mode;
+    float* sampled;
+};
+
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
-                                  float* raster, float* deriv, cudaStream_t stream);
+                                  float* raster, float* deriv, cudaStream_t stream,
+                                  const RasterShade* shade = nullptr);
 
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,
@@ -60,6 +74,9 @@ cudaError_t launch_texture_backward(const float* tex, size_t tex_view_stride, ui
 #include "../../include/pdr_capi.h"
 
 namespace pdr {
+
+pdr_status set_error(pdr_status code, const char* msg);
+pdr_status set_cuda_error(cudaError_t err, const char* what);
 
 cudaError_t launch_project_views(const float* apos, const float* anrm, const float* araster, uint32_t N,
                                  const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,

@@ -330,32 +330,79 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 }
 
 // ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ----------------------------
+//
+// One CTA per (view, 16x16 tile); each warp owns an 8x4 pixel region. The tile's triangles are
+// staged in shared memory (structure of arrays) 256 at a time. Before the per-pixel tests, every
+// lane takes one triangle of a group of 32 and decides whether any pixel of the warp's region can
+// pass that triangle's edge tests; only triangles that may pass are tested per pixel.
+//
+// The cull is rigorous. The exact edge function e(s) = cross(a - s, b - s) is linear in the sample
+// s (the s x s terms cancel), so over the region's sample box its extremes sit at the four corner
+// samples. The fp32 value a pixel computes, fl(e) = fl(fl(fl(ax-sx)*fl(by-sy)) - fl(fl(ay-sy)*fl(bx-sx))),
+// differs from the exact e by at most 4u(|A B| + |C D|) (u = 2^-24, four roundings per term), and the
+// corner values computed in fp32 carry the same bound. A triangle is skipped for the region when,
+// for one edge, the corner maximum plus 1e-6 * max(|A B| + |C D|) (about 17u, a generous bound of
+// both errors) still fails the reference's test fl(e) * sign < -1e-7 -- then every pixel of the
+// region fails it too, and the per-pixel loop would have skipped the triangle. Results are
+// unchanged; the depth test keeps the minimum (depth, id) as the reference's sequential loop does.
 
-struct TriSetup {
-    float s0x, s0y, s1x, s1y, s2x, s2y;
-    float4 p0, p1, p2;
-    float sign;  // coverage sign, or 0 when the triangle is skipped for every pixel
-    uint32_t t;
+constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA, eight 8x4 warp regions
+
+struct TileTriangles {
+    float s0x[kRasterThreads], s0y[kRasterThreads], s1x[kRasterThreads], s1y[kRasterThreads];
+    float s2x[kRasterThreads], s2y[kRasterThreads], sign[kRasterThreads];
+    uint32_t t[kRasterThreads];
+    float4 p0[kRasterThreads], p1[kRasterThreads], p2[kRasterThreads];
 };
 
-constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA
+// true when fl(cross(a - s, b - s)) * sign < -1e-7 holds for every sample s of the region box
+__device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx, float by, float sign, float sx_lo,
+                                                    float sx_hi, float sy_lo, float sy_hi) {
+    const float e00 = cross2(ax - sx_lo, ay - sy_lo, bx - sx_lo, by - sy_lo);
+    const float e10 = cross2(ax - sx_hi, ay - sy_lo, bx - sx_hi, by - sy_lo);
+    const float e01 = cross2(ax - sx_lo, ay - sy_hi, bx - sx_lo, by - sy_hi);
+    const float e11 = cross2(ax - sx_hi, ay - sy_hi, bx - sx_hi, by - sy_hi);
+    const float mA = fmaxf(fabsf(ax - sx_lo), fabsf(ax - sx_hi)), mD = fmaxf(fabsf(bx - sx_lo), fabsf(bx - sx_hi));
+    const float mB = fmaxf(fabsf(by - sy_lo), fabsf(by - sy_hi)), mC = fmaxf(fabsf(ay - sy_lo), fabsf(ay - sy_hi));
+    const float slack = 1e-6f * (mA * mB + mC * mD);
+    const float probe = e00 + e10 + e01 + e11 + slack;
+    if (probe != probe || isinf(probe)) return false;  // NaN or overflow: never cull
+    if (sign > 0.0f) return fmaxf(fmaxf(e00, e10), fmaxf(e01, e11)) + slack < -1e-7f;
+    return fminf(fminf(e00, e10), fminf(e01, e11)) - slack > 1e-7f;
+}
 
-template <bool kDeriv>
+struct ShadeArgs {
+    const float* attrs;     // [V][A] shared by all views, or nullptr
+    uint32_t A;
+    float* attr_out;        // [views][H][W][A]
+    const float2* uv_attrs; // [V][2], or nullptr
+    float2* uv_out;         // [views][H][W][2]
+    const float4* tex;      // [th][tw][4], or nullptr
+    uint32_t tw, th, mode;
+    float4* sampled;        // [views][H][W][4]
+};
+
+template <bool kDeriv, bool kShade>
 __global__ void __launch_bounds__(kRasterThreads)
 raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
                       const uint32_t* __restrict__ list, unsigned long long capacity, float4* __restrict__ raster,
-                      float4* __restrict__ deriv) {
-    __shared__ TriSetup tri[kRasterThreads];
+                      float4* __restrict__ deriv, ShadeArgs shade) {
+    __shared__ TileTriangles tri;
     const uint32_t view = blockIdx.y;
     const uint32_t tile = blockIdx.x;
     const float4* __restrict__ clip = clip_all + (size_t)view * V;
     const float4 vp = viewports[view];
-    const uint32_t px = (tile % tcx) * kTile + (threadIdx.x & 15u);
-    const uint32_t py = (tile / tcx) * kTile + (threadIdx.x >> 4);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t rx = (tile % tcx) * kTile + (warp & 1u) * 8u;   // region origin
+    const uint32_t ry = (tile / tcx) * kTile + (warp >> 1) * 4u;
+    const uint32_t px = rx + (lane & 7u);
+    const uint32_t py = ry + (lane >> 3);
     const float sx = sample_ndc(px, vp.x, vp.z);
     const float sy = sample_ndc(py, vp.y, vp.w);
+    const float sx_lo = sample_ndc(rx, vp.x, vp.z), sx_hi = sample_ndc(rx + 7u, vp.x, vp.z);
+    const float sy_lo = sample_ndc(ry, vp.y, vp.w), sy_hi = sample_ndc(ry + 3u, vp.y, vp.w);
     const uint32_t seg = view * tiles + tile;
     const uint32_t b = offsets[seg];
     uint32_t e = offsets[seg + 1];
@@ -369,55 +416,81 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
         __syncthreads();
         const uint32_t i = chunk + threadIdx.x;
         if (i < e) {
-            TriSetup s;
-            s.t = list[i];
-            s.sign = 0.0f;
-            const uint3 vi = idx[s.t];
+            const uint32_t t = list[i];
+            float sgn = 0.0f;
+            float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
+            float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f, s2x = 0.f, s2y = 0.f;
+            const uint3 vi = idx[t];
             if (vi.x < V && vi.y < V && vi.z < V) {
-                s.p0 = clip[vi.x];
-                s.p1 = clip[vi.y];
-                s.p2 = clip[vi.z];
-                if (!(s.p0.w <= 1e-8f || s.p1.w <= 1e-8f || s.p2.w <= 1e-8f)) {
-                    s.s0x = s.p0.x / s.p0.w; s.s0y = s.p0.y / s.p0.w;
-                    s.s1x = s.p1.x / s.p1.w; s.s1y = s.p1.y / s.p1.w;
-                    s.s2x = s.p2.x / s.p2.w; s.s2y = s.p2.y / s.p2.w;
-                    const float area = cross2(s.s1x - s.s0x, s.s1y - s.s0y, s.s2x - s.s0x, s.s2y - s.s0y);
+                p0 = clip[vi.x];
+                p1 = clip[vi.y];
+                p2 = clip[vi.z];
+                if (!(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f)) {
+                    s0x = p0.x / p0.w; s0y = p0.y / p0.w;
+                    s1x = p1.x / p1.w; s1y = p1.y / p1.w;
+                    s2x = p2.x / p2.w; s2y = p2.y / p2.w;
+                    const float area = cross2(s1x - s0x, s1y - s0y, s2x - s0x, s2y - s0y);
                     const bool skip = fabsf(area) <= 1e-12f || (cull == 1 && area <= 0.0f) || (cull == 2 && area >= 0.0f);
-                    if (!skip) s.sign = area > 0.0f ? 1.0f : -1.0f;
+                    if (!skip) sgn = area > 0.0f ? 1.0f : -1.0f;
                 }
             }
-            tri[threadIdx.x] = s;
+            tri.s0x[threadIdx.x] = s0x; tri.s0y[threadIdx.x] = s0y;
+            tri.s1x[threadIdx.x] = s1x; tri.s1y[threadIdx.x] = s1y;
+            tri.s2x[threadIdx.x] = s2x; tri.s2y[threadIdx.x] = s2y;
+            tri.sign[threadIdx.x] = sgn;
+            tri.t[threadIdx.x] = t;
+            tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
         }
         __syncthreads();
         const uint32_t n = min(e - chunk, (uint32_t)kRasterThreads);
-        for (uint32_t j = 0; j < n; ++j) {
-            const TriSetup& s = tri[j];
-            if (s.sign == 0.0f) continue;
-            const float e0 = cross2(s.s1x - sx, s.s1y - sy, s.s2x - sx, s.s2y - sy);
-            const float e1 = cross2(s.s2x - sx, s.s2y - sy, s.s0x - sx, s.s0y - sy);
-            const float e2 = cross2(s.s0x - sx, s.s0y - sy, s.s1x - sx, s.s1y - sy);
-            const float ceps = -1e-7f;
-            if (e0 * s.sign < ceps || e1 * s.sign < ceps || e2 * s.sign < ceps) continue;
-            const float q0x = s.p0.x - sx * s.p0.w, q0y = s.p0.y - sy * s.p0.w;
-            const float q1x = s.p1.x - sx * s.p1.w, q1y = s.p1.y - sy * s.p1.w;
-            const float q2x = s.p2.x - sx * s.p2.w, q2y = s.p2.y - sy * s.p2.w;
-            const float a0 = cross2(q1x, q1y, q2x, q2y);
-            const float a1 = cross2(q2x, q2y, q0x, q0y);
-            const float a2 = cross2(q0x, q0y, q1x, q1y);
-            const float ha = a0 + a1 + a2;
-            if (fabsf(ha) <= 1e-12f) continue;
-            const float inv = 1.0f / ha;
-            const float iz = s.p0.z * a0 + s.p1.z * a1 + s.p2.z * a2;
-            const float iw = s.p0.w * a0 + s.p1.w * a1 + s.p2.w * a2;
-            if (fabsf(iw) <= 1e-12f) continue;
-            const float depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
-            // nearest depth wins; ties go to the lowest triangle id (rasterize_forward.hlsl:136-140)
-            if (depth > best_depth || (depth == best_depth && best_tri != 0 && s.t + 1 >= best_tri)) continue;
-            best_depth = depth;
-            best_tri = s.t + 1;
-            bb0 = clamp_hlsl(a0 * inv, 0.0f, 1.0f);
-            bb1 = clamp_hlsl(a1 * inv, 0.0f, 1.0f);
-            binv = inv;
+        for (uint32_t g = 0; g < n; g += 32) {
+            const uint32_t j = g + lane;
+            bool maybe = false;
+            if (j < n) {
+                const float sgn = tri.sign[j];
+                if (sgn != 0.0f) {
+                    const float ax0 = tri.s0x[j], ay0 = tri.s0y[j], ax1 = tri.s1x[j], ay1 = tri.s1y[j];
+                    const float ax2 = tri.s2x[j], ay2 = tri.s2y[j];
+                    maybe = !(edge_rejects_region(ax1, ay1, ax2, ay2, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
+                              edge_rejects_region(ax2, ay2, ax0, ay0, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
+                              edge_rejects_region(ax0, ay0, ax1, ay1, sgn, sx_lo, sx_hi, sy_lo, sy_hi));
+                }
+            }
+            unsigned live = __ballot_sync(0xffffffffu, maybe);
+            while (live) {
+                const uint32_t k = g + (uint32_t)(__ffs(live) - 1);
+                live &= live - 1u;
+                const float sgn = tri.sign[k];
+                const float s0x = tri.s0x[k], s0y = tri.s0y[k], s1x = tri.s1x[k], s1y = tri.s1y[k];
+                const float s2x = tri.s2x[k], s2y = tri.s2y[k];
+                const float e0 = cross2(s1x - sx, s1y - sy, s2x - sx, s2y - sy);
+                const float e1 = cross2(s2x - sx, s2y - sy, s0x - sx, s0y - sy);
+                const float e2 = cross2(s0x - sx, s0y - sy, s1x - sx, s1y - sy);
+                const float ceps = -1e-7f;
+                if (e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps) continue;
+                const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
+                const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+                const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+                const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+                const float a0 = cross2(q1x, q1y, q2x, q2y);
+                const float a1 = cross2(q2x, q2y, q0x, q0y);
+                const float a2 = cross2(q0x, q0y, q1x, q1y);
+                const float ha = a0 + a1 + a2;
+                if (fabsf(ha) <= 1e-12f) continue;
+                const float inv = 1.0f / ha;
+                const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
+                const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
+                if (fabsf(iw) <= 1e-12f) continue;
+                const float depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
+                const uint32_t t = tri.t[k];
+                // nearest depth wins; ties go to the lowest triangle id (rasterize_forward.hlsl:136-140)
+                if (depth > best_depth || (depth == best_depth && best_tri != 0 && t + 1 >= best_tri)) continue;
+                best_depth = depth;
+                best_tri = t + 1;
+                bb0 = clamp_hlsl(a0 * inv, 0.0f, 1.0f);
+                bb1 = clamp_hlsl(a1 * inv, 0.0f, 1.0f);
+                binv = inv;
+            }
         }
     }
     if (px >= W || py >= H) return;
@@ -425,11 +498,17 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
     if (best_tri == 0) {
         raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (kDeriv) deriv[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (kShade) {
+            if (shade.attr_out)
+                for (uint32_t a = 0; a < shade.A; ++a) shade.attr_out[pix * shade.A + a] = 0.0f;
+            if (shade.uv_out) shade.uv_out[pix] = make_float2(0.0f, 0.0f);
+            if (shade.sampled) shade.sampled[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         return;
     }
     raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
+    const uint3 vi = idx[best_tri - 1];
     if (kDeriv) {
-        const uint3 vi = idx[best_tri - 1];
         const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
         const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
         const float da0_dy = -p1.x * p2.w + p1.w * p2.x;
@@ -441,6 +520,41 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
         const float dady = da0_dy + da1_dy + da2_dy;
         deriv[pix] = make_float4((da0_dx - bb0 * dadx) * binv * 2.0f / vp.z, (da0_dy - bb0 * dady) * binv * 2.0f / vp.w,
                                  (da1_dx - bb1 * dadx) * binv * 2.0f / vp.z, (da1_dy - bb1 * dady) * binv * 2.0f / vp.w);
+    }
+    if (kShade) {
+        // interpolate_forward.hlsl for the winner (id <= T and indices < V hold here), then
+        // texture_forward.hlsl at the interpolated uv: the same arithmetic as the separate kernels.
+        const float u = bb0, v = bb1, w = 1.0f - u - v;
+        if (shade.attr_out) {
+            const float* at = shade.attrs;
+            const uint32_t A = shade.A;
+            for (uint32_t a = 0; a < A; ++a)
+                shade.attr_out[pix * A + a] = u * __ldg(at + (size_t)vi.x * A + a) + v * __ldg(at + (size_t)vi.y * A + a) +
+                                              w * __ldg(at + (size_t)vi.z * A + a);
+        }
+        if (shade.uv_out) {
+            const float2 t0 = __ldg(shade.uv_attrs + vi.x), t1 = __ldg(shade.uv_attrs + vi.y), t2 = __ldg(shade.uv_attrs + vi.z);
+            const float2 uvp = make_float2(u * t0.x + v * t1.x + w * t2.x, u * t0.y + v * t1.y + w * t2.y);
+            shade.uv_out[pix] = uvp;
+            if (shade.sampled) {
+                const float tx = uvp.x * (float)shade.tw - 0.5f, ty = uvp.y * (float)shade.th - 0.5f;
+                const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+                const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+                const int32_t x0 = address_coordinate(bx, shade.tw, shade.mode), x1 = address_coordinate(add1(bx), shade.tw, shade.mode);
+                const int32_t y0 = address_coordinate(by, shade.th, shade.mode), y1 = address_coordinate(add1(by), shade.th, shade.mode);
+                const float w0 = (1.0f - fx) * (1.0f - fy), w1 = fx * (1.0f - fy), w2 = (1.0f - fx) * fy, w3 = fx * fy;
+                const float4 c0 = __ldg(shade.tex + (size_t)(uint32_t)y0 * shade.tw + (uint32_t)x0);
+                const float4 c1 = __ldg(shade.tex + (size_t)(uint32_t)y0 * shade.tw + (uint32_t)x1);
+                const float4 c2 = __ldg(shade.tex + (size_t)(uint32_t)y1 * shade.tw + (uint32_t)x0);
+                const float4 c3 = __ldg(shade.tex + (size_t)(uint32_t)y1 * shade.tw + (uint32_t)x1);
+                float4 r;
+                r.x = c0.x * w0 + c1.x * w1 + c2.x * w2 + c3.x * w3;
+                r.y = c0.y * w0 + c1.y * w1 + c2.y * w2 + c3.y * w3;
+                r.z = c0.z * w0 + c1.z * w1 + c2.z * w2 + c3.z * w3;
+                r.w = c0.w * w0 + c1.w * w1 + c2.w * w2 + c3.w * w3;
+                shade.sampled[pix] = r;
+            }
+        }
     }
 }
 
@@ -570,19 +684,42 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
-                                  float* raster, float* deriv, cudaStream_t stream) {
+                                  float* raster, float* deriv, cudaStream_t stream, const RasterShade* shade) {
     const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
     const dim3 grid(tcx * tcy, views);
-    if (deriv) {
-        raster_forward_kernel<true><<<grid, kRasterThreads, 0, stream>>>(
-            reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
-            reinterpret_cast<const float4*>(viewports), cull, tcx, tcx * tcy, offsets, list, capacity,
-            reinterpret_cast<float4*>(raster), reinterpret_cast<float4*>(deriv));
+    ShadeArgs sa{};
+    if (shade) {
+        sa.attrs = shade->attrs;
+        sa.A = shade->attribute_count;
+        sa.attr_out = shade->attr_out;
+        sa.uv_attrs = reinterpret_cast<const float2*>(shade->uv_attrs);
+        sa.uv_out = reinterpret_cast<float2*>(shade->uv_out);
+        sa.tex = reinterpret_cast<const float4*>(shade->texture);
+        sa.tw = shade->texture_width;
+        sa.th = shade->texture_height;
+        sa.mode = shade->address_mode;
+        sa.sampled = reinterpret_cast<float4*>(shade->sampled);
+    }
+    const float4* c4 = reinterpret_cast<const float4*>(clip);
+    const uint3* i3 = reinterpret_cast<const uint3*>(idx);
+    const float4* v4 = reinterpret_cast<const float4*>(viewports);
+    float4* r4 = reinterpret_cast<float4*>(raster);
+    float4* d4 = reinterpret_cast<float4*>(deriv);
+    const uint32_t tiles = tcx * tcy;
+    if (shade) {
+        if (deriv)
+            raster_forward_kernel<true, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
+                                                                                  offsets, list, capacity, r4, d4, sa);
+        else
+            raster_forward_kernel<false, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
+                                                                                   offsets, list, capacity, r4, nullptr, sa);
     } else {
-        raster_forward_kernel<false><<<grid, kRasterThreads, 0, stream>>>(
-            reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
-            reinterpret_cast<const float4*>(viewports), cull, tcx, tcx * tcy, offsets, list, capacity,
-            reinterpret_cast<float4*>(raster), nullptr);
+        if (deriv)
+            raster_forward_kernel<true, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
+                                                                                   offsets, list, capacity, r4, d4, sa);
+        else
+            raster_forward_kernel<false, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
+                                                                                    offsets, list, capacity, r4, nullptr, sa);
     }
     return cudaGetLastError();
 }

@@ -16,14 +16,33 @@ from . import _native
 from .rasterizer import Rasterizer, TILE, _ptr, _viewports
 
 
+class RenderArgsC(C.Structure):
+    """include/pdr_capi.h pdr_render_args."""
+
+    _fields_ = [
+        ("clip_positions", C.c_void_p), ("views", C.c_uint32), ("vertex_count", C.c_uint32), ("indices", C.c_void_p),
+        ("triangle_count", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("viewports", C.c_void_p),
+        ("cull_mode", C.c_uint32), ("attributes", C.c_void_p), ("attribute_count", C.c_uint32),
+        ("uv_attributes", C.c_void_p), ("texture", C.c_void_p), ("texture_width", C.c_uint32),
+        ("texture_height", C.c_uint32), ("address_mode", C.c_uint32), ("tile_offsets", C.c_void_p),
+        ("tile_triangles", C.c_void_p), ("capacity", C.c_uint64), ("workspace", C.c_void_p),
+        ("workspace_bytes", C.c_size_t), ("status", C.c_void_p), ("raster", C.c_void_p),
+        ("barycentric_derivatives", C.c_void_p), ("interpolated", C.c_void_p), ("uv", C.c_void_p),
+        ("sampled", C.c_void_p), ("grad_interpolated", C.c_void_p), ("grad_sampled", C.c_void_p),
+        ("grad_clip_positions", C.c_void_p), ("grad_attributes", C.c_void_p), ("grad_uv_attributes", C.c_void_p),
+        ("grad_texture", C.c_void_p),
+    ]
+
+
 class RenderFwdBwd:
     """Batched fwd+bwd of rasterize (with derivatives) -> interpolate(attributes) and interpolate(uv)
     -> texture, for `views` views of one mesh at one resolution."""
 
     def __init__(self, rasterizer: Rasterizer, indices: torch.Tensor, vertex_count: int, views: int, height: int,
                  width: int, attribute_count: int, texture_shape, viewports=None, capacity: Optional[int] = None,
-                 address_mode: int = 0):
+                 address_mode: int = 0, fused: bool = True):
         self.r = rasterizer
+        self.fused = fused
         ctx = rasterizer.context
         dev = ctx.device
         self.idx = indices.to(dev, torch.int32).contiguous()
@@ -61,9 +80,30 @@ class RenderFwdBwd:
             raise OverflowError(f"tile list needs {int(st[0]) & 0xFFFFFFFF} entries, capacity {self.capacity}")
         return int(st[0]) & 0xFFFFFFFF
 
+    def _args(self, clip, attrs, uv_attrs, texture, grad_attr_out=None, grad_sampled=None) -> RenderArgsC:
+        a = RenderArgsC()
+        a.clip_positions, a.views, a.vertex_count = clip.data_ptr(), self.views, self.V
+        a.indices, a.triangle_count, a.width, a.height = self.idx.data_ptr(), self.T, self.W, self.H
+        a.viewports, a.cull_mode = self.vps.data_ptr(), 0
+        a.attributes, a.attribute_count, a.uv_attributes = attrs.data_ptr(), self.A, uv_attrs.data_ptr()
+        a.texture, a.texture_width, a.texture_height, a.address_mode = texture.data_ptr(), self.tw, self.th, self.mode
+        a.tile_offsets, a.tile_triangles, a.capacity = self.offsets.data_ptr(), self.list.data_ptr(), self.capacity
+        a.workspace, a.workspace_bytes, a.status = self.ws.data_ptr(), self.ws_bytes, self.status.data_ptr()
+        a.raster, a.barycentric_derivatives = self.raster.data_ptr(), self.deriv.data_ptr()
+        a.interpolated, a.uv, a.sampled = self.attr_out.data_ptr(), self.uv.data_ptr(), self.sampled.data_ptr()
+        if grad_attr_out is not None:
+            a.grad_interpolated, a.grad_sampled = grad_attr_out.data_ptr(), grad_sampled.data_ptr()
+        a.grad_clip_positions, a.grad_attributes = self.grad_clip.data_ptr(), self.grad_attr.data_ptr()
+        a.grad_uv_attributes, a.grad_texture = self.grad_uv_attr.data_ptr(), self.grad_tex.data_ptr()
+        return a
+
     def forward(self, clip: torch.Tensor, attrs: torch.Tensor, uv_attrs: torch.Tensor, texture: torch.Tensor,
                 stream) -> None:
         L = _native.lib()
+        if self.fused:
+            a = self._args(clip, attrs, uv_attrs, texture)
+            _native.check(L.pdr_render_forward(C.addressof(a), stream))
+            return
         v, V, T, W, H = self.views, self.V, self.T, self.W, self.H
         _native.check(L.pdr_bin_tiles(_ptr(clip), v, V, _ptr(self.idx), T, W, H, _ptr(self.vps), _ptr(self.offsets),
                                       _ptr(self.list), self.capacity, _ptr(self.ws), self.ws_bytes, _ptr(self.status),
@@ -81,6 +121,10 @@ class RenderFwdBwd:
     def backward(self, clip: torch.Tensor, attrs: torch.Tensor, uv_attrs: torch.Tensor, texture: torch.Tensor,
                  grad_attr_out: torch.Tensor, grad_sampled: torch.Tensor, stream) -> None:
         L = _native.lib()
+        if self.fused:
+            a = self._args(clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled)
+            _native.check(L.pdr_render_backward(C.addressof(a), stream))
+            return
         v, V, T, W, H = self.views, self.V, self.T, self.W, self.H
         _native.check(L.pdr_texture_backward(_ptr(texture), 0, self.tw, self.th, self.C, self.mode, _ptr(self.uv),
                                              _ptr(self.raster), v, self.P, _ptr(grad_sampled), _ptr(self.grad_tex),
@@ -101,6 +145,8 @@ class RenderFwdBwd:
         self.forward(clip, attrs, uv_attrs, texture, stream)
         self.backward(clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled, stream)
 
-    # number of kernels one step launches (bin: count, 3 scan, fill, 2 sort; raster; 3 forward;
-    # texture backward; 2 interpolate backward; raster backward) and the memsets it issues
-    KERNELS_PER_STEP = 7 + 1 + 3 + 1 + 2 + 1
+    def kernels_per_step(self) -> int:
+        """Kernels one step launches: binning (count, three scan phases, fill, two sort passes), then
+        fused: raster with the shading epilogue + one backward; unfused: raster, three forwards,
+        texture backward, two interpolate backwards, raster backward."""
+        return 7 + (1 + 1 if self.fused else 1 + 3 + 1 + 2 + 1)
