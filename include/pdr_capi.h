@@ -285,6 +285,25 @@ PDR_API pdr_status pdr_render_forward(const pdr_render_args* args, void* stream)
 PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream);
 
 
+/* ---- allocation-free binning ------------------------------------------------------------------ */
+
+/* Size of the fixed scratch array behind pdr_bin_tiles_no_alloc (16 MiB). */
+#define PDR_BIN_TILES_NO_ALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* pdr_bin_tiles without a caller workspace; no counterpart in the reference. For callers that cannot
+ * allocate device memory: code running inside another component's CUDA-graph capture, real-time
+ * loops that must avoid cudaMalloc's synchronisation, plugin hosts that hand out buffers but no
+ * allocator. Inputs, outputs and status are the caller's, exactly as for pdr_bin_tiles; the scratch
+ * is a 16 MiB array compiled into the library and held on every GPU that loads it until the process
+ * exits. Bins needing more scratch than that (pdr_bin_tiles_workspace_bytes() > 16 MiB) are rejected
+ * with PDR_INVALID_ARGUMENT. The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress); make it before any stream capture. Every call shares the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
+PDR_API pdr_status pdr_bin_tiles_no_alloc(const float* clip_positions, uint32_t views, uint32_t vertex_count,
+                                          const uint32_t* indices, uint32_t triangle_count, uint32_t width,
+                                          uint32_t height, const float* viewports, uint32_t* tile_offsets,
+                                          uint32_t* tile_triangles, uint64_t capacity, uint32_t* status,
+                                          void* stream);
 
 #ifdef __cplusplus
 }

@@ -11,7 +11,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphotara_drender_gb300.so")
-SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "capi.cu"]
+SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
