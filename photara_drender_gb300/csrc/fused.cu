@@ -6,9 +6,10 @@
 // Backward: one thread per pixel runs, in the reference's order and arithmetic, texture_grad_texture
 // (double-exact weights, vector atomics), texture_grad_uv, interpolate_grad_attributes /
 // interpolate_grad_raster for both attribute sets, and rasterize_backward for the summed raster
-// gradient. Per-vertex gradients of a 16x16 tile are first summed in a shared-memory hash table and
-// flushed with one atomic per (vertex, component); intermediate grad_uv / grad_raster never leave
-// registers.
+// gradient. Per-vertex gradients are summed in three stages: over each run of adjacent pixels of a
+// warp that hit the same triangle (warp shuffles), then per 16x16 tile in a shared-memory hash table
+// written only by each run's last lane, then flushed with one global atomic per (vertex, component).
+// Intermediate grad_uv / grad_raster never leave registers.
 #include <cuda_runtime.h>
 
 #include "../../include/pdr_capi.h"
@@ -44,52 +45,74 @@ __device__ __forceinline__ uint32_t table_slot(VertexTable& tb, uint32_t v) {
     return kSlots;
 }
 
-struct VertexSink {
-    VertexTable* tb;
-    uint32_t nv;  // values per vertex in the table: uv (2), attributes (A), clip x/y/w (3)
+// Segmented inclusive sums over runs of equal keys in a warp (Hillis-Steele with head flags). The
+// add predicates depend only on the keys, so they are computed once and reused for every value.
+struct RunScan {
+    bool add[5];
+    bool tail;
+    __device__ __forceinline__ explicit RunScan(uint32_t key) {
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+        const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
+        bool f = lane == 0 || prev != key;
+        tail = lane == 31 || next != key;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+            const uint32_t o = 1u << s;
+            const bool fy = __shfl_up_sync(0xffffffffu, f, o);
+            add[s] = lane >= o && !f;
+            f = f || (lane >= o && fy);
+        }
+    }
+    __device__ __forceinline__ float sum(float x) const {
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+            const float y = __shfl_up_sync(0xffffffffu, x, 1u << s);
+            if (add[s]) x += y;
+        }
+        return x;
+    }
 };
 
-// Adds n values at offset `off` of vertex v's table entry; false when the table is full (the caller
-// then adds to global memory directly).
-__device__ __forceinline__ bool sink_add(const VertexSink& s, uint32_t v, uint32_t off, const float* vals, uint32_t n) {
-    const uint32_t slot = table_slot(*s.tb, v);
-    if (slot >= kSlots) return false;
-    float* dst = s.tb->val + (size_t)slot * s.nv + off;
-    for (uint32_t i = 0; i < n; ++i)
-        if (vals[i] != 0.0f) atomicAdd(dst + i, vals[i]);
-    return true;
-}
-
+template <int kA>
 __global__ void __launch_bounds__(kFusedThreads)
 render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
-                       const float* __restrict__ attrs, uint32_t A, const float2* __restrict__ uv_attrs,
+                       const float* __restrict__ attrs, const float2* __restrict__ uv_attrs,
                        const float4* __restrict__ tex, uint32_t tw, uint32_t th, uint32_t mode,
                        const float4* __restrict__ raster, const float2* __restrict__ uv,
                        const float* __restrict__ grad_attr_out, const float4* __restrict__ grad_sampled,
                        float* __restrict__ g_clip_all, float* __restrict__ g_attr, float* __restrict__ g_uv,
                        float* __restrict__ g_tex, uint32_t* __restrict__ status) {
+    constexpr uint32_t kNV = 2 + kA + 3;  // per vertex: uv attributes, attributes, clip x/y/w
     __shared__ VertexTable tb;
     const uint32_t view = blockIdx.y;
     const uint32_t tile = blockIdx.x;
-    const uint32_t nv = 2 + A + 3;
     for (uint32_t i = threadIdx.x; i < kSlots; i += kFusedThreads) tb.key[i] = kEmpty;
-    for (uint32_t i = threadIdx.x; i < kSlots * nv; i += kFusedThreads) tb.val[i] = 0.0f;
+    for (uint32_t i = threadIdx.x; i < kSlots * kNV; i += kFusedThreads) tb.val[i] = 0.0f;
     __syncthreads();
     float* g_clip = g_clip_all + (size_t)view * V * 4;
-    VertexSink sink{&tb, nv};
+    const uint32_t lane = threadIdx.x & 31u;
 
     const uint32_t px = (tile % tcx) * kTile + (threadIdx.x & 15u);
     const uint32_t py = (tile / tcx) * kTile + (threadIdx.x >> 4);
+    bool valid = false;           // pixel contributes vertex gradients (id in [1, T])
+    uint3 vi = make_uint3(0, 0, 0);
+    float cv[3][kNV];             // per corner contributions
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (uint32_t j = 0; j < kNV; ++j) cv[k][j] = 0.0f;
+    uint32_t id = 0;
+
     if (px < W && py < H) {
         const size_t pix = ((size_t)view * H + py) * W + px;
         const float4 r = raster[pix];
-        const uint32_t id = raster_id(r.w);
+        id = raster_id(r.w);
         const float2 u = uv ? uv[pix] : make_float2(0.0f, 0.0f);
-        float4 gs = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float gux = 0.0f, guy = 0.0f;
         if (tex) {
-            gs = grad_sampled[pix];
+            const float4 gs = grad_sampled[pix];
             // texture_grad_texture: pixels with raster.w != 0, double-exact weights (rasterizer.cpp:198-229)
             if (r.w != 0.0f) {
                 int32_t bx, by;
@@ -134,15 +157,21 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
             }
         }
         if (id != 0 && id <= T) {
-            const uint3 vi = idx[id - 1];
+            valid = true;
+            vi = idx[id - 1];
             const float bu = r.x, bv = r.y;
             const uint32_t vs[3] = {vi.x, vi.y, vi.z};
             const bool inside = vi.x < V && vi.y < V && vi.z < V;
-            // interpolate_grad_attributes for uv and attributes (distinct vertices, accumulated weight)
+            float ga[kA > 0 ? kA : 1];
+#pragma unroll
+            for (int a = 0; a < kA; ++a) ga[a] = grad_attr_out[pix * kA + a];
+            // interpolate_grad_attributes for uv and attributes: each distinct vertex once, with the
+            // weight accumulated as interpolate_grad_attributes.hlsl:42-54 does
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const uint32_t vx = vs[k];
                 bool first = true;
+#pragma unroll
                 for (int j = 0; j < k; ++j) first = first && vs[j] != vx;
                 if (!first || vx >= V) continue;
                 float wgt = 0.0f;
@@ -150,20 +179,13 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
                 if (vi.y == vx) wgt += bv;
                 if (vi.z == vx) wgt += 1.0f - bu - bv;
                 if (uv_attrs) {
-                    const float vals[2] = {wgt * gux, wgt * guy};
-                    if (!sink_add(sink, vx, 0, vals, 2)) {
-                        atomicAdd(g_uv + (size_t)vx * 2, vals[0]);
-                        atomicAdd(g_uv + (size_t)vx * 2 + 1, vals[1]);
-                    }
+                    cv[k][0] = wgt * gux;
+                    cv[k][1] = wgt * guy;
                 }
-                if (attrs) {
-                    float vals[8];
-                    for (uint32_t a = 0; a < A; ++a) vals[a] = wgt * grad_attr_out[pix * A + a];
-                    if (!sink_add(sink, vx, 2, vals, A))
-                        for (uint32_t a = 0; a < A; ++a) atomicAdd(g_attr + (size_t)vx * A + a, vals[a]);
-                }
+#pragma unroll
+                for (int a = 0; a < kA; ++a) cv[k][2 + a] = wgt * ga[a];
             }
-            // interpolate_grad_raster: uv attributes first, then attributes accumulated on top
+            // interpolate_grad_raster: uv attributes first, attributes accumulated on top
             float grx = 0.0f, gry = 0.0f;
             if (inside) {
                 if (uv_attrs) {
@@ -173,14 +195,14 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
                     grx += guy * (t0.y - t2.y);
                     gry += guy * (t1.y - t2.y);
                 }
-                if (attrs) {
+                if (kA > 0) {
                     float ax = 0.0f, ay = 0.0f;
-                    for (uint32_t a = 0; a < A; ++a) {
-                        const float g = grad_attr_out[pix * A + a];
-                        const float a0 = __ldg(attrs + (size_t)vi.x * A + a), a1 = __ldg(attrs + (size_t)vi.y * A + a);
-                        const float a2 = __ldg(attrs + (size_t)vi.z * A + a);
-                        ax += g * (a0 - a2);
-                        ay += g * (a1 - a2);
+#pragma unroll
+                    for (int a = 0; a < kA; ++a) {
+                        const float a0 = __ldg(attrs + (size_t)vi.x * kA + a), a1 = __ldg(attrs + (size_t)vi.y * kA + a);
+                        const float a2 = __ldg(attrs + (size_t)vi.z * kA + a);
+                        ax += ga[a] * (a0 - a2);
+                        ay += ga[a] * (a1 - a2);
                     }
                     grx = grx + ax;
                     gry = gry + ay;
@@ -225,38 +247,61 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
                         const float g0y = gc * (q1x - q2x) + gb1 * q2x;
                         const float g1y = gc * (q2x - q0x) - gb0 * q2x;
                         const float g2y = gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x;
-                        const float c0[3] = {g0x, g0y, -sx * g0x - sy * g0y};
-                        const float c1[3] = {g1x, g1y, -sx * g1x - sy * g1y};
-                        const float c2[3] = {g2x, g2y, -sx * g2x - sy * g2y};
-                        // table layout x, y, w; clip gradients are components 0, 1 and 3 (z stays 0)
-                        const uint32_t corners[3] = {vi.x, vi.y, vi.z};
-                        const float* cg[3] = {c0, c1, c2};
-                        for (int k = 0; k < 3; ++k) {
-                            if (!sink_add(sink, corners[k], 2 + A, cg[k], 3)) {
-                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 0, cg[k][0]);
-                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 1, cg[k][1]);
-                                atomicAdd(g_clip + (size_t)corners[k] * 4 + 3, cg[k][2]);
-                            }
-                        }
+                        cv[0][2 + kA] = g0x; cv[0][3 + kA] = g0y; cv[0][4 + kA] = -sx * g0x - sy * g0y;
+                        cv[1][2 + kA] = g1x; cv[1][3 + kA] = g1y; cv[1][4 + kA] = -sx * g1x - sy * g1y;
+                        cv[2][2 + kA] = g2x; cv[2][3 + kA] = g2y; cv[2][4 + kA] = -sx * g2x - sy * g2y;
                     }
                 }
             }
         }
     }
+    // Runs of pixels on the same triangle are contiguous along the tile row a warp covers: sum each
+    // run in registers, then only the run's last lane touches the shared table.
+    const uint32_t key = valid ? id : (0x80000000u | lane);
+    const RunScan scan(key);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (uint32_t j = 0; j < kNV; ++j) cv[k][j] = scan.sum(cv[k][j]);
+    if (valid && scan.tail) {
+        const uint32_t corners[3] = {vi.x, vi.y, vi.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t v = corners[k];
+            if (v >= V) continue;
+            const uint32_t slot = table_slot(tb, v);
+            if (slot < kSlots) {
+                float* dst = tb.val + (size_t)slot * kNV;
+#pragma unroll
+                for (uint32_t j = 0; j < kNV; ++j)
+                    if (cv[k][j] != 0.0f) atomicAdd(dst + j, cv[k][j]);
+            } else {  // table full: straight to global memory
+                if (g_uv) {
+                    atomicAdd(g_uv + (size_t)v * 2, cv[k][0]);
+                    atomicAdd(g_uv + (size_t)v * 2 + 1, cv[k][1]);
+                }
+#pragma unroll
+                for (int a = 0; a < kA; ++a) atomicAdd(g_attr + (size_t)v * kA + a, cv[k][2 + a]);
+                atomicAdd(g_clip + (size_t)v * 4 + 0, cv[k][2 + kA]);
+                atomicAdd(g_clip + (size_t)v * 4 + 1, cv[k][3 + kA]);
+                atomicAdd(g_clip + (size_t)v * 4 + 3, cv[k][4 + kA]);
+            }
+        }
+    }
     __syncthreads();
     // flush: one atomic per non-zero (vertex, component)
-    for (uint32_t s = threadIdx.x; s < kSlots; s += kFusedThreads) {
-        const uint32_t v = tb.key[s];
+    for (uint32_t sl = threadIdx.x; sl < kSlots; sl += kFusedThreads) {
+        const uint32_t v = tb.key[sl];
         if (v == kEmpty) continue;
-        const float* src = tb.val + (size_t)s * nv;
+        const float* src = tb.val + (size_t)sl * kNV;
         if (g_uv) {
             if (src[0] != 0.0f) atomicAdd(g_uv + (size_t)v * 2, src[0]);
             if (src[1] != 0.0f) atomicAdd(g_uv + (size_t)v * 2 + 1, src[1]);
         }
-        if (g_attr)
-            for (uint32_t a = 0; a < A; ++a)
-                if (src[2 + a] != 0.0f) atomicAdd(g_attr + (size_t)v * A + a, src[2 + a]);
-        const float* pc = src + 2 + A;
+#pragma unroll
+        for (int a = 0; a < kA; ++a)
+            if (src[2 + a] != 0.0f) atomicAdd(g_attr + (size_t)v * kA + a, src[2 + a]);
+        const float* pc = src + 2 + kA;
         if (pc[0] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 0, pc[0]);
         if (pc[1] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 1, pc[1]);
         if (pc[2] != 0.0f) atomicAdd(g_clip + (size_t)v * 4 + 3, pc[2]);
@@ -322,14 +367,27 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
     if (err != cudaSuccess) return set_cuda_error(err, "render_backward(memset)");
     const uint32_t tcx = (a->width + kTile - 1) / kTile, tcy = (a->height + kTile - 1) / kTile;
     const dim3 grid(tcx * tcy, a->views);
-    render_backward_kernel<<<grid, kFusedThreads, 0, s>>>(
-        reinterpret_cast<const float4*>(a->clip_positions), a->vertex_count, reinterpret_cast<const uint3*>(a->indices),
-        a->triangle_count, a->width, a->height, reinterpret_cast<const float4*>(a->viewports), tcx, a->attributes,
-        a->attributes ? a->attribute_count : 0, reinterpret_cast<const float2*>(a->uv_attributes),
-        reinterpret_cast<const float4*>(a->texture), a->texture_width, a->texture_height, a->address_mode,
-        reinterpret_cast<const float4*>(a->raster), reinterpret_cast<const float2*>(a->uv), a->grad_interpolated,
-        reinterpret_cast<const float4*>(a->grad_sampled), a->grad_clip_positions, a->grad_attributes,
-        a->grad_uv_attributes, a->grad_texture, a->status);
+    const uint32_t A = a->attributes ? a->attribute_count : 0;
+#define PDR_RENDER_BWD(KA)                                                                                          \
+    render_backward_kernel<KA><<<grid, kFusedThreads, 0, s>>>(                                                      \
+        reinterpret_cast<const float4*>(a->clip_positions), a->vertex_count, reinterpret_cast<const uint3*>(a->indices), \
+        a->triangle_count, a->width, a->height, reinterpret_cast<const float4*>(a->viewports), tcx, a->attributes,   \
+        reinterpret_cast<const float2*>(a->uv_attributes), reinterpret_cast<const float4*>(a->texture),            \
+        a->texture_width, a->texture_height, a->address_mode, reinterpret_cast<const float4*>(a->raster),           \
+        reinterpret_cast<const float2*>(a->uv), a->grad_interpolated, reinterpret_cast<const float4*>(a->grad_sampled), \
+        a->grad_clip_positions, a->grad_attributes, a->grad_uv_attributes, a->grad_texture, a->status)
+    switch (A) {
+        case 0: PDR_RENDER_BWD(0); break;
+        case 1: PDR_RENDER_BWD(1); break;
+        case 2: PDR_RENDER_BWD(2); break;
+        case 3: PDR_RENDER_BWD(3); break;
+        case 4: PDR_RENDER_BWD(4); break;
+        case 5: PDR_RENDER_BWD(5); break;
+        case 6: PDR_RENDER_BWD(6); break;
+        case 7: PDR_RENDER_BWD(7); break;
+        default: PDR_RENDER_BWD(8); break;
+    }
+#undef PDR_RENDER_BWD
     return set_cuda_error(cudaGetLastError(), "render_backward");
 }
 
