@@ -11,6 +11,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphotara_drender_gb300.so")
+CPP_LIB = os.path.join(HERE, "libphotara_drender.so")  # the C++ API of include/photara_drender/*.hpp
+CPP_SOURCES = [os.path.join(HERE, "cpp", "photara_drender.cpp")]
 SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
@@ -22,6 +24,10 @@ def nvcc() -> str:
     if not os.path.exists(path):
         raise RuntimeError("nvcc not found: the CUDA toolkit is required to build photara_drender_gb300")
     return path
+
+
+def cuda_lib_dir() -> str:
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
 
 
 def _deps() -> list[str]:
@@ -52,12 +58,33 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(SOURCES))) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"], check=True)
+    subprocess.run([cc, *ARCH, "-shared", "--cudart", "shared", "-Xlinker", f"-rpath,{cuda_lib_dir()}", "-o", tmp,
+                    *objs], check=True)
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_cpp(force: bool = False) -> str:
+    """Builds the C++ API library (photara_drender::Context, Rasterizer, TextureBaker, TextureRefiner)
+    over the C ABI library; it needs C++20 for std::span, as the reference's headers do."""
+    lib = build(force=force)
+    deps = CPP_SOURCES + [lib] + [os.path.join(INCLUDE, "photara_drender", f)
+                                  for f in os.listdir(os.path.join(INCLUDE, "photara_drender"))]
+    if not force and os.path.exists(CPP_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(CPP_LIB) for d in deps):
+        return CPP_LIB
+    tmp = CPP_LIB + f".tmp{os.getpid()}"
+    cmd = [nvcc(), "-std=c++20", "-O2", "-Xcompiler", "-fPIC,-Wall", "-shared", "--cudart", "shared", "-I", INCLUDE,
+           *CPP_SOURCES,
+           "-o", tmp, "-L", HERE, "-lphotara_drender_gb300", "-Xlinker", f"-rpath,$ORIGIN:{cuda_lib_dir()}"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"building the C++ API failed:\n{res.stderr}")
+    os.replace(tmp, CPP_LIB)
+    return CPP_LIB
 
 
 if __name__ == "__main__":
     import sys
 
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_cpp())

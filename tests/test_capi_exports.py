@@ -48,3 +48,20 @@ def test_status_codes_without_gpu():
         _native.check(L.pdr_rasterize_forward(None, 1, 3, None, 1, 8, 8, None, 0, None, None, 0, None, None, None))
     with pytest.raises(ValueError):
         _native.check(L.pdr_texture_forward(None, 0, 4, 4, 3, 0, None, None, 1, 16, None, None))
+
+
+def test_cpp_api_library_builds_and_links():
+    """The C++ API library builds over the C ABI and the native C++ test links against it (the
+    test itself needs a GPU and runs in tests/test_gpu_cpp_api.py)."""
+    import shutil
+    import subprocess
+
+    from photara_drender_gb300 import build
+
+    lib = build.build_cpp()
+    exe = os.path.join(os.path.dirname(lib), "_build", "cpp_api_test_link_check")
+    subprocess.run([shutil.which("g++") or "g++", "-std=c++20", "-O0", "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "native", "cpp_api_test.cpp"), "-o",
+                    exe, "-L", os.path.dirname(lib), "-lphotara_drender", f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                   check=True)
+    assert os.path.exists(exe)
