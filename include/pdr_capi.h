@@ -278,7 +278,8 @@ PDR_API size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_coun
                                           uint64_t capacity);
 /* Tile binning and one raster launch whose epilogue interpolates both attribute sets and samples the
  * texture for every pixel: the outputs of Rasterizer::forward + interpolate_forward (x2) +
- * texture_forward, bit-identical to the separate calls. */
+ * texture_forward, bit-identical to the separate calls. The raster does not depend on the order of
+ * a tile's triangles, so tile_triangles holds each tile's triangles unsorted (pdr_bin_tiles sorts). */
 PDR_API pdr_status pdr_render_forward(const pdr_render_args* args, void* stream);
 /* The adjoints of the forward in one pixel pass: texture_backward, interpolate_backward for both
  * attribute sets (raster gradients summed) and rasterize_backward. */

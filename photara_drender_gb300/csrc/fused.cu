@@ -47,17 +47,27 @@ __device__ __forceinline__ uint32_t table_slot(VertexTable& tb, uint32_t v) {
 
 // Segmented inclusive sums over runs of equal keys in a warp (Hillis-Steele with head flags). The
 // add predicates depend only on the keys, so they are computed once and reused for every value.
+// Step s adds the value 2^s lanes up; a run of length L needs the steps with 2^s < L, so the scan
+// stops after the warp's longest run (usually 2 to 4 pixels of a tile row) instead of after 5 steps.
 struct RunScan {
     bool add[5];
     bool tail;
+    uint32_t steps;  // warp-uniform
     __device__ __forceinline__ explicit RunScan(uint32_t key) {
         const uint32_t lane = threadIdx.x & 31u;
         const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
         const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
         bool f = lane == 0 || prev != key;
         tail = lane == 31 || next != key;
+        // distance to the run's head: lane minus the highest head at or below this lane
+        const uint32_t heads = __ballot_sync(0xffffffffu, f) & (0xffffffffu >> (31u - lane));
+        const uint32_t dist = lane - (31u - (uint32_t)__clz(heads));
+        const uint32_t longest = __reduce_max_sync(0xffffffffu, dist);
+        steps = 32u - (uint32_t)__clz(longest);  // bit length: 2^steps > longest
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
+            add[s] = false;
+            if ((uint32_t)s >= steps) continue;
             const uint32_t o = 1u << s;
             const bool fy = __shfl_up_sync(0xffffffffu, f, o);
             add[s] = lane >= o && !f;
@@ -67,6 +77,7 @@ struct RunScan {
     __device__ __forceinline__ float sum(float x) const {
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
+            if ((uint32_t)s >= steps) break;
             const float y = __shfl_up_sync(0xffffffffu, x, 1u << s);
             if (add[s]) x += y;
         }
@@ -75,7 +86,7 @@ struct RunScan {
 };
 
 template <int kA>
-__global__ void __launch_bounds__(kFusedThreads)
+__global__ void __launch_bounds__(kFusedThreads, 4)
 render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
                        const float* __restrict__ attrs, const float2* __restrict__ uv_attrs,
@@ -337,7 +348,7 @@ pdr_status pdr_render_forward(const pdr_render_args* a, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t err = launch_bin_tiles(a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count,
                                        a->width, a->height, a->viewports, a->tile_offsets, a->tile_triangles,
-                                       a->capacity, a->workspace, a->status, s);
+                                       a->capacity, a->workspace, a->status, s, /*sorted=*/false);
     if (err != cudaSuccess) return set_cuda_error(err, "render_forward(bins)");
     RasterShade shade{a->attributes, a->attribute_count, a->interpolated, a->uv_attributes, a->uv, a->texture,
                       a->texture_width, a->texture_height, a->address_mode, a->sampled};

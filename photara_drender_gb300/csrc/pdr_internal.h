@@ -25,7 +25,8 @@ size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, 
 
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
-                             unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream);
+                             unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream,
+                             bool sorted = true);
 
 // Optional fused forward epilogue: interpolate attributes and uv for the winning triangle and sample
 // a 4-channel texture at that uv, with the same arithmetic as the separate kernels.

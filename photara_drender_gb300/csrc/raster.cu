@@ -332,9 +332,17 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 // ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ----------------------------
 //
 // One CTA per (view, 16x16 tile); each warp owns an 8x4 pixel region. The tile's triangles are
-// staged in shared memory (structure of arrays) 256 at a time. Before the per-pixel tests, every
-// lane takes one triangle of a group of 32 and decides whether any pixel of the warp's region can
-// pass that triangle's edge tests; only triangles that may pass are tested per pixel.
+// staged in shared memory (structure of arrays) 256 at a time. Per warp, three steps:
+//   1. cull: every lane takes one triangle of a group of 32 and decides whether any pixel of the
+//      region can pass that triangle's edge tests;
+//   2. coverage: for each surviving triangle, every lane runs the edge tests for its pixel, and the
+//      passing (triangle, pixel) pairs are appended to a per-warp queue;
+//   3. depth: whenever 32 pairs are queued, each lane takes one pair, computes its depth with the
+//      reference's arithmetic and folds (depth, triangle) into the pixel's winner key with a
+//      shared-memory atomicMin.
+// Small triangles cover a few pixels of a region, so step 3 runs with full warps instead of the
+// few lanes a per-pixel loop would keep busy. Afterwards each pixel recomputes the winner's
+// barycentrics once.
 //
 // The cull is rigorous. The exact edge function e(s) = cross(a - s, b - s) is linear in the sample
 // s (the s x s terms cancel), so over the region's sample box its extremes sit at the four corner
@@ -369,6 +377,15 @@ __device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx
     if (probe != probe || isinf(probe)) return false;  // NaN or overflow: never cull
     if (sign > 0.0f) return fmaxf(fmaxf(e00, e10), fmaxf(e01, e11)) + slack < -1e-7f;
     return fminf(fminf(e00, e10), fminf(e01, e11)) - slack > 1e-7f;
+}
+
+// Orders (depth, triangle) pairs as the reference's depth test does: nearest depth first (-0 and
+// +0 equal), then the lowest triangle index.
+__device__ __forceinline__ unsigned long long depth_key(float depth, uint32_t t) {
+    uint32_t b = __float_as_uint(depth);
+    if ((b << 1) == 0u) b = 0u;
+    const uint32_t o = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return ((unsigned long long)o << 32) | t;
 }
 
 struct ShadeArgs {
@@ -409,9 +426,13 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
     if (e > capacity) e = (uint32_t)capacity;
     if (b > e) e = b;
 
-    float best_depth = 3.402823466e+38f;
-    uint32_t best_tri = 0;
-    float bb0 = 0.0f, bb1 = 0.0f, binv = 0.0f;
+    // Winner per pixel as a 64-bit key (ordered depth bits << 32 | triangle index): the minimum key is
+    // the nearest depth, ties to the lowest id, exactly the reference's sequential test.
+    __shared__ unsigned long long best_key[kRasterThreads];
+    __shared__ uint32_t queue[kRasterThreads / 32][64];  // per warp: (triangle slot << 5) | pixel lane
+    uint32_t* q = queue[warp];
+    best_key[threadIdx.x] = ~0ull;
+    const bool in_image = px < W && py < H;
     for (uint32_t chunk = b; chunk < e; chunk += kRasterThreads) {
         __syncthreads();
         const uint32_t i = chunk + threadIdx.x;
@@ -443,6 +464,31 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
         }
         __syncthreads();
         const uint32_t n = min(e - chunk, (uint32_t)kRasterThreads);
+        // Depth test of up to 32 queued (triangle, pixel) pairs, one per lane: the reference's
+        // arithmetic at the pair's pixel, folded into the pixel's winner key.
+        auto depth_pairs = [&](uint32_t count) {
+            const uint32_t ent = lane < count ? q[lane] : 0u;
+            const uint32_t pl = ent & 31u, k = ent >> 5;
+            const float psx = __shfl_sync(0xffffffffu, sx, pl);
+            const float psy = __shfl_sync(0xffffffffu, sy, pl);
+            if (lane < count) {
+                const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
+                const float q0x = p0.x - psx * p0.w, q0y = p0.y - psy * p0.w;
+                const float q1x = p1.x - psx * p1.w, q1y = p1.y - psy * p1.w;
+                const float q2x = p2.x - psx * p2.w, q2y = p2.y - psy * p2.w;
+                const float a0 = cross2(q1x, q1y, q2x, q2y);
+                const float a1 = cross2(q2x, q2y, q0x, q0y);
+                const float a2 = cross2(q0x, q0y, q1x, q1y);
+                const float ha = a0 + a1 + a2;
+                if (!(fabsf(ha) <= 1e-12f)) {
+                    const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
+                    const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
+                    if (!(fabsf(iw) <= 1e-12f))
+                        atomicMin(&best_key[(warp << 5) | pl], depth_key(clamp_hlsl(iz / iw, -1.0f, 1.0f), tri.t[k]));
+                }
+            }
+        };
+        uint32_t qn = 0;  // queued pairs, warp-uniform
         for (uint32_t g = 0; g < n; g += 32) {
             const uint32_t j = g + lane;
             bool maybe = false;
@@ -460,6 +506,7 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
             while (live) {
                 const uint32_t k = g + (uint32_t)(__ffs(live) - 1);
                 live &= live - 1u;
+                // coverage (rasterize_forward.hlsl edge tests) for every pixel of the region at once
                 const float sgn = tri.sign[k];
                 const float s0x = tri.s0x[k], s0y = tri.s0y[k], s1x = tri.s1x[k], s1y = tri.s1y[k];
                 const float s2x = tri.s2x[k], s2y = tri.s2y[k];
@@ -467,35 +514,34 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
                 const float e1 = cross2(s2x - sx, s2y - sy, s0x - sx, s0y - sy);
                 const float e2 = cross2(s0x - sx, s0y - sy, s1x - sx, s1y - sy);
                 const float ceps = -1e-7f;
-                if (e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps) continue;
-                const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
-                const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
-                const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
-                const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
-                const float a0 = cross2(q1x, q1y, q2x, q2y);
-                const float a1 = cross2(q2x, q2y, q0x, q0y);
-                const float a2 = cross2(q0x, q0y, q1x, q1y);
-                const float ha = a0 + a1 + a2;
-                if (fabsf(ha) <= 1e-12f) continue;
-                const float inv = 1.0f / ha;
-                const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
-                const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
-                if (fabsf(iw) <= 1e-12f) continue;
-                const float depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
-                const uint32_t t = tri.t[k];
-                // nearest depth wins; ties go to the lowest triangle id (rasterize_forward.hlsl:136-140)
-                if (depth > best_depth || (depth == best_depth && best_tri != 0 && t + 1 >= best_tri)) continue;
-                best_depth = depth;
-                best_tri = t + 1;
-                bb0 = clamp_hlsl(a0 * inv, 0.0f, 1.0f);
-                bb1 = clamp_hlsl(a1 * inv, 0.0f, 1.0f);
-                binv = inv;
+                const bool pass = in_image && !(e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps);
+                const unsigned m = __ballot_sync(0xffffffffu, pass);
+                if (!m) continue;
+                if (pass) q[qn + __popc(m & ((1u << lane) - 1u))] = (k << 5) | lane;
+                qn += __popc(m);
+                if (qn >= 32) {
+                    __syncwarp();
+                    depth_pairs(32);
+                    __syncwarp();
+                    const uint32_t rest = qn - 32;
+                    const uint32_t moved = lane < rest ? q[32 + lane] : 0u;
+                    __syncwarp();
+                    if (lane < rest) q[lane] = moved;
+                    __syncwarp();
+                    qn = rest;
+                }
             }
         }
+        if (qn) {
+            __syncwarp();
+            depth_pairs(qn);
+        }
     }
-    if (px >= W || py >= H) return;
+    __syncwarp();
+    if (!in_image) return;
     const size_t pix = ((size_t)view * H + py) * W + px;
-    if (best_tri == 0) {
+    const unsigned long long key = best_key[threadIdx.x];
+    if (key == ~0ull) {
         raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (kDeriv) deriv[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (kShade) {
@@ -506,8 +552,27 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
         }
         return;
     }
-    raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
+    // the winner's barycentrics and depth, recomputed with the reference's arithmetic
+    const uint32_t best_tri = (uint32_t)key + 1u;
     const uint3 vi = idx[best_tri - 1];
+    float bb0, bb1, binv, best_depth;
+    {
+        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+        const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+        const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+        const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+        const float a0 = cross2(q1x, q1y, q2x, q2y);
+        const float a1 = cross2(q2x, q2y, q0x, q0y);
+        const float a2 = cross2(q0x, q0y, q1x, q1y);
+        const float ha = a0 + a1 + a2;
+        binv = 1.0f / ha;
+        const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
+        const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
+        best_depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
+        bb0 = clamp_hlsl(a0 * binv, 0.0f, 1.0f);
+        bb1 = clamp_hlsl(a1 * binv, 0.0f, 1.0f);
+    }
+    raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
     if (kDeriv) {
         const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
         const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
@@ -647,7 +712,8 @@ size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, 
 
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
-                             unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream) {
+                             unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream,
+                             bool sorted) {
     const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
     const uint32_t tiles = tcx * tcy;
     const size_t segs = (size_t)tiles * views;
@@ -674,7 +740,8 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
     scan_local_kernel<<<nblocks, kScanThreads, 0, stream>>>(counts, (uint32_t)segs, offsets, block_sums);
     scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(block_sums, nblocks, offsets, (uint32_t)segs, status, capacity);
     scan_add_kernel<<<nblocks, kScanThreads, 0, stream>>>(offsets, (uint32_t)segs, block_sums, cursor);
-    bin_fill_kernel<<<tgrid, 256, 0, stream>>>(rects, T, tcx, tiles, cursor, unsorted, capacity);
+    bin_fill_kernel<<<tgrid, 256, 0, stream>>>(rects, T, tcx, tiles, cursor, sorted ? unsorted : list, capacity);
+    if (!sorted) return cudaGetLastError();  // each tile's triangles stay in arrival order
     bin_sort_small_kernel<<<(uint32_t)((segs + 7) / 8), 256, 0, stream>>>(offsets, (uint32_t)segs, unsorted, list,
                                                                            large_queue, status, capacity);
     bin_sort_large_kernel<<<num_sms() * 2, 512, 0, stream>>>(offsets, unsorted, list, large_queue, status, capacity);

@@ -146,7 +146,21 @@ class RenderFwdBwd:
         self.backward(clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled, stream)
 
     def kernels_per_step(self) -> int:
-        """Kernels one step launches: binning (count, three scan phases, fill, two sort passes), then
-        fused: raster with the shading epilogue + one backward; unfused: raster, three forwards,
-        texture backward, two interpolate backwards, raster backward."""
-        return 7 + (1 + 1 if self.fused else 1 + 3 + 1 + 2 + 1)
+        """Kernels one step launches: binning (count, three scan phases, fill; the unfused path also
+        sorts each tile, two passes), then fused: raster with the shading epilogue + one backward;
+        unfused: raster, three forwards, texture backward, two interpolate backwards, raster backward."""
+        return 5 + 1 + 1 if self.fused else 5 + 2 + 1 + 3 + 1 + 2 + 1
+
+    def capture(self, clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled) -> "torch.cuda.CUDAGraph":
+        """Records one step into a CUDA graph (replay with .replay()); for small, launch-bound batches.
+        The inputs must stay at the same addresses while the graph is in use."""
+        dev = self.r.context.device
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):  # warm the argument paths outside the capture
+            self.step(clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step(clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled)
+        return g
