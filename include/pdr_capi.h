@@ -49,6 +49,7 @@ typedef int32_t pdr_status;
 #define PDR_STATUS_LARGE_TILES 3
 #define PDR_STATUS_TEXEL_ERROR 4   /* 1 non-finite uv on a covered pixel, 2 texel position beyond 1e9 */
 #define PDR_STATUS_INDEX_ERROR 5   /* 1 when a triangle index is >= the vertex count */
+#define PDR_STATUS_PRECOND_TIMEOUT 6 /* 1 when a tensor-core wait of the preconditioner MLP gave up */
 
 PDR_API const char* pdr_last_error(void);
 PDR_API int32_t pdr_version(void);
@@ -305,6 +306,85 @@ PDR_API pdr_status pdr_bin_tiles_no_alloc(const float* clip_positions, uint32_t 
                                           uint32_t height, const float* viewports, uint32_t* tile_offsets,
                                           uint32_t* tile_triangles, uint64_t capacity, uint32_t* status,
                                           void* stream);
+
+
+/* ---- learned refine preconditioner --------------------------------------------------------------
+ * No counterpart in the reference. A 16 -> 64 -> 64 -> 4 MLP (ReLU, BF16 weights and operands, FP32
+ * accumulation on the tensor cores) maps per-texel refine features to per-channel log step
+ * multipliers for the Adam update. Parameters are one FP32 vector of PDR_PRECOND_PARAMS values,
+ * [W1 64x16 | b1 64 | W2 64x64 | b2 64 | W3 4x64 | b3 4] with weights row-major [out][in], plus its
+ * BF16 copy (same layout, 16-byte aligned) that the matrix multiplies read. */
+#define PDR_PRECOND_IN 16
+#define PDR_PRECOND_HIDDEN 64
+#define PDR_PRECOND_OUT 4
+#define PDR_PRECOND_PARAMS 5508
+
+/* out [count][4] = MLP(features [count][16] BF16). */
+PDR_API pdr_status pdr_precond_forward(const float* params, const uint16_t* params_bf16, const uint16_t* features,
+                                       uint64_t count, float* out, uint32_t* status, void* stream);
+/* One training pass over count samples: loss = inv_norm * sum weight * (MLP(x) - target)^2 (targets and
+ * weights [count][4] FP32); grads [PDR_PRECOND_PARAMS] and loss [1] are overwritten with its gradient
+ * and value. */
+PDR_API pdr_status pdr_precond_train_step(const float* params, const uint16_t* params_bf16, const uint16_t* features,
+                                          const float* targets, const float* target_weights, uint64_t count,
+                                          float inv_norm, float* grads, float* loss, uint32_t* status, void* stream);
+/* Adam step `step` (0-based) on the FP32 parameters; refreshes params_bf16. */
+PDR_API pdr_status pdr_precond_adam(float* params, const float* grads, float* moment1, float* moment2, uint32_t step,
+                                    float learning_rate, float beta1, float beta2, float epsilon,
+                                    uint16_t* params_bf16, void* stream);
+/* Static per-texel inputs of the features: observation weight (sum of masked bilinear tap weights over
+ * all views), the number of views that see the texel, and a chart-edge distance proxy (the smallest
+ * r in 1, 2, 4 .. 32 with an invalid or other-chart texel at offset r, 64 when none). views_host is a
+ * HOST array of the cached views (device buffers); scratch holds width*height bytes. */
+PDR_API pdr_status pdr_precond_texel_stats(const pdr_refine_view* views_host, uint32_t view_count, uint32_t width,
+                                           uint32_t height, const uint8_t* valid, const int32_t* chart_ids,
+                                           float* observation, float* view_counts, float* edge_distance,
+                                           uint8_t* scratch, void* stream);
+/* features [texel_count][16] BF16 from the refine state (texture, Adam moments with their bias
+ * corrections) and the static inputs; progress is the fraction of the schedule done. */
+PDR_API pdr_status pdr_precond_features(const float* texture, const float* moment1, const float* moment2,
+                                        float bias_correction1, float bias_correction2, float epsilon,
+                                        const float* observation, const float* view_counts,
+                                        const float* edge_distance, float progress, uint64_t texel_count,
+                                        uint16_t* features, void* stream);
+/* The Adam update of pdr_refine_adam with each texel's step scaled per channel by
+ * exp(clamp(multipliers[t][c], log 1/8, log 16)); plain Adam when *fallback != 0. */
+PDR_API pdr_status pdr_refine_adam_scaled(float* texture, float* gradient, float* moment1, float* moment2,
+                                          uint64_t texel_count, const float* multipliers, const uint32_t* fallback,
+                                          float learning_rate, float beta1, float beta2, float epsilon,
+                                          float bias_correction1, float bias_correction2, float clamp_min,
+                                          float clamp_max, void* stream);
+
+/* The plain-Adam fallback test of pdr_refine_run_learned on its own: sets *fallback to 1 when
+ * sum(loss[begin + window .. begin + 2 window)) > (1 + tolerance) * sum(loss[begin .. begin + window)). */
+PDR_API pdr_status pdr_precond_fallback_check(const float* loss_history, uint32_t begin, uint32_t window,
+                                              float tolerance, uint32_t* fallback, void* stream);
+
+/* State of a learned refinement (device pointers). */
+typedef struct {
+    const float* params;
+    const uint16_t* params_bf16;
+    const float* observation;     /* [texels] from pdr_precond_texel_stats */
+    const float* view_counts;     /* [texels] */
+    const float* edge_distance;   /* [texels] */
+    uint16_t* features;           /* [texels][16] scratch */
+    float* multipliers;           /* [texels][4] */
+    uint32_t* fallback;           /* one word; cleared at the start, set when plain Adam takes over */
+    uint32_t* status;             /* PDR_STATUS_WORDS words */
+    uint32_t refresh_interval;    /* steps between MLP evaluations */
+    float fallback_tolerance;     /* relative rise of the windowed batch loss that switches to plain Adam */
+} pdr_precond_run;
+
+/* pdr_refine_run with the learned preconditioner: every refresh_interval steps the features and the
+ * MLP give new multipliers; from the second window on, a rise of the mean batch loss of the last
+ * window over the one before by more than fallback_tolerance switches to plain Adam for the rest of
+ * the run (decided on the device, so the whole run can be one CUDA graph). The seam polish is plain. */
+PDR_API pdr_status pdr_refine_run_learned(const pdr_refine_options* options, const pdr_refine_view* views,
+                                          uint32_t view_count, const double* view_valid_weights,
+                                          uint64_t max_view_pixels, const float* seam_uv_pairs, uint32_t pair_count,
+                                          const uint8_t* tv_valid, const int32_t* tv_chart_ids, float* texture,
+                                          float* gradient, float* moment1, float* moment2, float* loss_history,
+                                          const pdr_precond_run* precond, int32_t use_graph, void* stream);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,7 @@ STATUS_TILE_ENTRIES_HI = 1
 STATUS_TILE_OVERFLOW = 2
 STATUS_TEXEL_ERROR = 4
 STATUS_INDEX_ERROR = 5
+STATUS_PRECOND_TIMEOUT = 6
 
 _vp = C.c_void_p
 _u32 = C.c_uint32
@@ -70,6 +71,16 @@ _SIGNATURES = {
                                        _vp]),
     "pdr_refine_graph_launch": (_i32, [_vp, _vp]),
     "pdr_refine_graph_destroy": (_i32, [_vp]),
+    "pdr_precond_forward": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp, _vp]),
+    "pdr_precond_train_step": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, C.c_float, _vp, _vp, _vp, _vp]),
+    "pdr_precond_adam": (_i32, [_vp, _vp, _vp, _vp, _u32, C.c_float, C.c_float, C.c_float, C.c_float, _vp, _vp]),
+    "pdr_precond_texel_stats": (_i32, [_vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pdr_precond_features": (_i32, [_vp, _vp, _vp, C.c_float, C.c_float, C.c_float, _vp, _vp, _vp, C.c_float, _u64,
+                                    _vp, _vp]),
+    "pdr_refine_adam_scaled": (_i32, [_vp, _vp, _vp, _vp, _u64, _vp, _vp] + [C.c_float] * 8 + [_vp]),
+    "pdr_precond_fallback_check": (_i32, [_vp, _u32, _u32, C.c_float, _vp, _vp]),
+    "pdr_refine_run_learned": (_i32, [_vp, _vp, _u32, _vp, _u64, _vp, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                      _i32, _vp]),
 }
 
 OPTIONAL_SIGNATURES: dict = {}

@@ -20,6 +20,26 @@ import torch
 from . import _native
 from .rasterizer import Context, DeviceInfo, Rasterizer, _Io, _ptr, _viewports
 
+@dataclass
+class _RefineState:
+    """Validated refinement inputs and the per-view caches (device buffers kept alive in `keep`)."""
+    io: object
+    init: torch.Tensor
+    options: "RefineOptionsC"
+    table: object
+    table_dev: torch.Tensor
+    weights: list
+    max_pixels: int
+    pairs: Optional[torch.Tensor]
+    npairs: int
+    tv_valid: Optional[torch.Tensor]
+    tv_chart: Optional[torch.Tensor]
+    keep: list
+    t0: float
+    t1: float
+    initial_is_tensor: bool
+
+
 BLEND_MODES = {"best_view": 0, "weighted_average": 1, "softmax": 2}
 VISIBILITY_MODES = {"shadow_map": 0, "hybrid_ray_query": 1, "ray_query": 2}
 
@@ -323,12 +343,18 @@ class TextureBaker:
                                 viewports, seam_uv_pairs, steps, batch_size, learning_rate, minimum_learning_rate,
                                 photometric_epsilon, seam_polish_steps, seam_learning_rate, adam_beta1, adam_beta2,
                                 adam_epsilon, clamp_min, clamp_max, seam_epsilon, total_variation_weight,
-                                atlas_valid_mask, chart_ids, total_variation_epsilon, use_graph)
+                                atlas_valid_mask, chart_ids, total_variation_epsilon, use_graph=use_graph)
 
-    def _refine(self, initial_texture, positions, uv, indices, images, world_to_clip, visibility_masks, viewports,
-                seam_uv_pairs, steps, batch_size, learning_rate, minimum_learning_rate, photometric_epsilon,
-                seam_polish_steps, seam_learning_rate, adam_beta1, adam_beta2, adam_epsilon, clamp_min, clamp_max,
-                seam_epsilon, tv_weight, atlas_valid_mask, chart_ids, tv_epsilon, use_graph):
+    def _refine(self, *args, use_graph=True):
+        st = self._refine_prepare(*args)
+        return self._refine_finish(st, use_graph)
+
+    def _refine_prepare(self, initial_texture, positions, uv, indices, images, world_to_clip, visibility_masks,
+                        viewports, seam_uv_pairs, steps, batch_size, learning_rate, minimum_learning_rate,
+                        photometric_epsilon, seam_polish_steps, seam_learning_rate, adam_beta1, adam_beta2,
+                        adam_epsilon, clamp_min, clamp_max, seam_epsilon, tv_weight, atlas_valid_mask, chart_ids,
+                        tv_epsilon) -> "_RefineState":
+        """texture_refiner.cpp:174-253: validation, options and the per-view caches (uv, target, mask)."""
         ctx = self.context
         t0 = time.perf_counter()
         io = _Io(ctx, initial_texture, positions, uv, indices)
@@ -412,25 +438,42 @@ class TextureBaker:
         torch.cuda.synchronize(ctx.device)
         t1 = time.perf_counter()
 
+        return _RefineState(io=io, init=init, options=o, table=table, table_dev=table_dev, weights=weights,
+                            max_pixels=max_pixels, pairs=pairs, npairs=npairs, tv_valid=tv_valid, tv_chart=tv_chart,
+                            keep=keep, t0=t0, t1=t1, initial_is_tensor=isinstance(initial_texture, torch.Tensor))
+
+    def _refine_finish(self, st: "_RefineState", use_graph: bool, precond=None):
+        """Runs the optimisation (plain, or learned when `precond` is a pdr_precond_run structure)."""
+        ctx = self.context
+        o = st.options
+        init, pairs, npairs = st.init, st.pairs, st.npairs
+        steps, seam_polish_steps = int(o.steps), int(o.seam_polish_steps)
+        t1 = st.t1
         tex = init.clone().contiguous()
         grad = torch.empty_like(tex)
         m1 = torch.empty_like(tex)
         m2 = torch.empty_like(tex)
         seam_steps = 0 if npairs == 0 else int(seam_polish_steps)
         loss = torch.empty(int(steps) + seam_steps, dtype=torch.float32, device=ctx.device)
-        vw = (C.c_double * n)(*weights)
-        _native.call("pdr_refine_run", C.addressof(o), _ptr(table_dev), n, C.addressof(vw), max_pixels, _ptr(pairs), npairs,
-                     _ptr(tv_valid), _ptr(tv_chart), _ptr(tex), _ptr(grad), _ptr(m1), _ptr(m2), _ptr(loss),
-                     int(bool(use_graph)), ctx.stream())
+        n = len(st.weights)
+        vw = (C.c_double * n)(*st.weights)
+        if precond is None:
+            _native.call("pdr_refine_run", C.addressof(o), _ptr(st.table_dev), n, C.addressof(vw), st.max_pixels,
+                         _ptr(pairs), npairs, _ptr(st.tv_valid), _ptr(st.tv_chart), _ptr(tex), _ptr(grad), _ptr(m1),
+                         _ptr(m2), _ptr(loss), int(bool(use_graph)), ctx.stream())
+        else:
+            _native.call("pdr_refine_run_learned", C.addressof(o), _ptr(st.table_dev), n, C.addressof(vw),
+                         st.max_pixels, _ptr(pairs), npairs, _ptr(st.tv_valid), _ptr(st.tv_chart), _ptr(tex),
+                         _ptr(grad), _ptr(m1), _ptr(m2), _ptr(loss), C.addressof(precond), int(bool(use_graph)),
+                         ctx.stream())
         torch.cuda.synchronize(ctx.device)
         t2 = time.perf_counter()
-        del keep
         color = tex
         hist = loss[: int(steps)]
         seam = loss[int(steps):]
-        if io.numpy or not isinstance(initial_texture, torch.Tensor):
+        if st.io.numpy or not st.initial_is_tensor:
             color, hist, seam = color.cpu().numpy(), hist.cpu().numpy(), seam.cpu().numpy()
-        return color, hist, seam, t1 - t0, t2 - t1
+        return color, hist, seam, t1 - st.t0, t2 - t1
 
 
 def project_texture_atlas(mesh: UnwrappedMesh, images: Sequence[np.ndarray], world_to_clip, camera_positions, *,

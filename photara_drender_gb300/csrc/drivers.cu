@@ -2,6 +2,8 @@
 // whole TextureRefiner::refine loop, src/texture_refiner.cpp:304-426).
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include <string>
 #include <vector>
 
@@ -39,7 +41,7 @@ pdr_status check_refine_options(const pdr_refine_options* o) {
 pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* views, uint32_t nviews,
                           const double* valid_weights, uint64_t max_pixels, const float* pairs, uint32_t npairs,
                           const uint8_t* tv_valid, const int32_t* tv_chart, float* tex, float* grad, float* m1,
-                          float* m2, float* loss, cudaStream_t stream) {
+                          float* m2, float* loss, cudaStream_t stream, const pdr_precond_run* pc = nullptr) {
     const size_t n = (size_t)o->width * o->height * 3;
     const uint32_t seam_steps = npairs == 0 ? 0u : o->seam_polish_steps;
     cudaError_t err = cudaSuccess;
@@ -50,7 +52,20 @@ pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* vi
     chk(cudaMemsetAsync(grad, 0, n * sizeof(float), stream));
     chk(cudaMemsetAsync(m1, 0, n * sizeof(float), stream));
     chk(cudaMemsetAsync(m2, 0, n * sizeof(float), stream));
+    const uint64_t texels = (uint64_t)o->width * o->height;
+    if (pc) chk(cudaMemsetAsync(pc->fallback, 0, sizeof(uint32_t), stream));
     for (uint32_t step = 0; step < o->steps && err == cudaSuccess; ++step) {
+        if (pc && step % pc->refresh_interval == 0) {
+            // learned multipliers from the state after `step` updates (moments corrected for that count)
+            const uint32_t K = pc->refresh_interval;
+            if (step >= 2 * K) chk(launch_fallback_check(loss, step - 2 * K, K, pc->fallback_tolerance, pc->fallback, stream));
+            float lr_prev = 0.0f, bc1 = 1.0f, bc2 = 1.0f;
+            if (step > 0) refine_schedule(o, step - 1, &lr_prev, &bc1, &bc2);
+            chk(launch_precond_features(tex, m1, m2, bc1, bc2, o->adam_epsilon, pc->observation, pc->view_counts,
+                                        pc->edge_distance, (float)step / (float)o->steps, texels, pc->features, stream));
+            chk(launch_precond_forward(pc->params, pc->params_bf16, pc->features, texels, pc->multipliers, pc->status,
+                                       stream));
+        }
         // texture_refiner.cpp:317-324
         double bvw = 0.0;
         for (uint32_t b = 0; b < o->batch_size; ++b) bvw += valid_weights[((size_t)step * o->batch_size + b) % nviews];
@@ -61,8 +76,12 @@ pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* vi
             chk(launch_tv(tex, o->width, o->height, tv_valid, tv_chart, o->tv_epsilon, o->tv_scale, grad, stream));
         float lr, bc1, bc2;
         refine_schedule(o, step, &lr, &bc1, &bc2);
-        chk(launch_adam(tex, grad, m1, m2, n, lr, o->adam_beta1, o->adam_beta2, o->adam_epsilon, bc1, bc2, o->clamp_min,
-                        o->clamp_max, stream));
+        if (pc)
+            chk(launch_adam_scaled(tex, grad, m1, m2, texels, pc->multipliers, pc->fallback, lr, o->adam_beta1,
+                                   o->adam_beta2, o->adam_epsilon, bc1, bc2, o->clamp_min, o->clamp_max, stream));
+        else
+            chk(launch_adam(tex, grad, m1, m2, n, lr, o->adam_beta1, o->adam_beta2, o->adam_epsilon, bc1, bc2,
+                            o->clamp_min, o->clamp_max, stream));
     }
     if (seam_steps) {
         // texture_refiner.cpp:371-415: reset gradient and moments, then seam + Adam steps
@@ -116,6 +135,44 @@ struct pdr_refine_graph_t {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
+
+namespace {
+
+// Records `enqueue(stream)` on a private stream (the caller's stream is never left in capture mode)
+// and instantiates the graph.
+template <class Enqueue>
+pdr_status capture_graph(pdr_refine_graph* out, Enqueue&& enqueue) {
+    cudaStream_t cap = nullptr;
+    cudaError_t err = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (err != cudaSuccess) return cuda_status(err, "cudaStreamCreate");
+    auto* g = new pdr_refine_graph_t();
+    pdr_status st = PDR_OK;
+    err = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) {
+        st = enqueue(cap);
+        const cudaError_t end = cudaStreamEndCapture(cap, &g->graph);
+        if (st == PDR_OK && end != cudaSuccess) st = cuda_status(end, "cudaStreamEndCapture");
+    } else {
+        st = cuda_status(err, "cudaStreamBeginCapture");
+    }
+    if (st == PDR_OK) {
+        err = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (err != cudaSuccess) st = cuda_status(err, "cudaGraphInstantiate");
+    }
+    cudaStreamDestroy(cap);
+    if (st != PDR_OK) {
+        pdr_refine_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return PDR_OK;
+}
+
+bool precond_params_ok(const float* params, const uint16_t* wbf) {
+    return params && wbf && aligned(wbf, 16) && aligned(params, 4);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -226,32 +283,11 @@ pdr_status pdr_refine_graph_create(pdr_refine_graph* out, const pdr_refine_optio
     *out = nullptr;
     pdr_status st = check_refine_run(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tex, grad, m1, m2, loss);
     if (st) return st;
-    // record on a private stream so the caller's stream is never left in capture mode
-    cudaStream_t cap = nullptr;
-    cudaError_t err = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
-    if (err != cudaSuccess) return cuda_status(err, "cudaStreamCreate");
-    auto* g = new pdr_refine_graph_t();
-    err = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    if (err == cudaSuccess) {
-        st = enqueue_refine(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tv_valid, tv_chart, tex, grad, m1,
-                            m2, loss, cap);
-        const cudaError_t end = cudaStreamEndCapture(cap, &g->graph);
-        if (st == PDR_OK && end != cudaSuccess) st = cuda_status(end, "cudaStreamEndCapture");
-    } else {
-        st = cuda_status(err, "cudaStreamBeginCapture");
-    }
-    if (st == PDR_OK) {
-        err = cudaGraphInstantiate(&g->exec, g->graph, 0);
-        if (err != cudaSuccess) st = cuda_status(err, "cudaGraphInstantiate");
-    }
-    cudaStreamDestroy(cap);
     (void)stream;
-    if (st != PDR_OK) {
-        pdr_refine_graph_destroy(g);
-        return st;
-    }
-    *out = g;
-    return PDR_OK;
+    return capture_graph(out, [&](cudaStream_t cap) {
+        return enqueue_refine(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tv_valid, tv_chart, tex, grad,
+                              m1, m2, loss, cap);
+    });
 }
 
 pdr_status pdr_refine_graph_launch(pdr_refine_graph g, void* stream) {
@@ -265,6 +301,121 @@ pdr_status pdr_refine_graph_destroy(pdr_refine_graph g) {
     if (g->graph) cudaGraphDestroy(g->graph);
     delete g;
     return PDR_OK;
+}
+
+
+pdr_status pdr_precond_forward(const float* params, const uint16_t* wbf, const uint16_t* features, uint64_t count,
+                               float* out, uint32_t* status, void* stream) {
+    if (!precond_params_ok(params, wbf) || !features || !out || !status)
+        return fail(PDR_INVALID_ARGUMENT, "preconditioner buffers are required (BF16 buffers 16-byte aligned)");
+    if (!aligned(features, 16) || !aligned(out, 16)) return fail(PDR_INVALID_ARGUMENT, "features/out must be 16-byte aligned");
+    if (count == 0) return PDR_OK;
+    return cuda_status(launch_precond_forward(params, wbf, features, count, out, status, (cudaStream_t)stream),
+                       "precond_forward");
+}
+
+pdr_status pdr_precond_train_step(const float* params, const uint16_t* wbf, const uint16_t* features,
+                                  const float* targets, const float* weights, uint64_t count, float inv_norm,
+                                  float* grads, float* loss, uint32_t* status, void* stream) {
+    if (!precond_params_ok(params, wbf) || !features || !targets || !weights || !grads || !loss || !status)
+        return fail(PDR_INVALID_ARGUMENT, "preconditioner buffers are required (BF16 buffers 16-byte aligned)");
+    if (!aligned(features, 16) || !aligned(targets, 16) || !aligned(weights, 16))
+        return fail(PDR_INVALID_ARGUMENT, "features/targets/weights must be 16-byte aligned");
+    if (count == 0 || !std::isfinite(inv_norm)) return fail(PDR_INVALID_ARGUMENT, "training batch is empty");
+    return cuda_status(launch_precond_train(params, wbf, features, targets, weights, count, inv_norm, grads, loss, status,
+                                            (cudaStream_t)stream),
+                       "precond_train_step");
+}
+
+pdr_status pdr_precond_adam(float* params, const float* grads, float* m, float* v, uint32_t step, float lr, float b1,
+                            float b2, float eps, uint16_t* wbf, void* stream) {
+    if (!params || !grads || !m || !v || !wbf) return fail(PDR_INVALID_ARGUMENT, "preconditioner buffers are required");
+    if (!(lr > 0.0f) || !(b1 > 0.0f && b1 < 1.0f) || !(b2 > 0.0f && b2 < 1.0f) || !(eps > 0.0f))
+        return fail(PDR_INVALID_ARGUMENT, "preconditioner optimiser options are invalid");
+    const float bc1 = 1.0f - std::pow(b1, (float)(step + 1)), bc2 = 1.0f - std::pow(b2, (float)(step + 1));
+    return cuda_status(launch_precond_adam(params, grads, m, v, lr, b1, b2, eps, bc1, bc2, wbf, (cudaStream_t)stream),
+                       "precond_adam");
+}
+
+pdr_status pdr_precond_texel_stats(const pdr_refine_view* views_host, uint32_t nviews, uint32_t W, uint32_t H,
+                                   const uint8_t* valid, const int32_t* chart, float* obs, float* view_counts,
+                                   float* edge, uint8_t* scratch, void* stream) {
+    if (!views_host || nviews == 0 || W == 0 || H == 0 || !valid || !obs || !view_counts || !edge || !scratch)
+        return fail(PDR_INVALID_ARGUMENT, "texel statistics need views, the valid mask and output buffers");
+    const cudaStream_t s = (cudaStream_t)stream;
+    const size_t N = (size_t)W * H;
+    cudaError_t err = cudaMemsetAsync(obs, 0, N * sizeof(float), s);
+    if (err == cudaSuccess) err = cudaMemsetAsync(view_counts, 0, N * sizeof(float), s);
+    if (err == cudaSuccess) err = cudaMemsetAsync(scratch, 0, N, s);
+    for (uint32_t k = 0; k < nviews && err == cudaSuccess; ++k) {
+        const pdr_refine_view& v = views_host[k];
+        if (!v.uv || !v.mask) return fail(PDR_INVALID_ARGUMENT, "a cached view has no uv or mask buffer");
+        err = launch_observe_view(v.uv, v.mask, v.pixel_count, W, H, obs, scratch, view_counts, s);
+    }
+    if (err == cudaSuccess) err = launch_edge_distance(valid, chart, W, H, edge, s);
+    return cuda_status(err, "precond_texel_stats");
+}
+
+pdr_status pdr_precond_features(const float* tex, const float* m1, const float* m2, float bc1, float bc2, float eps,
+                                const float* obs, const float* view_counts, const float* edge, float progress,
+                                uint64_t N, uint16_t* feat, void* stream) {
+    if (!tex || !m1 || !m2 || !obs || !view_counts || !edge || !feat)
+        return fail(PDR_INVALID_ARGUMENT, "feature inputs are required");
+    if (!aligned(feat, 16)) return fail(PDR_INVALID_ARGUMENT, "features must be 16-byte aligned");
+    if (!(bc1 > 0.0f) || !(bc2 > 0.0f)) return fail(PDR_INVALID_ARGUMENT, "bias corrections must be positive");
+    if (N == 0) return PDR_OK;
+    return cuda_status(launch_precond_features(tex, m1, m2, bc1, bc2, eps, obs, view_counts, edge, progress, N, feat,
+                                               (cudaStream_t)stream),
+                       "precond_features");
+}
+
+pdr_status pdr_refine_adam_scaled(float* tex, float* grad, float* m1, float* m2, uint64_t N, const float* mult,
+                                  const uint32_t* fallback, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                                  float cmin, float cmax, void* stream) {
+    if (!tex || !grad || !m1 || !m2 || !mult || !fallback)
+        return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers are required");
+    if (!aligned(mult, 16)) return fail(PDR_INVALID_ARGUMENT, "multipliers must be 16-byte aligned");
+    if (N == 0) return PDR_OK;
+    return cuda_status(launch_adam_scaled(tex, grad, m1, m2, N, mult, fallback, lr, b1, b2, eps, bc1, bc2, cmin, cmax,
+                                          (cudaStream_t)stream),
+                       "refine_adam_scaled");
+}
+
+pdr_status pdr_precond_fallback_check(const float* loss, uint32_t begin, uint32_t window, float tolerance,
+                                      uint32_t* fallback, void* stream) {
+    if (!loss || !fallback || window == 0 || !(tolerance >= 0.0f))
+        return fail(PDR_INVALID_ARGUMENT, "fallback check needs a loss history, a window and a flag");
+    return cuda_status(launch_fallback_check(loss, begin, window, tolerance, fallback, (cudaStream_t)stream),
+                       "precond_fallback_check");
+}
+
+pdr_status pdr_refine_run_learned(const pdr_refine_options* o, const pdr_refine_view* views, uint32_t nviews,
+                                  const double* valid_weights, uint64_t max_pixels, const float* pairs, uint32_t npairs,
+                                  const uint8_t* tv_valid, const int32_t* tv_chart, float* tex, float* grad, float* m1,
+                                  float* m2, float* loss, const pdr_precond_run* pc, int32_t use_graph, void* stream) {
+    pdr_status st = check_refine_run(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tex, grad, m1, m2, loss);
+    if (st) return st;
+    if (!pc || !precond_params_ok(pc->params, pc->params_bf16) || !pc->observation || !pc->view_counts ||
+        !pc->edge_distance || !pc->features || !pc->multipliers || !pc->fallback || !pc->status ||
+        pc->refresh_interval == 0 || !(pc->fallback_tolerance >= 0.0f))
+        return fail(PDR_INVALID_ARGUMENT, "the learned refinement state is incomplete");
+    if (!aligned(pc->features, 16) || !aligned(pc->multipliers, 16))
+        return fail(PDR_INVALID_ARGUMENT, "features/multipliers must be 16-byte aligned");
+    // kernel attributes are set before any capture begins
+    const cudaError_t init = precond_prepare();
+    if (init != cudaSuccess) return cuda_status(init, "precond_prepare");
+    if (!use_graph)
+        return enqueue_refine(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tv_valid, tv_chart, tex, grad,
+                              m1, m2, loss, (cudaStream_t)stream, pc);
+    pdr_refine_graph g = nullptr;
+    st = capture_graph(&g, [&](cudaStream_t cap) {
+        return enqueue_refine(o, views, nviews, valid_weights, max_pixels, pairs, npairs, tv_valid, tv_chart, tex, grad,
+                              m1, m2, loss, cap, pc);
+    });
+    if (st) return st;
+    st = pdr_refine_graph_launch(g, stream);
+    pdr_refine_graph_destroy(g);
+    return st;
 }
 
 }  // extern "C"

@@ -98,6 +98,26 @@ cudaError_t launch_tv(const float* tex, uint32_t tw, uint32_t th, const uint8_t*
                       float scale, float* grad, cudaStream_t stream);
 cudaError_t launch_adam(float* tex, float* grad, float* m, float* v, size_t n, float lr, float b1, float b2, float eps,
                         float bc1, float bc2, float cmin, float cmax, cudaStream_t stream);
+cudaError_t precond_prepare();  // sets the kernels' shared-memory limits (once; before any capture)
+cudaError_t launch_precond_forward(const float* params, const uint16_t* wbf, const uint16_t* feat, uint64_t n,
+                                   float* out, uint32_t* status, cudaStream_t stream);
+cudaError_t launch_precond_train(const float* params, const uint16_t* wbf, const uint16_t* feat, const float* target,
+                                 const float* weight, uint64_t n, float inv_norm, float* grads, float* loss,
+                                 uint32_t* status, cudaStream_t stream);
+cudaError_t launch_precond_adam(float* params, const float* grads, float* m, float* v, float lr, float b1, float b2,
+                                float eps, float bc1, float bc2, uint16_t* wbf, cudaStream_t stream);
+cudaError_t launch_observe_view(const float* uv, const float* mask, uint64_t P, uint32_t tw, uint32_t th, float* obs,
+                                uint8_t* seen, float* views, cudaStream_t stream);
+cudaError_t launch_edge_distance(const uint8_t* valid, const int32_t* chart, uint32_t tw, uint32_t th, float* edge,
+                                 cudaStream_t stream);
+cudaError_t launch_precond_features(const float* tex, const float* m1, const float* m2, float bc1, float bc2,
+                                    float eps, const float* obs, const float* views, const float* edge, float progress,
+                                    uint64_t N, uint16_t* feat, cudaStream_t stream);
+cudaError_t launch_adam_scaled(float* tex, float* grad, float* m1, float* m2, uint64_t N, const float* mult,
+                               const uint32_t* fallback, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                               float cmin, float cmax, cudaStream_t stream);
+cudaError_t launch_fallback_check(const float* loss, uint32_t begin, uint32_t window, float tolerance,
+                                  uint32_t* fallback, cudaStream_t stream);
 void refine_schedule(const pdr_refine_options* o, uint32_t step, float* lr, float* bc1, float* bc2);
 
 }  // namespace pdr
