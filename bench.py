@@ -350,19 +350,19 @@ def bake_leg(dev, hbm):
                       "the per-view shadow rasters included)"}
 
 
-def refine_leg(dev, hbm):
-    """C3 refine: 1000 masked photometric Adam steps with chart-aware TV, then the seam polish, recorded and
-    launched as one CUDA graph."""
+def refine_scene(c, dev, baker):
+    """A refinement scene of config `c` (triangles, views, height, width, atlas, seed): the displaced
+    sphere with six packed charts, views rendered from a smooth-noise ground-truth atlas with a per-view
+    exposure gain U[0.8, 1.2], binary foreground masks (silhouette eroded by 2 pixels and a random
+    ellipse), the atlas valid mask and chart ids, and the seam pairs."""
     import torch
     import torch.nn.functional as F
 
-    from photara_drender_gb300 import TextureBaker
     from photara_drender_gb300 import synthetic as S
+    from photara_drender_gb300.precond import atlas_layout
 
-    c = REFINE
     pos3, _, uv, idx, chart, remap = S.displaced_sphere(c["triangles"], seed=c["seed"], atlas_size=c["atlas"])
     mats, _ = S.orbit_cameras(c["views"], radius=3.0, fov_y_deg=45.0, aspect=c["width"] / c["height"])
-    baker = TextureBaker(dev.index or 0)
     r = baker.rasterizer
     t_pos, t_uv = torch.tensor(pos3, device=dev), torch.tensor(uv, device=dev)
     t_idx = torch.tensor(idx.astype(np.int32), device=dev)
@@ -371,7 +371,6 @@ def refine_leg(dev, hbm):
     rng = np.random.default_rng(c["seed"])
     gain = torch.tensor(rng.uniform(0.8, 1.2, size=c["views"]).astype(np.float32), device=dev)
     images = (color * gain[:, None, None, None]).contiguous()
-    # binary foreground masks: silhouette eroded by 2 pixels and a random ellipse
     sil = (raster[..., 3] > 0).float()
     eroded = 1.0 - F.max_pool2d((1.0 - sil)[:, None], 5, stride=1, padding=2)[:, 0]
     yy = torch.arange(c["height"], device=dev, dtype=torch.float32)[:, None] / c["height"]
@@ -382,42 +381,139 @@ def refine_leg(dev, hbm):
         ell[k] = (((xx - cx) / rx) ** 2 + ((yy - cy) / ry) ** 2 <= 1.0).float()
     masks = (eroded * ell).contiguous()
     del raster, color, sil, eroded, ell
-    # atlas validity and chart ids (for the chart-aware TV) from the rasterized UV layout
-    aclip = torch.cat([t_uv * 2.0 - 1.0, torch.zeros_like(t_uv[:, :1]), torch.ones_like(t_uv[:, :1])], 1)
-    araster, _ = r.forward(aclip.contiguous(), t_idx, (c["atlas"], c["atlas"]), output_barycentric_derivatives=False)
-    fid = araster[..., 3].long()
-    valid = (fid > 0).float()
-    t_chart = torch.tensor(chart, device=dev)
-    charts = torch.where(fid > 0, t_chart[(fid - 1).clamp(min=0)], torch.full_like(fid, -1)).to(torch.int32)
+    valid, charts = atlas_layout(r, t_uv, t_idx, chart, c["atlas"], c["atlas"])
     pairs = torch.tensor(S.seam_uv_pairs(uv, idx, remap, chart), device=dev)
-    init = torch.full((c["atlas"], c["atlas"], 3), 0.5, device=dev)
-    kw = dict(visibility_masks=[masks[k] for k in range(c["views"])], seam_uv_pairs=pairs, steps=c["steps"],
-              batch_size=c["batch"], learning_rate=c["lr"], minimum_learning_rate=c["min_lr"],
-              seam_polish_steps=c["seam_steps"], seam_learning_rate=c["seam_lr"],
-              total_variation_weight=c["tv_weight"], atlas_valid_mask=valid, chart_ids=charts, use_graph=True)
-    views = [images[k] for k in range(c["views"])]
-    tex, hist, seam, pre_s, opt_s = baker.refine_texture(init, t_pos, t_uv, t_idx, views, mats, **kw)
+    return dict(pos=t_pos, uv=t_uv, idx=t_idx, mats=mats, images=[images[k] for k in range(c["views"])],
+                masks=[masks[k] for k in range(c["views"])], valid=valid, charts=charts, pairs=pairs, gt=gt)
+
+
+def refine_args(c, sc, steps):
+    """Positional arguments of TextureBaker._refine_prepare for scene `sc` with the config's schedule."""
+    import torch
+
+    init = torch.full((c["atlas"], c["atlas"], 3), 0.5, device=sc["pos"].device)
+    return (init, sc["pos"], sc["uv"], sc["idx"], sc["images"], sc["mats"], sc["masks"], None, sc["pairs"], steps,
+            c["batch"], c["lr"], c["min_lr"], 1e-3, c["seam_steps"], c["seam_lr"], 0.9, 0.999, 1e-8, 0.0, 1.0, 1e-4,
+            c["tv_weight"], sc["valid"].float(), sc["charts"], 1e-4)
+
+
+def refine_leg(dev, hbm):
+    """C3 refine: 1000 masked photometric Adam steps with chart-aware TV, then the seam polish, recorded and
+    launched as one CUDA graph."""
+    import torch
+
+    from photara_drender_gb300 import TextureBaker
+
+    c = REFINE
+    baker = TextureBaker(dev.index or 0)
+    sc = refine_scene(c, dev, baker)
+    with baker.context.lock:
+        tex, hist, seam, pre_s, opt_s = baker._refine(*refine_args(c, sc, c["steps"]), use_graph=True)
     torch.cuda.synchronize(dev)
+    pairs = sc["pairs"]
     steps = c["steps"] + (c["seam_steps"] if pairs.shape[0] else 0)
     P = c["views"] * c["height"] * c["width"]
     n = c["atlas"] ** 2 * 3
     # per photometric step: batch views x pixels x (uv 8 + target 12 + mask 4) + atlas gather + dense Adam 32 B/value
     step_bytes = c["batch"] * (P // c["views"]) * 24 + n * 4 + n * 32
-    vmask = valid.bool()
-    err = (tex - gt).abs()[vmask].mean().item()
+    vmask = sc["valid"].bool()
+    err = (tex - sc["gt"]).abs()[vmask].mean().item()
     return {"workload": c["name"], "optimization_seconds": opt_s, "precompute_seconds": pre_s,
             "ms_per_step": opt_s / steps * 1e3, "steps": steps, "final_loss": float(hist[-1]),
             "first_loss": float(hist[0]), "seam_pairs": int(pairs.shape[0]),
             "final_seam_loss": float(seam[-1]) if len(seam) else None,
             "algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_bytes * c["steps"] / opt_s / 1e9,
             "frac": step_bytes * c["steps"] / opt_s / 1e9 / hbm, "mean_abs_error_vs_ground_truth": err,
-            "timing": "TextureBaker.refine_texture optimisation wall time (graph record + instantiate + launch + "
+            "timing": "TextureBaker refinement optimisation wall time (graph record + instantiate + launch + "
                       "sync), texture starting at 0.5"}
+
+
+# C5: the preconditioner is trained on plain trajectories of 64 seeded scenes of the C2 kind (smaller, so the
+# training data is collected in seconds) and evaluated on a held-out 1M-triangle, 48-view 2048x1536 scene.
+PRECOND_TRAIN = dict(triangles=50_000, views=16, height=512, width=512, atlas=1024, steps=1000, batch=4, lr=1e-2,
+                     min_lr=2.5e-4, tv_weight=1e-4, seam_steps=30, seam_lr=1e-3, scenes=64, interval=25,
+                     samples=4096, fit_steps=600, fit_batch=65536, fit_lr=2e-3)
+PRECOND_EVAL = dict(name="c5_learned_precond_1M_48x2048x1536_atlas4096", triangles=1_000_000, views=48, height=1536,
+                    width=2048, atlas=4096, steps=1000, batch=4, lr=1e-2, min_lr=2.5e-4, tv_weight=1e-4,
+                    seam_steps=30, seam_lr=1e-3, seed=1000, budgets=(60, 125, 250, 500), refresh=25, tolerance=0.02)
+
+
+def c5_leg(dev, hbm):
+    """Learned vs plain refinement: time for the learned refiner to reach the plain 1000-step photometric loss
+    (within 1%), with plain runs of the same shortened schedules as a control."""
+    import torch
+
+    from photara_drender_gb300 import TextureBaker
+    from photara_drender_gb300.precond import (PrecondMLP, photometric_loss, plain_trajectory_samples,
+                                               refine_learned, texel_stats)
+
+    tr, ev = PRECOND_TRAIN, PRECOND_EVAL
+    baker = TextureBaker(dev.index or 0)
+    t0 = time.perf_counter()
+    feats, targets, weights = [], [], []
+    with baker.context.lock:
+        for k in range(tr["scenes"]):
+            sc = refine_scene(dict(tr, seed=k), dev, baker)
+            st = baker._refine_prepare(*refine_args(tr, sc, tr["steps"]))
+            stats = texel_stats(st, sc["valid"], sc["charts"])
+            f, t, w, _ = plain_trajectory_samples(st, stats, sc["valid"], interval=tr["interval"],
+                                                  samples=tr["samples"], seed=k)
+            feats.append(f)
+            targets.append(t)
+            weights.append(w)
+            del sc, st, stats
+    torch.cuda.synchronize(dev)
+    t1 = time.perf_counter()
+    F_, T_, W_ = torch.cat(feats), torch.cat(targets), torch.cat(weights)
+    mlp = PrecondMLP(dev.index or 0, seed=0)
+    fit = mlp.fit(F_, T_, W_, steps=tr["fit_steps"], batch=tr["fit_batch"], lr=tr["fit_lr"])
+    torch.cuda.synchronize(dev)
+    t2 = time.perf_counter()
+
+    sc = refine_scene(ev, dev, baker)
+    runs = {}
+    with baker.context.lock:
+        def plain(steps):
+            st = baker._refine_prepare(*refine_args(ev, sc, steps))
+            out = baker._refine_finish(st, True)
+            return {"steps": steps, "seconds": out[4], "loss": photometric_loss(st, out[0])}
+
+        def learned(steps):
+            st = baker._refine_prepare(*refine_args(ev, sc, steps))
+            stats = texel_stats(st, sc["valid"], sc["charts"])
+            out = refine_learned(baker, st, mlp, stats, refresh_interval=ev["refresh"],
+                                 fallback_tolerance=ev["tolerance"], use_graph=True)
+            return {"steps": steps, "seconds": out[4], "loss": photometric_loss(st, out[0]), "fell_back": out[5]}
+
+        plain(ev["budgets"][0])  # warm-up (graph instantiation paths, caches)
+        runs["plain"] = plain(ev["steps"])
+        for b in ev["budgets"]:
+            runs[f"learned_{b}"] = learned(b)
+            runs[f"plain_{b}"] = plain(b)
+    target = runs["plain"]["loss"] * 1.01
+    hit = [runs[f"learned_{b}"] for b in ev["budgets"] if runs[f"learned_{b}"]["loss"] <= target]
+    best = min(hit, key=lambda r: r["seconds"]) if hit else None
+    plain_hit = [runs[f"plain_{b}"] for b in ev["budgets"] if runs[f"plain_{b}"]["loss"] <= target]
+    return {"workload": ev["name"], "plain_loss": runs["plain"]["loss"], "plain_seconds": runs["plain"]["seconds"],
+            "target_loss": target,
+            "learned_seconds_to_target": best["seconds"] if best else None,
+            "learned_steps_to_target": best["steps"] if best else None,
+            "time_ratio_vs_plain": best["seconds"] / runs["plain"]["seconds"] if best else None,
+            "plain_short_schedule_reaches_target": [r["steps"] for r in plain_hit],
+            "runs": runs, "training": {"scenes": tr["scenes"], "samples": int(F_.shape[0]),
+                                       "collect_seconds": t1 - t0, "fit_seconds": t2 - t1,
+                                       "fit_loss_first": float(np.mean(fit[:10])),
+                                       "fit_loss_last": float(np.mean(fit[-10:]))},
+            "loss": "masked Charbonnier photometric loss over all views, each view normalised as one refiner batch"}
 
 
 # ---- GPU arm ------------------------------------------------------------------------------------------
 
 STAGES = ["bin_tiles", "rasterize_forward+shade", "render_backward"]
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the two fused kernels on this
+# 64-view workload, from a single-pass ncu capture of the full-size run (the capture cannot run inside
+# the timed region; it is re-taken whenever these kernels change).
+KERNEL_TRAFFIC = {"rasterize_forward+shade": 2131642624 + 4511363328, "render_backward": 6804823040 + 1575863296}
 
 
 def stage_bytes(w, T, V, entries):
@@ -595,7 +691,8 @@ def run_gpu(args, world, rank, local):
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": pipe.kernels_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": KERNEL_TRAFFIC.get(dom_name) if views == 64 else None,
                          "algorithmic_bytes": sbytes[dom_name], "ms": float(stage_ms[dom])},
             "stages_ms": {n: float(t) for n, t in zip(STAGES, stage_ms)},
             "pipeline": "fused" if pipe.fused else "separate kernels",
@@ -609,7 +706,7 @@ def run_gpu(args, world, rank, local):
         }
         if world == 1:
             for key, skip, leg in (("c1", args.skip_c1, c1_leg), ("bake", args.skip_bake, bake_leg),
-                                   ("refine", args.skip_refine, refine_leg)):
+                                   ("refine", args.skip_refine, refine_leg), ("precond", args.skip_precond, c5_leg)):
                 if skip:
                     continue
                 try:
@@ -631,6 +728,7 @@ def main():
     ap.add_argument("--skip-c1", action="store_true", help="omit the small-mesh (C1) leg")
     ap.add_argument("--skip-bake", action="store_true", help="omit the bake leg")
     ap.add_argument("--skip-refine", action="store_true", help="omit the refine leg")
+    ap.add_argument("--skip-precond", action="store_true", help="omit the learned-preconditioner leg")
     args = ap.parse_args()
     if args.views:
         WORKLOAD["views"] = args.views

@@ -374,7 +374,8 @@ pdr_status pdr_refine_adam_scaled(float* tex, float* grad, float* m1, float* m2,
                                   float cmin, float cmax, void* stream) {
     if (!tex || !grad || !m1 || !m2 || !mult || !fallback)
         return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers are required");
-    if (!aligned(mult, 16)) return fail(PDR_INVALID_ARGUMENT, "multipliers must be 16-byte aligned");
+    if (!aligned(mult, 16) || !aligned(tex, 16) || !aligned(grad, 16) || !aligned(m1, 16) || !aligned(m2, 16))
+        return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers and multipliers must be 16-byte aligned");
     if (N == 0) return PDR_OK;
     return cuda_status(launch_adam_scaled(tex, grad, m1, m2, N, mult, fallback, lr, b1, b2, eps, bc1, bc2, cmin, cmax,
                                           (cudaStream_t)stream),

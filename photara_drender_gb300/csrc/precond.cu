@@ -32,7 +32,8 @@ constexpr uint32_t kIn = PDR_PRECOND_IN, kHid = PDR_PRECOND_HIDDEN, kOut = PDR_P
 constexpr uint32_t kOutPad = 16;    // the last layer runs with N = 16, the smallest N of an M = 128 MMA
 constexpr uint32_t kRows = 128;     // samples per tile = MMA M = TMEM lanes
 constexpr uint32_t kThreads = 128;  // warp w owns TMEM lanes 32w..32w+31
-constexpr uint32_t kTmemCols = 128; // D1 / D3 / dH1 in columns 0..63, D2 / dH2 in 64..127
+constexpr uint32_t kTrainCols = 128; // training: D1 / D3 / dH1 in columns 0..63, D2 / dH2 in 64..127
+constexpr uint32_t kFwdCols = 64;    // inference: every layer's accumulator in columns 0..63
 constexpr uint32_t kOffW1 = 0, kOffB1 = 1024, kOffW2 = 1088, kOffB2 = 5184, kOffW3 = 5248, kOffB3 = 5504;
 static_assert(kOffB3 + kOut == PDR_PRECOND_PARAMS, "parameter layout");
 constexpr long long kWaitCycles = 2000000000ll;  // about one second at 2 GHz
@@ -109,6 +110,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 64 consecutive FP32 columns of this thread's TMEM lane (load and wait in one statement, so no use of
+// the registers can be scheduled before the data has arrived)
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float* v) {
+    uint32_t r[64];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&h);
@@ -161,10 +176,10 @@ struct TensorCoreCta {
     uint32_t abort;
 };
 
-__device__ __forceinline__ void tc_setup(TensorCoreCta& c) {
+__device__ __forceinline__ void tc_setup(TensorCoreCta& c, uint32_t cols) {
     if ((threadIdx.x >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&c.tmem)),
-                     "r"(kTmemCols)
+                     "r"(cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -194,7 +209,7 @@ __device__ __forceinline__ bool tc_gemm(TensorCoreCta& c, uint32_t d_col, uint32
     return c.abort == 0;
 }
 
-__device__ __forceinline__ void tc_teardown(TensorCoreCta& c, uint32_t phase, uint32_t* status) {
+__device__ __forceinline__ void tc_teardown(TensorCoreCta& c, uint32_t phase, uint32_t* status, uint32_t cols) {
     if (c.abort) {
         // the MMA of the current phase may still be running: wait for it once more before freeing TMEM
         mbar_wait(smem_addr(&c.mbar), phase);
@@ -203,7 +218,7 @@ __device__ __forceinline__ void tc_teardown(TensorCoreCta& c, uint32_t phase, ui
     fence_before_sync();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "r"(cols) : "memory");
 }
 
 constexpr uint32_t kIdescHid = idesc_bf16(kRows, kHid);
@@ -211,10 +226,12 @@ constexpr uint32_t kIdescOut = idesc_bf16(kRows, kOutPad);
 
 // ---- inference ----------------------------------------------------------------------------------------
 
+// The hidden activations of both layers share one buffer (layer 2's MMA has finished reading H1 before
+// H2 is written), and every accumulator uses TMEM columns 0..63: about 32 KB of shared memory and 64
+// columns per CTA, so up to seven tiles are in flight per SM.
 struct __align__(128) FwdSmem {
     uint8_t x[kRows * kIn * 2];
-    uint8_t h1[kRows * kHid * 2];
-    uint8_t h2[kRows * kHid * 2];
+    uint8_t h[kRows * kHid * 2];
     uint8_t w1[kHid * kIn * 2];
     uint8_t w2[kHid * kHid * 2];
     uint8_t w3[kOutPad * kHid * 2];
@@ -230,7 +247,7 @@ __global__ void __launch_bounds__(kThreads) precond_forward_kernel(const float* 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& s = *reinterpret_cast<FwdSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    tc_setup(s.tc);
+    tc_setup(s.tc, kFwdCols);
     load_weight(s.w1, wbf + kOffW1, kHid, kHid, kIn);
     load_weight(s.w2, wbf + kOffW2, kHid, kHid, kHid);
     load_weight(s.w3, wbf + kOffW3, kOutPad, kOut, kHid);
@@ -256,31 +273,31 @@ __global__ void __launch_bounds__(kThreads) precond_forward_kernel(const float* 
         *reinterpret_cast<uint4*>(s.x + core_off(tid, 8, kIn)) = f1;
         operands_ready();
         if (!tc_gemm(s.tc, 0, smem_addr(s.x), smem_addr(s.w1), kIn, 1, kIdescHid, phase)) break;
-        float v[16];
-#pragma unroll 1
-        for (uint32_t c0 = 0; c0 < kHid; c0 += 16) {
-            tmem_ld16(s.tc.tmem + lane_addr + c0, v);
+        float v[64];
+        tmem_ld64(s.tc.tmem + lane_addr, v);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + s.b1[c0 + i], 0.0f);
-            store_row16(s.h1, tid, c0, kHid, v);
+        for (uint32_t c0 = 0; c0 < kHid; c0 += 16) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[c0 + i] = fmaxf(v[c0 + i] + s.b1[c0 + i], 0.0f);
+            store_row16(s.h, tid, c0, kHid, v + c0);
         }
         operands_ready();
-        if (!tc_gemm(s.tc, 64, smem_addr(s.h1), smem_addr(s.w2), kHid, 4, kIdescHid, phase)) break;
-#pragma unroll 1
-        for (uint32_t c0 = 0; c0 < kHid; c0 += 16) {
-            tmem_ld16(s.tc.tmem + lane_addr + 64 + c0, v);
+        if (!tc_gemm(s.tc, 0, smem_addr(s.h), smem_addr(s.w2), kHid, 4, kIdescHid, phase)) break;
+        tmem_ld64(s.tc.tmem + lane_addr, v);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + s.b2[c0 + i], 0.0f);
-            store_row16(s.h2, tid, c0, kHid, v);
+        for (uint32_t c0 = 0; c0 < kHid; c0 += 16) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[c0 + i] = fmaxf(v[c0 + i] + s.b2[c0 + i], 0.0f);
+            store_row16(s.h, tid, c0, kHid, v + c0);
         }
         operands_ready();
-        if (!tc_gemm(s.tc, 0, smem_addr(s.h2), smem_addr(s.w3), kHid, 4, kIdescOut, phase)) break;
+        if (!tc_gemm(s.tc, 0, smem_addr(s.h), smem_addr(s.w3), kHid, 4, kIdescOut, phase)) break;
         tmem_ld16(s.tc.tmem + lane_addr, v);
         if (row < n) out[row] = make_float4(v[0] + s.b3[0], v[1] + s.b3[1], v[2] + s.b3[2], v[3] + s.b3[3]);
         fence_before_sync();
         __syncthreads();
     }
-    tc_teardown(s.tc, phase, status);
+    tc_teardown(s.tc, phase, status, kFwdCols);
 }
 
 // ---- training ---------------------------------------------------------------------------------------
@@ -311,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1) precond_train_kernel(
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     TrainSmem& s = *reinterpret_cast<TrainSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    tc_setup(s.tc);
+    tc_setup(s.tc, kTrainCols);
     load_weight(s.w1, wbf + kOffW1, kHid, kHid, kIn);
     load_weight(s.w2, wbf + kOffW2, kHid, kHid, kHid);
     load_weight(s.w3, wbf + kOffW3, kOutPad, kOut, kHid);
@@ -457,7 +474,7 @@ __global__ void __launch_bounds__(kThreads, 1) precond_train_kernel(
         __syncthreads();
     }
     const bool aborted = s.tc.abort != 0;
-    tc_teardown(s.tc, phase, status);
+    tc_teardown(s.tc, phase, status, kTrainCols);
     if (aborted) return;
 #pragma unroll
     for (int j = 0; j < 32; ++j) atomicAdd(grads + kOffW2 + o2 * kHid + i2 + j, a2[j]);
@@ -606,28 +623,49 @@ __global__ void features_kernel(const float* __restrict__ tex, const float* __re
 }
 
 // Adam with a per-texel, per-channel step multiplier exp(clamp(out_c, log 1/8, log 16)); the
-// multipliers are ignored (plain Adam) once *fallback is set. Arithmetic otherwise as adam_kernel.
+// multipliers are ignored (plain Adam) once *fallback is set. Arithmetic as adam_kernel, streamed the
+// same way (four consecutive values per thread; value k belongs to texel k / 3, channel k % 3).
+__device__ __forceinline__ void adam_scaled_one(float& x, float& g, float& m, float& v, float s, float lr, float b1,
+                                                float b2, float eps, float bc1, float bc2, float cmin, float cmax) {
+    const float mm = b1 * m + (1.0f - b1) * g;
+    const float vv = b2 * v + (1.0f - b2) * g * g;
+    m = mm;
+    v = vv;
+    x = clamp_hlsl(x - lr * s * (mm / bc1) / (sqrtf(vv / bc2) + eps), cmin, cmax);
+    g = 0.0f;
+}
+
+__device__ __forceinline__ float step_multiplier(const float* __restrict__ mult, uint64_t k, bool plain) {
+    if (plain) return 1.0f;
+    const uint64_t t = k / 3;
+    return expf(fminf(fmaxf(mult[t * 4 + (k - t * 3)], -2.0794415f), 2.7725887f));
+}
+
 __global__ void adam_scaled_kernel(float* __restrict__ tex, float* __restrict__ grad, float* __restrict__ m1,
-                                   float* __restrict__ m2, uint64_t N, const float4* __restrict__ mult,
+                                   float* __restrict__ m2, uint64_t n, const float* __restrict__ mult,
                                    const uint32_t* __restrict__ fallback, float lr, float b1, float b2, float eps,
                                    float bc1, float bc2, float cmin, float cmax) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
     const bool plain = *fallback != 0;
-    const float4 o = mult[i];
-    const float oc[3] = {o.x, o.y, o.z};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const size_t k = i * 3 + c;
-        const float g = grad[k];
-        const float mm = b1 * m1[k] + (1.0f - b1) * g;
-        const float vv = b2 * m2[k] + (1.0f - b2) * g * g;
-        m1[k] = mm;
-        m2[k] = vv;
-        const float s = plain ? 1.0f : expf(fminf(fmaxf(oc[c], -2.0794415f), 2.7725887f));
-        tex[k] = clamp_hlsl(tex[k] - lr * s * (mm / bc1) / (sqrtf(vv / bc2) + eps), cmin, cmax);
-        grad[k] = 0.0f;
+    const uint64_t n4 = n / 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        float4 x = reinterpret_cast<float4*>(tex)[i];
+        float4 g = reinterpret_cast<float4*>(grad)[i];
+        float4 m = reinterpret_cast<float4*>(m1)[i];
+        float4 v = reinterpret_cast<float4*>(m2)[i];
+        const uint64_t k = i * 4;
+        adam_scaled_one(x.x, g.x, m.x, v.x, step_multiplier(mult, k, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+        adam_scaled_one(x.y, g.y, m.y, v.y, step_multiplier(mult, k + 1, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+        adam_scaled_one(x.z, g.z, m.z, v.z, step_multiplier(mult, k + 2, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+        adam_scaled_one(x.w, g.w, m.w, v.w, step_multiplier(mult, k + 3, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+        reinterpret_cast<float4*>(tex)[i] = x;
+        reinterpret_cast<float4*>(grad)[i] = g;
+        reinterpret_cast<float4*>(m1)[i] = m;
+        reinterpret_cast<float4*>(m2)[i] = v;
     }
+    for (uint64_t k = n4 * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+        adam_scaled_one(tex[k], grad[k], m1[k], m2[k], step_multiplier(mult, k, plain), lr, b1, b2, eps, bc1, bc2, cmin,
+                        cmax);
 }
 
 // Plain-Adam fallback: after each refresh window, if the mean batch loss of the last window rose by more
@@ -655,8 +693,17 @@ uint32_t grid_for(uint64_t tiles, uint32_t per_sm) {
 
 }  // namespace
 
+// Resident forward CTAs per SM: 4 x (33 KB shared memory, 128 threads x 94 registers, 64 TMEM columns) fits
+// every limit of an SM (228 KB, 64K registers, 512 TMEM columns) with room to spare.
+constexpr uint32_t kForwardCtasPerSm = 4;
+
 cudaError_t precond_prepare() {
-    static const cudaError_t fwd = set_smem(precond_forward_kernel, sizeof(FwdSmem));
+    static const cudaError_t fwd = [] {
+        const cudaError_t e = set_smem(precond_forward_kernel, sizeof(FwdSmem));
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(precond_forward_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    (int)cudaSharedmemCarveoutMaxShared);
+    }();
     static const cudaError_t train = set_smem(precond_train_kernel, sizeof(TrainSmem));
     return fwd != cudaSuccess ? fwd : train;
 }
@@ -666,7 +713,7 @@ cudaError_t launch_precond_forward(const float* params, const uint16_t* wbf, con
     const cudaError_t attr = precond_prepare();
     if (attr != cudaSuccess) return attr;
     const uint64_t tiles = (n + kRows - 1) / kRows;
-    precond_forward_kernel<<<grid_for(tiles, 4), kThreads, sizeof(FwdSmem), stream>>>(
+    precond_forward_kernel<<<grid_for(tiles, kForwardCtasPerSm), kThreads, sizeof(FwdSmem), stream>>>(
         params, reinterpret_cast<const __nv_bfloat16*>(wbf), reinterpret_cast<const __nv_bfloat16*>(feat), n,
         reinterpret_cast<float4*>(out), status);
     return cudaGetLastError();
@@ -722,9 +769,13 @@ cudaError_t launch_precond_features(const float* tex, const float* m1, const flo
 cudaError_t launch_adam_scaled(float* tex, float* grad, float* m1, float* m2, uint64_t N, const float* mult,
                                const uint32_t* fallback, float lr, float b1, float b2, float eps, float bc1, float bc2,
                                float cmin, float cmax, cudaStream_t stream) {
-    adam_scaled_kernel<<<(unsigned)((N + 255) / 256), 256, 0, stream>>>(tex, grad, m1, m2, N,
-                                                                        reinterpret_cast<const float4*>(mult), fallback,
-                                                                        lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+    const uint64_t n = N * 3;
+    uint64_t blocks = (n / 4 + 255) / 256;
+    const uint64_t cap = (uint64_t)num_sms() * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    adam_scaled_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tex, grad, m1, m2, n, mult, fallback, lr, b1, b2, eps,
+                                                             bc1, bc2, cmin, cmax);
     return cudaGetLastError();
 }
 

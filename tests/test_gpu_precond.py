@@ -239,3 +239,31 @@ def test_trajectory_samples_and_learned_run(dev):
     mlp.fit(f, t, w, steps=50, batch=4096)
     out = refine_learned(baker, baker._refine_prepare(*args), mlp, stats)
     assert torch.isfinite(out[0]).all() and np.isfinite(out[1].cpu().numpy()).all()
+
+
+@pytest.mark.parametrize("fallback", [0, 1])
+def test_scaled_adam_matches_restatement(dev, fallback):
+    """pdr_refine_adam_scaled against NumPy float32: the multiplier is exp(clamp(out, log 1/8, log 16)),
+    ignored when the fallback flag is set; the update otherwise follows the plain Adam kernel."""
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    rng = np.random.default_rng(7 + fallback)
+    N = 10007
+    x, g = rng.uniform(0, 1, (N, 3)).astype(np.float32), rng.normal(0, 1e-3, (N, 3)).astype(np.float32)
+    m, v = rng.normal(0, 1e-3, (N, 3)).astype(np.float32), rng.uniform(0, 1e-6, (N, 3)).astype(np.float32)
+    mult = rng.uniform(-4, 4, (N, 4)).astype(np.float32)
+    t = [torch.tensor(a, device=dev) for a in (x, g, m, v, mult)]
+    flag = torch.tensor([fallback], dtype=torch.int32, device=dev)
+    lr, b1, b2, eps, bc1, bc2 = 1e-2, 0.9, 0.999, 1e-8, 0.271, 0.00299
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    _native.call("pdr_refine_adam_scaled", _ptr(t[0]), _ptr(t[1]), _ptr(t[2]), _ptr(t[3]), N, _ptr(t[4]), _ptr(flag),
+                 lr, b1, b2, eps, bc1, bc2, 0.0, 1.0, s)
+    f32 = np.float32
+    mm = f32(b1) * m + (f32(1) - f32(b1)) * g
+    vv = f32(b2) * v + (f32(1) - f32(b2)) * g * g
+    sc = np.ones((N, 3), np.float32) if fallback else np.exp(np.clip(mult[:, :3], f32(-2.0794415), f32(2.7725887)))
+    ref = np.clip(x - f32(lr) * sc * (mm / f32(bc1)) / (np.sqrt(vv / f32(bc2)) + f32(eps)), 0.0, 1.0)
+    assert np.allclose(t[0].cpu().numpy(), ref, rtol=2e-6, atol=1e-7)
+    assert np.array_equal(t[2].cpu().numpy(), mm) and np.array_equal(t[3].cpu().numpy(), vv)
+    assert not t[1].any()
