@@ -5,7 +5,7 @@ fenghuayumo/photara_drender rebuilt as sm_103a CUDA kernels behind a C ABI
 from .rasterizer import ADDRESS_MODES, CULL_MODES, Context, DeviceInfo, Rasterizer, enumerate_devices
 from .baking import (BakedTexture, TextureBakeOutput, TextureBaker, UnwrappedMesh, project_texture_atlas,
                      suggest_softmax_scale)
-from .torch import interpolate, rasterize, texture
+from .torch import RenderOutput, interpolate, rasterize, render, texture
 from .atlas import (AtlasOptimizationOptions, TexturedRender, atlas_total_variation, masked_charbonnier_loss,
                     optimize_texture_atlas, render_textured_mesh, seam_consistency_loss)
 
@@ -15,5 +15,6 @@ __all__ = [
     "ADDRESS_MODES", "AtlasOptimizationOptions", "BakedTexture", "CULL_MODES", "Context", "DeviceInfo", "Rasterizer",
     "TextureBakeOutput", "TextureBaker", "TexturedRender", "UnwrappedMesh", "atlas_total_variation",
     "enumerate_devices", "interpolate", "masked_charbonnier_loss", "optimize_texture_atlas", "project_texture_atlas",
-    "rasterize", "render_textured_mesh", "seam_consistency_loss", "suggest_softmax_scale", "texture",
+    "rasterize", "render", "RenderOutput", "render_textured_mesh", "seam_consistency_loss", "suggest_softmax_scale",
+    "texture",
 ]

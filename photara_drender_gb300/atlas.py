@@ -13,7 +13,7 @@ from typing import List, NamedTuple, Optional, Sequence, Tuple
 import torch
 
 from .rasterizer import Rasterizer
-from .torch import interpolate, rasterize, texture as sample_texture
+from .torch import interpolate, rasterize, render, texture as sample_texture
 
 
 class TexturedRender(NamedTuple):
@@ -44,7 +44,13 @@ def render_textured_mesh(clip_positions: torch.Tensor, indices: torch.Tensor, ve
                          texture_values: torch.Tensor, resolution: Sequence[int], *, rasterizer: Rasterizer,
                          viewport: Optional[Sequence[float]] = None, cull_mode: str = "none",
                          address_mode: str = "clamp") -> TexturedRender:
-    """atlas.py:36-62: rasterize -> interpolate uv -> texture, keeping the intermediates."""
+    """atlas.py:36-62: rasterize -> interpolate uv -> texture, keeping the intermediates. A 4-channel
+    texture takes the fused forward / backward kernels (same outputs and gradients)."""
+    if texture_values.ndim == 3 and texture_values.shape[2] == 4 and texture_values.dtype == torch.float32:
+        out = render(clip_positions, indices, resolution, rasterizer=rasterizer, vertex_uv=vertex_uv,
+                     texture=texture_values, viewport=viewport, cull_mode=cull_mode, address_mode=address_mode)
+        valid_mask = (out.raster[..., 3:4] > 0).to(dtype=out.sampled.dtype)
+        return TexturedRender(out.sampled, valid_mask, out.raster, out.derivatives, out.uv)
     raster, derivatives = rasterize(clip_positions, indices, resolution, rasterizer=rasterizer, viewport=viewport,
                                     cull_mode=cull_mode, output_barycentric_derivatives=True)
     uv = interpolate(vertex_uv, raster, indices, rasterizer=rasterizer)

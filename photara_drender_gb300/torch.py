@@ -6,7 +6,8 @@ is accepted: positions [B, V, 4] give rasters [B, H, W, 4].
 """
 from __future__ import annotations
 
-from typing import Optional, Sequence, Tuple
+import ctypes as C
+from typing import NamedTuple, Optional, Sequence, Tuple
 
 import torch
 
@@ -140,3 +141,179 @@ def texture(texture_values: torch.Tensor, uv: torch.Tensor, raster: torch.Tensor
             address_mode: str = "clamp") -> torch.Tensor:
     """Sample a texture bilinearly and propagate gradients to texels and UV coordinates (torch.py:231-241)."""
     return _TextureFunction.apply(texture_values, uv, raster, rasterizer, address_mode)
+
+
+# ---- fused rasterize -> interpolate -> texture ---------------------------------------------------------
+
+class RenderOutput(NamedTuple):
+    raster: torch.Tensor          # [B, H, W, 4] (or [H, W, 4] for unbatched positions)
+    derivatives: torch.Tensor     # [B, H, W, 4]
+    interpolated: Optional[torch.Tensor]  # [B, H, W, A] when vertex_attributes were given
+    uv: Optional[torch.Tensor]    # [B, H, W, 2] when vertex_uv was given
+    sampled: Optional[torch.Tensor]       # [B, H, W, 4] when a texture was given
+
+
+_MODES = {"none": 0, "back": 1, "front": 2}
+_ADDRESS = {"clamp": 0, "wrap": 1, "mirror": 2}
+
+
+def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, cull, mode):
+    from . import _native
+    from .pipeline import RenderArgsC
+    from .rasterizer import TILE, _ptr
+
+    ctx = r.context
+    dev = ctx.device
+    views, V = clip.shape[0], clip.shape[1]
+    T = idx.shape[0]
+    tiles = ((w + TILE - 1) // TILE) * ((h + TILE - 1) // TILE)
+    f = dict(dtype=torch.float32, device=dev)
+    out = dict(raster=torch.empty((views, h, w, 4), **f), deriv=torch.empty((views, h, w, 4), **f),
+               interp=torch.empty((views, h, w, attrs.shape[1]), **f) if attrs is not None else None,
+               uv=torch.empty((views, h, w, 2), **f) if uv_attrs is not None else None,
+               sampled=torch.empty((views, h, w, 4), **f) if tex is not None else None)
+    offsets = torch.empty(views * tiles + 1, dtype=torch.int32, device=dev)
+    capacity = max(getattr(r, "_render_capacity", 0), 2 * T * views + 1024)
+    L = _native.lib()
+    for _ in range(3):
+        lst = torch.empty(capacity, dtype=torch.int32, device=dev)
+        ws_bytes = L.pdr_render_workspace_bytes(views, T, w, h, capacity)
+        ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+        ctx.status.zero_()
+        a = RenderArgsC()
+        a.clip_positions, a.views, a.vertex_count = clip.data_ptr(), views, V
+        a.indices, a.triangle_count, a.width, a.height = idx.data_ptr(), T, w, h
+        a.viewports, a.cull_mode = vps.data_ptr(), cull
+        if attrs is not None:
+            a.attributes, a.attribute_count, a.interpolated = attrs.data_ptr(), attrs.shape[1], out["interp"].data_ptr()
+        if uv_attrs is not None:
+            a.uv_attributes, a.uv = uv_attrs.data_ptr(), out["uv"].data_ptr()
+        if tex is not None:
+            a.texture, a.texture_width, a.texture_height = tex.data_ptr(), tex.shape[1], tex.shape[0]
+            a.address_mode, a.sampled = mode, out["sampled"].data_ptr()
+        a.tile_offsets, a.tile_triangles, a.capacity = offsets.data_ptr(), lst.data_ptr(), capacity
+        a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
+        a.raster, a.barycentric_derivatives = out["raster"].data_ptr(), out["deriv"].data_ptr()
+        _native.check(L.pdr_render_forward(C.addressof(a), ctx.stream()))
+        st = ctx.status.cpu()
+        total = int(st[_native.STATUS_TILE_ENTRIES]) & 0xFFFFFFFF
+        if int(st[_native.STATUS_TILE_ENTRIES_HI]) != 0:
+            raise OverflowError("Tile triangle list exceeds backend limits")
+        if not int(st[_native.STATUS_TILE_OVERFLOW]):
+            r._render_capacity = max(getattr(r, "_render_capacity", 0), total + total // 8 + 1024)
+            return out
+        capacity = total + total // 8 + 1024
+    raise RuntimeError("tile binning did not converge")
+
+
+class _RenderFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, positions, vertex_attributes, vertex_uv, texture_values, indices, resolution, rasterizer,
+                viewport, cull_mode, address_mode):
+        from .rasterizer import _viewports
+
+        r = rasterizer
+        with r.context.lock:
+            clip = positions.detach()
+            batched = clip.ndim == 3
+            clip = (clip if batched else clip.unsqueeze(0)).contiguous()
+            idx = indices.detach().to(r.context.device, torch.int32).contiguous()
+            h, w = int(resolution[0]), int(resolution[1])
+            vps, _ = _viewports(viewport, clip.shape[0], w, h, r.context.device)
+            attrs = vertex_attributes.detach().contiguous() if vertex_attributes is not None else None
+            uva = vertex_uv.detach().contiguous() if vertex_uv is not None else None
+            tex = texture_values.detach().contiguous() if texture_values is not None else None
+            out = _render_forward(r, clip, idx, h, w, attrs, uva, tex, vps, _MODES[cull_mode], _ADDRESS[address_mode])
+        ctx.r, ctx.vps, ctx.batched, ctx.viewport = r, vps, batched, viewport
+        ctx.mode = _ADDRESS[address_mode]
+        ctx.save_for_backward(clip, idx, attrs, uva, tex, out["raster"], out["uv"])
+        squeeze = (lambda t: t) if batched else (lambda t: t[0] if t is not None else None)
+        result = (squeeze(out["raster"]), squeeze(out["deriv"]), squeeze(out["interp"]), squeeze(out["uv"]),
+                  squeeze(out["sampled"]))
+        ctx.mark_non_differentiable(result[1])
+        return result
+
+    @staticmethod
+    def backward(ctx, g_raster, _g_deriv, g_interp, g_uv, g_sampled):
+        from . import _native
+        from .pipeline import RenderArgsC
+
+        clip, idx, attrs, uva, tex, raster, uv_out = ctx.saved_tensors
+        r = ctx.r
+        unb = (lambda t: t) if ctx.batched else (lambda t: t.unsqueeze(0) if t is not None else None)
+        g_raster, g_interp, g_uv, g_sampled = unb(g_raster), unb(g_interp), unb(g_uv), unb(g_sampled)
+        views, V = clip.shape[0], clip.shape[1]
+        dev = clip.device
+        f = dict(dtype=torch.float32, device=dev)
+        grad_clip = torch.empty((views, V, 4), **f)
+        grad_attr = torch.empty_like(attrs) if attrs is not None else None
+        grad_uv = torch.empty_like(uva) if uva is not None else None
+        grad_tex = torch.empty_like(tex) if tex is not None else None
+        with r.context.lock:
+            a = RenderArgsC()
+            a.clip_positions, a.views, a.vertex_count = clip.data_ptr(), views, V
+            a.indices, a.triangle_count = idx.data_ptr(), idx.shape[0]
+            a.width, a.height = raster.shape[2], raster.shape[1]
+            a.viewports, a.raster = ctx.vps.data_ptr(), raster.data_ptr()
+            keep = []
+            if attrs is not None:
+                gi = g_interp.contiguous() if g_interp is not None else torch.zeros(
+                    (views,) + tuple(raster.shape[1:3]) + (attrs.shape[1],), **f)
+                keep.append(gi)
+                a.attributes, a.attribute_count = attrs.data_ptr(), attrs.shape[1]
+                a.grad_interpolated, a.grad_attributes = gi.data_ptr(), grad_attr.data_ptr()
+            if uva is not None:
+                a.uv_attributes, a.uv, a.grad_uv_attributes = uva.data_ptr(), uv_out.data_ptr(), grad_uv.data_ptr()
+            if tex is not None:
+                gs = g_sampled.contiguous() if g_sampled is not None else torch.zeros_like(raster)
+                keep.append(gs)
+                a.texture, a.texture_width, a.texture_height, a.address_mode = (tex.data_ptr(), tex.shape[1],
+                                                                                tex.shape[0], ctx.mode)
+                a.grad_sampled, a.grad_texture = gs.data_ptr(), grad_tex.data_ptr()
+            a.grad_clip_positions, a.status = grad_clip.data_ptr(), r.context.status.data_ptr()
+            r.context.status.zero_()
+            _native.check(_native.lib().pdr_render_backward(C.addressof(a), r.context.stream()))
+            st = r.context.status.cpu()
+            if int(st[_native.STATUS_TEXEL_ERROR]) == 1:
+                raise ValueError("uv contains a non-finite value in a covered pixel")
+            if int(st[_native.STATUS_TEXEL_ERROR]) == 2:
+                raise IndexError("uv is too large for portable texture addressing")
+        # upstream gradients on the raster or uv outputs themselves go through the separate adjoints
+        extra = g_raster.contiguous() if g_raster is not None else None
+        if g_uv is not None and uva is not None:
+            gua, gr = r.interpolate_backward(uva, idx, raster, g_uv.contiguous())
+            grad_uv = grad_uv + gua
+            extra = gr if extra is None else extra + gr
+        if extra is not None:
+            grad_clip = grad_clip + r.backward(clip, idx, raster, extra.contiguous(), ctx.viewport)
+        if not ctx.batched:
+            grad_clip = grad_clip[0]
+        return grad_clip, grad_attr, grad_uv, grad_tex, None, None, None, None, None, None
+
+
+def render(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequence[int], *, rasterizer: Rasterizer,
+           vertex_attributes: Optional[torch.Tensor] = None, vertex_uv: Optional[torch.Tensor] = None,
+           texture: Optional[torch.Tensor] = None, viewport=None, cull_mode: str = "none",
+           address_mode: str = "clamp") -> RenderOutput:
+    """rasterize -> interpolate(vertex_attributes), interpolate(vertex_uv) -> texture in one fused forward
+    kernel and one fused backward kernel: the outputs of `rasterize`, two `interpolate` calls and `texture`,
+    bit-identical to them, with the same gradients. vertex_attributes [V, A] (A <= 8) and vertex_uv [V, 2]
+    are shared by all views; the texture is [H, W, 4] and needs vertex_uv."""
+    if positions.dtype != torch.float32 or positions.ndim not in (2, 3) or positions.shape[-1] != 4:
+        raise ValueError("positions must be a float32 tensor with shape [vertex_count, 4]")
+    if indices.ndim != 2 or indices.shape[1] != 3:
+        raise ValueError("indices must have shape [triangle_count, 3]")
+    if cull_mode not in _MODES:
+        raise ValueError("cull_mode must be 'none', 'back', or 'front'")
+    if address_mode not in _ADDRESS:
+        raise ValueError("address_mode must be 'clamp', 'wrap', or 'mirror'")
+    V = positions.shape[-2]
+    if vertex_attributes is not None and (vertex_attributes.ndim != 2 or vertex_attributes.shape[0] != V
+                                          or not 1 <= vertex_attributes.shape[1] <= 8):
+        raise ValueError("vertex_attributes must have shape [vertex_count, 1..8]")
+    if vertex_uv is not None and tuple(vertex_uv.shape) != (V, 2):
+        raise ValueError("vertex_uv must have shape [vertex_count, 2]")
+    if texture is not None and (vertex_uv is None or texture.ndim != 3 or texture.shape[2] != 4):
+        raise ValueError("texture must have shape [height, width, 4] and needs vertex_uv")
+    return RenderOutput(*_RenderFunction.apply(positions, vertex_attributes, vertex_uv, texture, indices,
+                                               tuple(resolution), rasterizer, viewport, cull_mode, address_mode))

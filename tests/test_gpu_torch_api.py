@@ -123,3 +123,51 @@ def test_native_refine_smoke(rast):
     o_ref, o_hist, _ = api.refine(baked.color[..., :3] * 0.5, wp, buv, IDX, [image], mats, steps=3, batch_size=1,
                                   learning_rate=0.05, minimum_learning_rate=0.01, seam_polish_steps=0)
     assert np.allclose(hist, o_hist, rtol=1e-5) and np.abs(refined - o_ref).max() < 1e-5
+
+
+@pytest.mark.parametrize("batched", [True, False])
+def test_fused_render_equals_separate_ops(rast, batched):
+    """photara_drender_gb300.torch.render (one fused forward and one fused backward kernel) against
+    rasterize -> interpolate x2 -> texture: outputs bit-identical; gradients equal up to the summation
+    order of the atomics (here also with upstream gradients on the raster and uv outputs, which take
+    the separate adjoint kernels)."""
+    rng = np.random.default_rng(9)
+    pos3, idx = S.icosphere(3)
+    mats, _ = S.orbit_cameras(3)
+    clip = S.clip_positions(pos3, mats)
+    if not batched:
+        clip = clip[1]
+    dev = torch.device("cuda", 0)
+    V = pos3.shape[0]
+    inputs = dict(clip=clip, attrs=rng.uniform(size=(V, 3)).astype(np.float32),
+                  uv=S.spherical_uv(pos3) * 1.2 - 0.1, tex=rng.uniform(size=(32, 48, 4)).astype(np.float32))
+    tidx = torch.tensor(idx.astype(np.int64), device=dev)
+    res = (80, 96)
+    lead = (3,) if batched else ()
+    g = dict(a=rng.normal(size=lead + res + (3,)), u=rng.normal(size=lead + res + (2,)),
+             s=rng.normal(size=lead + res + (4,)), r=rng.normal(size=lead + res + (4,)))
+    g = {k: torch.tensor(v.astype(np.float32), device=dev) for k, v in g.items()}
+
+    def leaves():
+        return {k: torch.tensor(np.asarray(v, np.float32), device=dev, requires_grad=True) for k, v in inputs.items()}
+
+    f = leaves()
+    out = pdr.render(f["clip"], tidx, res, rasterizer=rast, vertex_attributes=f["attrs"], vertex_uv=f["uv"],
+                     texture=f["tex"], address_mode="wrap")
+    s_ = leaves()
+    raster, deriv = pdr.rasterize(s_["clip"], tidx, res, rasterizer=rast)
+    a = pdr.interpolate(s_["attrs"], raster, tidx, rasterizer=rast)
+    u = pdr.interpolate(s_["uv"], raster, tidx, rasterizer=rast)
+    smp = pdr.texture(s_["tex"], u, raster, rasterizer=rast, address_mode="wrap")
+    for x, y in ((out.raster, raster), (out.derivatives, deriv), (out.interpolated, a), (out.uv, u), (out.sampled, smp)):
+        assert x.shape == y.shape and torch.equal(x.view(torch.int32), y.view(torch.int32))
+    loss_f = (out.interpolated * g["a"]).sum() + (out.sampled * g["s"]).sum() + (out.uv * g["u"]).sum() + \
+        (out.raster * g["r"]).sum()
+    loss_s = (a * g["a"]).sum() + (smp * g["s"]).sum() + (u * g["u"]).sum() + (raster * g["r"]).sum()
+    loss_f.backward()
+    loss_s.backward()
+    for k in inputs:
+        x, y = f[k].grad, s_[k].grad
+        assert x.shape == y.shape
+        scale = float(y.abs().max())
+        assert float((x - y).abs().max()) <= 1e-4 * scale + 1e-7, k
