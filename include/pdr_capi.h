@@ -386,6 +386,57 @@ PDR_API pdr_status pdr_refine_run_learned(const pdr_refine_options* options, con
                                           float* gradient, float* moment1, float* moment2, float* loss_history,
                                           const pdr_precond_run* precond, int32_t use_graph, void* stream);
 
+
+/* ---- uneven multi-mesh batches in one launch ------------------------------------------------------
+ * No counterpart in the reference, which renders one mesh per call. Every (mesh, view) of a batch is
+ * one job. A batch runs as one binning pass, one raster launch over the tiles of all jobs (with the
+ * shading epilogue of pdr_render_forward) and one adjoint launch (pdr_render_backward per job), for
+ * meshes of any mix of triangle counts, view counts, resolutions and texture sizes. The mesh array is
+ * a HOST array of structs holding device pointers; all meshes share one attribute count. */
+typedef struct {
+    const float* clip_positions;      /* [views][V][4] */
+    const uint32_t* indices;          /* [T][3] */
+    const float* viewports;           /* [views][4] */
+    const float* attributes;          /* [V][A], or NULL when the batch's attribute_count is 0 */
+    const float* uv_attributes;       /* [V][2], or NULL */
+    const float* texture;             /* [texture_height][texture_width][4], or NULL (needs uv_attributes) */
+    uint32_t views, vertex_count, triangle_count, width, height, texture_width, texture_height;
+    float* raster;                    /* [views][H][W][4] */
+    float* barycentric_derivatives;   /* [views][H][W][4] */
+    float* interpolated;              /* [views][H][W][A] */
+    float* uv;                        /* [views][H][W][2] */
+    float* sampled;                   /* [views][H][W][4] */
+    const float* grad_interpolated;   /* [views][H][W][A] (backward) */
+    const float* grad_sampled;        /* [views][H][W][4] (backward) */
+    float* grad_clip_positions;       /* [views][V][4] (backward) */
+    float* grad_attributes;           /* [V][A] (backward) */
+    float* grad_uv_attributes;        /* [V][2] (backward) */
+    float* grad_texture;              /* [texture_height][texture_width][4] (backward) */
+} pdr_render_mesh;
+
+/* Forward tile shape and the triangles staged in shared memory per pass (the bin depth): 16x8/128,
+ * 16x16/128, 16x16/256, 32x16/256 or 32x16/512. The outputs do not depend on the choice. */
+typedef struct {
+    uint32_t tile_width, tile_height, stage_triangles;
+} pdr_batch_config;
+
+/* Number of tile segments (tile_offsets holds segments + 1 words) and workspace bytes of a batch. */
+PDR_API pdr_status pdr_render_batch_sizes(const pdr_render_mesh* meshes, uint32_t mesh_count,
+                                          const pdr_batch_config* config, uint32_t attribute_count,
+                                          uint64_t* tile_segments, size_t* workspace_bytes);
+/* Bins and rasterizes every view of every mesh, writing raster, derivatives, interpolated attributes,
+ * uv and texture samples; status as pdr_bin_tiles (re-run with a larger capacity on overflow). */
+PDR_API pdr_status pdr_render_batch_forward(const pdr_render_mesh* meshes, uint32_t mesh_count,
+                                            uint32_t attribute_count, uint32_t cull_mode, uint32_t address_mode,
+                                            const pdr_batch_config* config, uint32_t* tile_offsets,
+                                            uint32_t* tile_triangles, uint64_t capacity, void* workspace,
+                                            size_t workspace_bytes, uint32_t* status, void* stream);
+/* The adjoints of the forward for every mesh (gradient outputs are overwritten). */
+PDR_API pdr_status pdr_render_batch_backward(const pdr_render_mesh* meshes, uint32_t mesh_count,
+                                             uint32_t attribute_count, uint32_t address_mode,
+                                             const pdr_batch_config* config, void* workspace,
+                                             size_t workspace_bytes, uint32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

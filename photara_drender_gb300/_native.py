@@ -81,6 +81,9 @@ _SIGNATURES = {
     "pdr_precond_fallback_check": (_i32, [_vp, _u32, _u32, C.c_float, _vp, _vp]),
     "pdr_refine_run_learned": (_i32, [_vp, _vp, _u32, _vp, _u64, _vp, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                       _i32, _vp]),
+    "pdr_render_batch_sizes": (_i32, [_vp, _u32, _vp, _u32, _vp, _vp]),
+    "pdr_render_batch_forward": (_i32, [_vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _u64, _vp, _sz, _vp, _vp]),
+    "pdr_render_batch_backward": (_i32, [_vp, _u32, _u32, _u32, _vp, _vp, _sz, _vp, _vp]),
 }
 
 OPTIONAL_SIGNATURES: dict = {}

@@ -23,6 +23,11 @@ int num_sms();
 
 size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity);
 
+// Exclusive scan of per-segment counts into CSR offsets (offsets[segs] = total) and the fill cursors;
+// status gets the total and the overflow flag against capacity. block_sums holds scan_block_count(segs).
+cudaError_t launch_scan_counts(const uint32_t* counts, size_t segs, uint32_t* offsets, unsigned long long* block_sums,
+                               uint32_t* cursor, uint32_t* status, unsigned long long capacity, cudaStream_t stream);
+size_t scan_block_count(size_t segs);
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
                              unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream,

@@ -11,54 +11,17 @@
 
 #include "pdr_common.cuh"
 #include "pdr_internal.h"
+#include "bin_rect.cuh"
+#include "raster_tile.cuh"
 
 namespace pdr {
 namespace {
 
-constexpr uint32_t kNoRect = 0xffffffffu;
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr uint32_t kScanBlock = kScanThreads * kScanItems;
 constexpr uint32_t kSmallSort = 1024;   // tiles up to this many entries sort in one warp
 constexpr uint32_t kWindowBits = 8192 * 32;  // id window of the large-tile bitmap sort (32 KB)
-
-struct TriRect {
-    uint32_t x;  // tx0 | tx1 << 16, or kNoRect
-    uint32_t y;  // ty0 | ty1 << 16
-};
-
-// src/rasterizer.cpp:73-125 for one triangle: pixel bounding box of the NDC bounds, clamped.
-__device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__ pos, const uint3 vi,
-                                                      uint32_t W, uint32_t H, float4 vp) {
-    TriRect r{kNoRect, 0};
-    float min_x = INFINITY, min_y = INFINITY, max_x = -INFINITY, max_y = -INFINITY;
-    const uint32_t v[3] = {vi.x, vi.y, vi.z};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float4 p = pos[v[c]];
-        if (!(p.w > 1e-8f) || !isfinite(p.w)) return r;
-        const float x = p.x / p.w;
-        const float y = p.y / p.w;
-        if (!isfinite(x) || !isfinite(y)) return r;
-        min_x = x < min_x ? x : min_x;
-        min_y = y < min_y ? y : min_y;
-        max_x = max_x < x ? x : max_x;
-        max_y = max_y < y ? y : max_y;
-    }
-    if (max_x < -1.0f || min_x > 1.0f || max_y < -1.0f || min_y > 1.0f) return r;
-    const int64_t px0 = f2i_sat(floorf((min_x * 0.5f + 0.5f) * vp.z + vp.x));
-    const int64_t px1 = (int64_t)f2i_sat(ceilf((max_x * 0.5f + 0.5f) * vp.z + vp.x)) - 1;
-    const int64_t py0 = f2i_sat(floorf((min_y * 0.5f + 0.5f) * vp.w + vp.y));
-    const int64_t py1 = (int64_t)f2i_sat(ceilf((max_y * 0.5f + 0.5f) * vp.w + vp.y)) - 1;
-    const int64_t wm = (int64_t)W - 1, hm = (int64_t)H - 1;
-    const uint32_t x0 = (uint32_t)(px0 < 0 ? 0 : (px0 > wm ? wm : px0));
-    const uint32_t x1 = (uint32_t)(px1 < 0 ? 0 : (px1 > wm ? wm : px1));
-    const uint32_t y0 = (uint32_t)(py0 < 0 ? 0 : (py0 > hm ? hm : py0));
-    const uint32_t y1 = (uint32_t)(py1 < 0 ? 0 : (py1 > hm ? hm : py1));
-    r.x = (x0 / kTile) | ((x1 / kTile) << 16);
-    r.y = (y0 / kTile) | ((y1 / kTile) << 16);
-    return r;
-}
 
 // Pass 1: per (view, triangle) tile rectangle and per-tile counts (warp-aggregated when the
 // lanes of a warp land in the same single tile).
@@ -331,73 +294,9 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 
 // ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ----------------------------
 //
-// One CTA per (view, 16x16 tile); each warp owns an 8x4 pixel region. The tile's triangles are
-// staged in shared memory (structure of arrays) 256 at a time. Per warp, three steps:
-//   1. cull: every lane takes one triangle of a group of 32 and decides whether any pixel of the
-//      region can pass that triangle's edge tests;
-//   2. coverage: for each surviving triangle, every lane runs the edge tests for its pixel, and the
-//      passing (triangle, pixel) pairs are appended to a per-warp queue;
-//   3. depth: whenever 32 pairs are queued, each lane takes one pair, computes its depth with the
-//      reference's arithmetic and folds (depth, triangle) into the pixel's winner key with a
-//      shared-memory atomicMin.
-// Small triangles cover a few pixels of a region, so step 3 runs with full warps instead of the
-// few lanes a per-pixel loop would keep busy. Afterwards each pixel recomputes the winner's
-// barycentrics once.
-//
-// The cull is rigorous. The exact edge function e(s) = cross(a - s, b - s) is linear in the sample
-// s (the s x s terms cancel), so over the region's sample box its extremes sit at the four corner
-// samples. The fp32 value a pixel computes, fl(e) = fl(fl(fl(ax-sx)*fl(by-sy)) - fl(fl(ay-sy)*fl(bx-sx))),
-// differs from the exact e by at most 4u(|A B| + |C D|) (u = 2^-24, four roundings per term), and the
-// corner values computed in fp32 carry the same bound. A triangle is skipped for the region when,
-// for one edge, the corner maximum plus 1e-6 * max(|A B| + |C D|) (about 17u, a generous bound of
-// both errors) still fails the reference's test fl(e) * sign < -1e-7 -- then every pixel of the
-// region fails it too, and the per-pixel loop would have skipped the triangle. Results are
-// unchanged; the depth test keeps the minimum (depth, id) as the reference's sequential loop does.
+// One CTA per (view, 16x16 tile) running raster_tile (raster_tile.cuh) over the tile's bin.
 
 constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA, eight 8x4 warp regions
-
-struct TileTriangles {
-    float s0x[kRasterThreads], s0y[kRasterThreads], s1x[kRasterThreads], s1y[kRasterThreads];
-    float s2x[kRasterThreads], s2y[kRasterThreads], sign[kRasterThreads];
-    uint32_t t[kRasterThreads];
-    float4 p0[kRasterThreads], p1[kRasterThreads], p2[kRasterThreads];
-};
-
-// true when fl(cross(a - s, b - s)) * sign < -1e-7 holds for every sample s of the region box
-__device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx, float by, float sign, float sx_lo,
-                                                    float sx_hi, float sy_lo, float sy_hi) {
-    const float e00 = cross2(ax - sx_lo, ay - sy_lo, bx - sx_lo, by - sy_lo);
-    const float e10 = cross2(ax - sx_hi, ay - sy_lo, bx - sx_hi, by - sy_lo);
-    const float e01 = cross2(ax - sx_lo, ay - sy_hi, bx - sx_lo, by - sy_hi);
-    const float e11 = cross2(ax - sx_hi, ay - sy_hi, bx - sx_hi, by - sy_hi);
-    const float mA = fmaxf(fabsf(ax - sx_lo), fabsf(ax - sx_hi)), mD = fmaxf(fabsf(bx - sx_lo), fabsf(bx - sx_hi));
-    const float mB = fmaxf(fabsf(by - sy_lo), fabsf(by - sy_hi)), mC = fmaxf(fabsf(ay - sy_lo), fabsf(ay - sy_hi));
-    const float slack = 1e-6f * (mA * mB + mC * mD);
-    const float probe = e00 + e10 + e01 + e11 + slack;
-    if (probe != probe || isinf(probe)) return false;  // NaN or overflow: never cull
-    if (sign > 0.0f) return fmaxf(fmaxf(e00, e10), fmaxf(e01, e11)) + slack < -1e-7f;
-    return fminf(fminf(e00, e10), fminf(e01, e11)) - slack > 1e-7f;
-}
-
-// Orders (depth, triangle) pairs as the reference's depth test does: nearest depth first (-0 and
-// +0 equal), then the lowest triangle index.
-__device__ __forceinline__ unsigned long long depth_key(float depth, uint32_t t) {
-    uint32_t b = __float_as_uint(depth);
-    if ((b << 1) == 0u) b = 0u;
-    const uint32_t o = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-    return ((unsigned long long)o << 32) | t;
-}
-
-struct ShadeArgs {
-    const float* attrs;     // [V][A] shared by all views, or nullptr
-    uint32_t A;
-    float* attr_out;        // [views][H][W][A]
-    const float2* uv_attrs; // [V][2], or nullptr
-    float2* uv_out;         // [views][H][W][2]
-    const float4* tex;      // [th][tw][4], or nullptr
-    uint32_t tw, th, mode;
-    float4* sampled;        // [views][H][W][4]
-};
 
 template <bool kDeriv, bool kShade>
 __global__ void __launch_bounds__(kRasterThreads)
@@ -406,221 +305,32 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
                       const uint32_t* __restrict__ list, unsigned long long capacity, float4* __restrict__ raster,
                       float4* __restrict__ deriv, ShadeArgs shade) {
-    __shared__ TileTriangles tri;
     const uint32_t view = blockIdx.y;
     const uint32_t tile = blockIdx.x;
-    const float4* __restrict__ clip = clip_all + (size_t)view * V;
-    const float4 vp = viewports[view];
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t rx = (tile % tcx) * kTile + (warp & 1u) * 8u;   // region origin
-    const uint32_t ry = (tile / tcx) * kTile + (warp >> 1) * 4u;
-    const uint32_t px = rx + (lane & 7u);
-    const uint32_t py = ry + (lane >> 3);
-    const float sx = sample_ndc(px, vp.x, vp.z);
-    const float sy = sample_ndc(py, vp.y, vp.w);
-    const float sx_lo = sample_ndc(rx, vp.x, vp.z), sx_hi = sample_ndc(rx + 7u, vp.x, vp.z);
-    const float sy_lo = sample_ndc(ry, vp.y, vp.w), sy_hi = sample_ndc(ry + 3u, vp.y, vp.w);
+    const size_t P = (size_t)W * H;
+    RasterView v;
+    v.clip = clip_all + (size_t)view * V;
+    v.idx = idx;
+    v.V = V;
+    v.T = T;
+    v.W = W;
+    v.H = H;
+    v.cull = cull;
+    v.vp = viewports[view];
+    v.raster = raster + view * P;
+    v.deriv = kDeriv ? deriv + view * P : nullptr;
+    v.shade = shade;
+    if (kShade) {
+        if (shade.attr_out) v.shade.attr_out = shade.attr_out + view * P * shade.A;
+        if (shade.uv_out) v.shade.uv_out = shade.uv_out + view * P;
+        if (shade.sampled) v.shade.sampled = shade.sampled + view * P;
+    }
     const uint32_t seg = view * tiles + tile;
     const uint32_t b = offsets[seg];
     uint32_t e = offsets[seg + 1];
     if (e > capacity) e = (uint32_t)capacity;
     if (b > e) e = b;
-
-    // Winner per pixel as a 64-bit key (ordered depth bits << 32 | triangle index): the minimum key is
-    // the nearest depth, ties to the lowest id, exactly the reference's sequential test.
-    __shared__ unsigned long long best_key[kRasterThreads];
-    __shared__ uint32_t queue[kRasterThreads / 32][64];  // per warp: (triangle slot << 5) | pixel lane
-    uint32_t* q = queue[warp];
-    best_key[threadIdx.x] = ~0ull;
-    const bool in_image = px < W && py < H;
-    for (uint32_t chunk = b; chunk < e; chunk += kRasterThreads) {
-        __syncthreads();
-        const uint32_t i = chunk + threadIdx.x;
-        if (i < e) {
-            const uint32_t t = list[i];
-            float sgn = 0.0f;
-            float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
-            float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f, s2x = 0.f, s2y = 0.f;
-            const uint3 vi = idx[t];
-            if (vi.x < V && vi.y < V && vi.z < V) {
-                p0 = clip[vi.x];
-                p1 = clip[vi.y];
-                p2 = clip[vi.z];
-                if (!(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f)) {
-                    s0x = p0.x / p0.w; s0y = p0.y / p0.w;
-                    s1x = p1.x / p1.w; s1y = p1.y / p1.w;
-                    s2x = p2.x / p2.w; s2y = p2.y / p2.w;
-                    const float area = cross2(s1x - s0x, s1y - s0y, s2x - s0x, s2y - s0y);
-                    const bool skip = fabsf(area) <= 1e-12f || (cull == 1 && area <= 0.0f) || (cull == 2 && area >= 0.0f);
-                    if (!skip) sgn = area > 0.0f ? 1.0f : -1.0f;
-                }
-            }
-            tri.s0x[threadIdx.x] = s0x; tri.s0y[threadIdx.x] = s0y;
-            tri.s1x[threadIdx.x] = s1x; tri.s1y[threadIdx.x] = s1y;
-            tri.s2x[threadIdx.x] = s2x; tri.s2y[threadIdx.x] = s2y;
-            tri.sign[threadIdx.x] = sgn;
-            tri.t[threadIdx.x] = t;
-            tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
-        }
-        __syncthreads();
-        const uint32_t n = min(e - chunk, (uint32_t)kRasterThreads);
-        // Depth test of up to 32 queued (triangle, pixel) pairs, one per lane: the reference's
-        // arithmetic at the pair's pixel, folded into the pixel's winner key.
-        auto depth_pairs = [&](uint32_t count) {
-            const uint32_t ent = lane < count ? q[lane] : 0u;
-            const uint32_t pl = ent & 31u, k = ent >> 5;
-            const float psx = __shfl_sync(0xffffffffu, sx, pl);
-            const float psy = __shfl_sync(0xffffffffu, sy, pl);
-            if (lane < count) {
-                const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
-                const float q0x = p0.x - psx * p0.w, q0y = p0.y - psy * p0.w;
-                const float q1x = p1.x - psx * p1.w, q1y = p1.y - psy * p1.w;
-                const float q2x = p2.x - psx * p2.w, q2y = p2.y - psy * p2.w;
-                const float a0 = cross2(q1x, q1y, q2x, q2y);
-                const float a1 = cross2(q2x, q2y, q0x, q0y);
-                const float a2 = cross2(q0x, q0y, q1x, q1y);
-                const float ha = a0 + a1 + a2;
-                if (!(fabsf(ha) <= 1e-12f)) {
-                    const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
-                    const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
-                    if (!(fabsf(iw) <= 1e-12f))
-                        atomicMin(&best_key[(warp << 5) | pl], depth_key(clamp_hlsl(iz / iw, -1.0f, 1.0f), tri.t[k]));
-                }
-            }
-        };
-        uint32_t qn = 0;  // queued pairs, warp-uniform
-        for (uint32_t g = 0; g < n; g += 32) {
-            const uint32_t j = g + lane;
-            bool maybe = false;
-            if (j < n) {
-                const float sgn = tri.sign[j];
-                if (sgn != 0.0f) {
-                    const float ax0 = tri.s0x[j], ay0 = tri.s0y[j], ax1 = tri.s1x[j], ay1 = tri.s1y[j];
-                    const float ax2 = tri.s2x[j], ay2 = tri.s2y[j];
-                    maybe = !(edge_rejects_region(ax1, ay1, ax2, ay2, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
-                              edge_rejects_region(ax2, ay2, ax0, ay0, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
-                              edge_rejects_region(ax0, ay0, ax1, ay1, sgn, sx_lo, sx_hi, sy_lo, sy_hi));
-                }
-            }
-            unsigned live = __ballot_sync(0xffffffffu, maybe);
-            while (live) {
-                const uint32_t k = g + (uint32_t)(__ffs(live) - 1);
-                live &= live - 1u;
-                // coverage (rasterize_forward.hlsl edge tests) for every pixel of the region at once
-                const float sgn = tri.sign[k];
-                const float s0x = tri.s0x[k], s0y = tri.s0y[k], s1x = tri.s1x[k], s1y = tri.s1y[k];
-                const float s2x = tri.s2x[k], s2y = tri.s2y[k];
-                const float e0 = cross2(s1x - sx, s1y - sy, s2x - sx, s2y - sy);
-                const float e1 = cross2(s2x - sx, s2y - sy, s0x - sx, s0y - sy);
-                const float e2 = cross2(s0x - sx, s0y - sy, s1x - sx, s1y - sy);
-                const float ceps = -1e-7f;
-                const bool pass = in_image && !(e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps);
-                const unsigned m = __ballot_sync(0xffffffffu, pass);
-                if (!m) continue;
-                if (pass) q[qn + __popc(m & ((1u << lane) - 1u))] = (k << 5) | lane;
-                qn += __popc(m);
-                if (qn >= 32) {
-                    __syncwarp();
-                    depth_pairs(32);
-                    __syncwarp();
-                    const uint32_t rest = qn - 32;
-                    const uint32_t moved = lane < rest ? q[32 + lane] : 0u;
-                    __syncwarp();
-                    if (lane < rest) q[lane] = moved;
-                    __syncwarp();
-                    qn = rest;
-                }
-            }
-        }
-        if (qn) {
-            __syncwarp();
-            depth_pairs(qn);
-        }
-    }
-    __syncwarp();
-    if (!in_image) return;
-    const size_t pix = ((size_t)view * H + py) * W + px;
-    const unsigned long long key = best_key[threadIdx.x];
-    if (key == ~0ull) {
-        raster[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (kDeriv) deriv[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (kShade) {
-            if (shade.attr_out)
-                for (uint32_t a = 0; a < shade.A; ++a) shade.attr_out[pix * shade.A + a] = 0.0f;
-            if (shade.uv_out) shade.uv_out[pix] = make_float2(0.0f, 0.0f);
-            if (shade.sampled) shade.sampled[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
-        return;
-    }
-    // the winner's barycentrics and depth, recomputed with the reference's arithmetic
-    const uint32_t best_tri = (uint32_t)key + 1u;
-    const uint3 vi = idx[best_tri - 1];
-    float bb0, bb1, binv, best_depth;
-    {
-        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
-        const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
-        const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
-        const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
-        const float a0 = cross2(q1x, q1y, q2x, q2y);
-        const float a1 = cross2(q2x, q2y, q0x, q0y);
-        const float a2 = cross2(q0x, q0y, q1x, q1y);
-        const float ha = a0 + a1 + a2;
-        binv = 1.0f / ha;
-        const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
-        const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
-        best_depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
-        bb0 = clamp_hlsl(a0 * binv, 0.0f, 1.0f);
-        bb1 = clamp_hlsl(a1 * binv, 0.0f, 1.0f);
-    }
-    raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
-    if (kDeriv) {
-        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
-        const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
-        const float da0_dy = -p1.x * p2.w + p1.w * p2.x;
-        const float da1_dx = -p2.w * p0.y + p2.y * p0.w;
-        const float da1_dy = -p2.x * p0.w + p2.w * p0.x;
-        const float da2_dx = -p0.w * p1.y + p0.y * p1.w;
-        const float da2_dy = -p0.x * p1.w + p0.w * p1.x;
-        const float dadx = da0_dx + da1_dx + da2_dx;
-        const float dady = da0_dy + da1_dy + da2_dy;
-        deriv[pix] = make_float4((da0_dx - bb0 * dadx) * binv * 2.0f / vp.z, (da0_dy - bb0 * dady) * binv * 2.0f / vp.w,
-                                 (da1_dx - bb1 * dadx) * binv * 2.0f / vp.z, (da1_dy - bb1 * dady) * binv * 2.0f / vp.w);
-    }
-    if (kShade) {
-        // interpolate_forward.hlsl for the winner (id <= T and indices < V hold here), then
-        // texture_forward.hlsl at the interpolated uv: the same arithmetic as the separate kernels.
-        const float u = bb0, v = bb1, w = 1.0f - u - v;
-        if (shade.attr_out) {
-            const float* at = shade.attrs;
-            const uint32_t A = shade.A;
-            for (uint32_t a = 0; a < A; ++a)
-                shade.attr_out[pix * A + a] = u * __ldg(at + (size_t)vi.x * A + a) + v * __ldg(at + (size_t)vi.y * A + a) +
-                                              w * __ldg(at + (size_t)vi.z * A + a);
-        }
-        if (shade.uv_out) {
-            const float2 t0 = __ldg(shade.uv_attrs + vi.x), t1 = __ldg(shade.uv_attrs + vi.y), t2 = __ldg(shade.uv_attrs + vi.z);
-            const float2 uvp = make_float2(u * t0.x + v * t1.x + w * t2.x, u * t0.y + v * t1.y + w * t2.y);
-            shade.uv_out[pix] = uvp;
-            if (shade.sampled) {
-                const float tx = uvp.x * (float)shade.tw - 0.5f, ty = uvp.y * (float)shade.th - 0.5f;
-                const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
-                const float fx = tx - floorf(tx), fy = ty - floorf(ty);
-                const int32_t x0 = address_coordinate(bx, shade.tw, shade.mode), x1 = address_coordinate(add1(bx), shade.tw, shade.mode);
-                const int32_t y0 = address_coordinate(by, shade.th, shade.mode), y1 = address_coordinate(add1(by), shade.th, shade.mode);
-                const float w0 = (1.0f - fx) * (1.0f - fy), w1 = fx * (1.0f - fy), w2 = (1.0f - fx) * fy, w3 = fx * fy;
-                const float4 c0 = __ldg(shade.tex + (size_t)(uint32_t)y0 * shade.tw + (uint32_t)x0);
-                const float4 c1 = __ldg(shade.tex + (size_t)(uint32_t)y0 * shade.tw + (uint32_t)x1);
-                const float4 c2 = __ldg(shade.tex + (size_t)(uint32_t)y1 * shade.tw + (uint32_t)x0);
-                const float4 c3 = __ldg(shade.tex + (size_t)(uint32_t)y1 * shade.tw + (uint32_t)x1);
-                float4 r;
-                r.x = c0.x * w0 + c1.x * w1 + c2.x * w2 + c3.x * w3;
-                r.y = c0.y * w0 + c1.y * w1 + c2.y * w2 + c3.y * w3;
-                r.z = c0.z * w0 + c1.z * w1 + c2.z * w2 + c3.z * w3;
-                r.w = c0.w * w0 + c1.w * w1 + c2.w * w2 + c3.w * w3;
-                shade.sampled[pix] = r;
-            }
-        }
-    }
+    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, list, b, e);
 }
 
 // ---- rasterize backward: shaders/rasterize_backward.hlsl:36-158 -------------------------
@@ -709,6 +419,17 @@ size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, 
     bytes += align_up((size_t)capacity * sizeof(uint32_t));    // unsorted list
     return bytes;
 }
+
+cudaError_t launch_scan_counts(const uint32_t* counts, size_t segs, uint32_t* offsets, unsigned long long* block_sums,
+                               uint32_t* cursor, uint32_t* status, unsigned long long capacity, cudaStream_t stream) {
+    const uint32_t nblocks = (uint32_t)((segs + 1 + kScanBlock - 1) / kScanBlock);
+    scan_local_kernel<<<nblocks, kScanThreads, 0, stream>>>(counts, (uint32_t)segs, offsets, block_sums);
+    scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(block_sums, nblocks, offsets, (uint32_t)segs, status, capacity);
+    scan_add_kernel<<<nblocks, kScanThreads, 0, stream>>>(offsets, (uint32_t)segs, block_sums, cursor);
+    return cudaGetLastError();
+}
+
+size_t scan_block_count(size_t segs) { return (segs + 1 + kScanBlock - 1) / kScanBlock; }
 
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
