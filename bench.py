@@ -429,6 +429,84 @@ def refine_leg(dev, hbm):
                       "sync), texture starting at 0.5"}
 
 
+C4 = dict(name="c4_uneven_batch_16_meshes", meshes=16, tri_min=10_000, tri_max=1_000_000, views=(4, 48),
+          resolutions=((512, 512), (1024, 1024), (1536, 2048)), textures=(2048, 4096), attributes=8, seed=0, reps=3)
+
+
+def c4_leg(dev, hbm):
+    """C4: 16 meshes of log-uniform 10k-1M triangles, 4-48 views each at 512^2, 1024^2 or 2048x1536,
+    8-channel attributes, 2048^2 or 4096^2 RGBA textures, forward + backward in one batch (one binning
+    pass, one raster launch, one adjoint launch) with the autotuned tile shape and bin depth; each mesh
+    is also timed alone for the per-mesh p50 / p99."""
+    import torch
+
+    from photara_drender_gb300 import Rasterizer
+    from photara_drender_gb300 import synthetic as S
+    from photara_drender_gb300.batch import BatchMesh, MeshBatch
+
+    c = C4
+    rng = np.random.default_rng(c["seed"])
+    g = torch.Generator(device=dev).manual_seed(c["seed"])
+    r = Rasterizer(dev.index or 0)
+    meshes, desc = [], []
+    for k in range(c["meshes"]):
+        T = int(np.exp(rng.uniform(np.log(c["tri_min"]), np.log(c["tri_max"]))))
+        views = int(rng.integers(c["views"][0], c["views"][1] + 1))
+        h, w = c["resolutions"][int(rng.integers(len(c["resolutions"])))]
+        ts = int(c["textures"][int(rng.integers(len(c["textures"])))])
+        pos3, _, uv, idx, _, _ = S.displaced_sphere(T, seed=k, atlas_size=ts)
+        mats, _ = S.orbit_cameras(views, radius=3.0, fov_y_deg=45.0, aspect=w / h)
+        V = pos3.shape[0]
+        m = BatchMesh(clip=torch.tensor(S.clip_positions(pos3, mats), device=dev),
+                      indices=torch.tensor(idx.astype(np.int32), device=dev), height=h, width=w,
+                      attributes=torch.rand((V, c["attributes"]), device=dev, generator=g),
+                      uv_attributes=torch.tensor(uv, device=dev),
+                      texture=torch.rand((ts, ts, 4), device=dev, generator=g))
+        m.grads["interp"] = torch.randn((views, h, w, c["attributes"]), device=dev, generator=g)
+        m.grads["sampled"] = torch.randn((views, h, w, 4), device=dev, generator=g)
+        meshes.append(m)
+        desc.append({"triangles": int(idx.shape[0]), "views": views, "resolution": [h, w], "texture": ts})
+    batch = MeshBatch(r, meshes)
+    tune = batch.autotune(reps=2)
+    best = (batch.config.tile_width, batch.config.tile_height, batch.config.stage_triangles)
+
+    def timed(b):
+        b.forward()
+        b.backward()
+        out = []
+        for _ in range(c["reps"]):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            b.forward()
+            b.backward()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            out.append(e0.elapsed_time(e1))
+        return float(np.median(out))
+
+    batch_ms = timed(batch)
+    per_mesh = []
+    for m in meshes:
+        single = MeshBatch(r, [m], config=best)
+        per_mesh.append(timed(single))
+        del single
+    P = sum(d["views"] * d["resolution"][0] * d["resolution"][1] for d in desc)
+    A = c["attributes"]
+    # forward outputs 16 + 16 + 4A + 8 + 16, backward inputs 4A + 16 per pixel; textures read and
+    # their gradients written once
+    alg = P * (16 + 16 + 4 * A + 8 + 16 + 4 * A + 16) + sum(2 * d["texture"] ** 2 * 16 for d in desc)
+    return {"workload": c["name"], "batch_ms": batch_ms, "mpix_per_s": P / 1e6 / (batch_ms / 1e3),
+            "pixels": P, "meshes": desc, "autotune_ms": {f"{a}x{b}/{k}": t for (a, b, k), t in tune.items()},
+            "config": {"tile": [best[0], best[1]], "stage_triangles": best[2]},
+            "per_mesh_ms_p50": float(np.percentile(per_mesh, 50)), "per_mesh_ms_p99": float(np.percentile(per_mesh, 99)),
+            "per_mesh_ms": per_mesh, "per_mesh_sum_ms": float(np.sum(per_mesh)),
+            "algorithmic_bytes": alg, "achieved_gbs": alg / (batch_ms / 1e3) / 1e9,
+            "frac": alg / (batch_ms / 1e3) / 1e9 / hbm,
+            "timing": "CUDA events, median of 3 forward+backward passes (host plan upload included); per mesh: the "
+                      "same batch API with one mesh"}
+
+
 # C5: the preconditioner is trained on plain trajectories of 64 seeded scenes of the C2 kind (smaller, so the
 # training data is collected in seconds) and evaluated on a held-out 1M-triangle, 48-view 2048x1536 scene.
 PRECOND_TRAIN = dict(triangles=50_000, views=16, height=512, width=512, atlas=1024, steps=1000, batch=4, lr=1e-2,
@@ -727,7 +805,8 @@ def run_gpu(args, world, rank, local):
         }
         if world == 1:
             for key, skip, leg in (("c1", args.skip_c1, c1_leg), ("bake", args.skip_bake, bake_leg),
-                                   ("refine", args.skip_refine, refine_leg), ("precond", args.skip_precond, c5_leg)):
+                                   ("refine", args.skip_refine, refine_leg), ("c4", args.skip_c4, c4_leg),
+                                   ("precond", args.skip_precond, c5_leg)):
                 if skip:
                     continue
                 try:
@@ -749,6 +828,7 @@ def main():
     ap.add_argument("--skip-c1", action="store_true", help="omit the small-mesh (C1) leg")
     ap.add_argument("--skip-bake", action="store_true", help="omit the bake leg")
     ap.add_argument("--skip-refine", action="store_true", help="omit the refine leg")
+    ap.add_argument("--skip-c4", action="store_true", help="omit the uneven multi-mesh batch leg")
     ap.add_argument("--skip-precond", action="store_true", help="omit the learned-preconditioner leg")
     args = ap.parse_args()
     if args.views:

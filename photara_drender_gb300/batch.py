@@ -76,13 +76,17 @@ class MeshBatch:
             if m.viewports is None:
                 m.viewports, _ = _viewports(None, views, m.width, m.height, dev)
             shape = (views, m.height, m.width)
-            m.outputs = dict(raster=torch.empty(shape + (4,), **f), deriv=torch.empty(shape + (4,), **f))
+            # outputs already attached to the mesh (e.g. by another batch holding it) are reused
+            need = {"raster": 4, "deriv": 4}
             if m.attributes is not None:
-                m.outputs["interp"] = torch.empty(shape + (self.A,), **f)
+                need["interp"] = self.A
             if m.uv_attributes is not None:
-                m.outputs["uv"] = torch.empty(shape + (2,), **f)
+                need["uv"] = 2
             if m.texture is not None:
-                m.outputs["sampled"] = torch.empty(shape + (4,), **f)
+                need["sampled"] = 4
+            for name, channels in need.items():
+                if name not in m.outputs:
+                    m.outputs[name] = torch.empty(shape + (channels,), **f)
         self.status = torch.zeros(_native.STATUS_WORDS, dtype=torch.int32, device=dev)
         self.capacity = 0
         self.set_config(config)
@@ -152,13 +156,10 @@ class MeshBatch:
     def allocate_gradients(self) -> None:
         for m in self.meshes:
             f = dict(dtype=torch.float32, device=m.clip.device)
-            m.grads.setdefault("clip", torch.empty(m.clip.shape, **f))
-            if m.attributes is not None:
-                m.grads.setdefault("attributes", torch.empty(m.attributes.shape, **f))
-            if m.uv_attributes is not None:
-                m.grads.setdefault("uv_attributes", torch.empty(m.uv_attributes.shape, **f))
-            if m.texture is not None:
-                m.grads.setdefault("texture", torch.empty(m.texture.shape, **f))
+            for name, src in (("clip", m.clip), ("attributes", m.attributes), ("uv_attributes", m.uv_attributes),
+                              ("texture", m.texture)):
+                if src is not None and name not in m.grads:
+                    m.grads[name] = torch.empty(src.shape, **f)
 
     def backward(self, stream=None) -> None:
         """Adjoints of the last forward; upstream gradients are m.grads['interp'] / m.grads['sampled']."""
