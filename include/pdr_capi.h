@@ -437,6 +437,31 @@ PDR_API pdr_status pdr_render_batch_backward(const pdr_render_mesh* meshes, uint
                                              const pdr_batch_config* config, void* workspace,
                                              size_t workspace_bytes, uint32_t* status, void* stream);
 
+
+/* ---- ray-query visibility (shaders/project_ray_visibility.hlsl:14-55, src/context.cpp:446-453) ----
+ * A bounding-volume hierarchy of the world-space mesh built on the device, traced with one any-hit ray
+ * per (atlas texel, view). */
+/* Bytes of the BVH buffer and of the scratch its build uses. */
+PDR_API pdr_status pdr_bvh_sizes(uint32_t triangle_count, size_t* bvh_bytes, size_t* build_bytes);
+/* Builds the BVH of positions [V][3] / indices [T][3] into bvh (synchronises the stream once). */
+PDR_API pdr_status pdr_bvh_build(const float* positions, uint32_t vertex_count, const uint32_t* indices,
+                                 uint32_t triangle_count, void* bvh, size_t bvh_bytes, void* scratch,
+                                 size_t scratch_bytes, void* stream);
+/* project_ray_visibility.hlsl for every covered texel and view: bit (v & 31) of visibility
+ * [texel][ceil(views / 32)] is set when camera v (cameras [views][4], xyz used) is visible. */
+PDR_API pdr_status pdr_ray_visibility(const void* bvh, uint32_t triangle_count, const float* atlas_positions,
+                                      const float* atlas_normals, const float* atlas_raster, uint32_t atlas_texels,
+                                      const float* cameras, uint32_t view_count, float ray_origin_bias,
+                                      uint32_t* visibility, void* stream);
+/* pdr_project_views for visibility modes 1 (ray x shadow map) and 2 (ray) with the visibility bits of
+ * pdr_ray_visibility instead of per-view arrays. */
+PDR_API pdr_status pdr_project_views_bits(const float* atlas_positions, const float* atlas_normals,
+                                          const float* atlas_raster, uint32_t atlas_texels,
+                                          const pdr_projection_view* views, uint32_t view_count, uint32_t blend_mode,
+                                          uint32_t pcf_radius, uint32_t visibility_mode, const uint32_t* visibility,
+                                          float* color, float* confidence, uint32_t* source_view, float* valid_mask,
+                                          float* coverage_mask, uint32_t* face_ids, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

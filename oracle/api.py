@@ -241,7 +241,9 @@ BLEND = {"best_view": 0, "weighted_average": 1, "softmax": 2}
 
 def bake(positions, normals, uv, indices, images, world_to_clip, camera_positions, *, visibility_masks=None,
          viewports=None, resolution=(1024, 1024), blend_mode="weighted_average", pcf_radius=1, softmax_scale=0.0,
-         mask_floor=0.0, weights=None, depth_bias=1e-3, min_view_cosine=0.05):
+         mask_floor=0.0, weights=None, depth_bias=1e-3, min_view_cosine=0.05, visibility_mode=0, ray_bits=None):
+    """texture_baker.cpp:156-361. With ray_bits ([texels, ceil(views / 32)] uint32 camera-visibility bits)
+    visibility_mode 1 multiplies them with the shadow map and 2 uses them alone."""
     pos, nrm, uvv, idx = _f(positions), _f(normals), _f(uv), _u(indices)
     h, w = resolution
     views, keep = _views(images, world_to_clip, camera_positions, visibility_masks, viewports, weights, depth_bias,
@@ -252,9 +254,12 @@ def bake(positions, normals, uv, indices, images, world_to_clip, camera_position
     valid = np.zeros((h, w), dtype=np.float32)
     cov = np.zeros((h, w), dtype=np.float32)
     faces = np.zeros((h, w), dtype=np.uint32)
-    _check(lib().ora_bake(_p(pos), _p(nrm), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views, len(images),
-                          w, h, BLEND[blend_mode], pcf_radius, C.c_float(mask_floor), C.c_float(softmax_scale),
-                          _p(color), _p(conf), _p(src, _u32p), _p(valid), _p(cov), _p(faces, _u32p)))
+    bits = None if ray_bits is None else np.ascontiguousarray(ray_bits, dtype=np.uint32)
+    _check(lib().ora_bake_ex(_p(pos), _p(nrm), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views,
+                             len(images), w, h, BLEND[blend_mode], pcf_radius, C.c_float(mask_floor),
+                             C.c_float(softmax_scale), int(visibility_mode) if bits is not None else 0,
+                             _p(bits, _u32p), _p(color), _p(conf), _p(src, _u32p), _p(valid), _p(cov),
+                             _p(faces, _u32p)))
     del keep
     return color, conf, src, valid, cov, faces
 
@@ -380,3 +385,16 @@ def project_texture_view(m16, camera, view_weight, viewport, atlas_wh, image_wh,
     pp.has_mask, pp.visibility_mode, pp.view_index = int(has_mask), visibility_mode, view_index
     lib().ora_project_texture(C.byref(pp), _p(apos), _p(anrm), _p(araster), _p(shadow), _p(photo), _p(mask),
                               _p(rayvis), _p(acc_color), _p(acc_weight), _p(best_conf), _p(source_view, _u32p))
+
+
+def ray_visibility(positions, indices, atlas_positions, atlas_normals, atlas_raster, camera, bias=1e-4):
+    """project_ray_visibility.hlsl for one camera with triangles tested in double: int8 per texel,
+    1 visible, 0 occluded or uncovered, -1 undecided (a near miss or near hit)."""
+    pos, idx = _f(positions), _u(indices)
+    ap, an, ar = _f(atlas_positions), _f(atlas_normals), _f(atlas_raster)
+    N = ar.size // 4
+    state = np.empty(N, dtype=np.int8)
+    cam = _f(camera).reshape(3)
+    _check(lib().ora_ray_visibility(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], _p(ap), _p(an), _p(ar),
+                                    C.c_uint64(N), _p(cam), C.c_float(bias), state.ctypes.data_as(C.POINTER(C.c_int8))))
+    return state

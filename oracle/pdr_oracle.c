@@ -795,6 +795,16 @@ int ora_bake(const float* pos3, const float* nrm3, const float* uv2, uint32_t V,
              uint32_t blend_mode, uint32_t pcf_radius, float mask_floor, float softmax_scale,
              float* color4, float* confidence, uint32_t* source_view, float* valid_mask,
              float* coverage_mask, uint32_t* face_ids) {
+    return ora_bake_ex(pos3, nrm3, uv2, V, idx, T, views, nviews, aw, ah, blend_mode, pcf_radius, mask_floor,
+                       softmax_scale, 0, NULL, color4, confidence, source_view, valid_mask, coverage_mask, face_ids);
+}
+
+int ora_bake_ex(const float* pos3, const float* nrm3, const float* uv2, uint32_t V, const uint32_t* idx,
+                uint32_t T, const ora_view* views, uint32_t nviews, uint32_t aw, uint32_t ah,
+                uint32_t blend_mode, uint32_t pcf_radius, float mask_floor, float softmax_scale,
+                uint32_t visibility_mode, const uint32_t* ray_bits,
+                float* color4, float* confidence, uint32_t* source_view, float* valid_mask,
+                float* coverage_mask, uint32_t* face_ids) {
     if (V == 0 || T == 0 || nviews == 0) return ORA_INVALID;
     for (uint64_t i = 0; i < (uint64_t)T * 3; ++i) if (idx[i] >= V) return ORA_RANGE;
     if (aw == 0 || ah == 0 || pcf_radius > 4 || !isfinite(mask_floor) || mask_floor < 0.0f || mask_floor > 1.0f)
@@ -869,8 +879,12 @@ int ora_bake(const float* pos3, const float* nrm3, const float* uv2, uint32_t V,
         pp.blend_mode = blend_mode;
         pp.pcf_radius = pcf_radius;
         pp.has_mask = vw->visibility_mask != NULL;
-        pp.visibility_mode = 0;
+        pp.visibility_mode = ray_bits ? visibility_mode : 0;
         pp.view_index = k;
+        if (ray_bits) {
+            const uint32_t words = (nviews + 31) / 32;
+            for (uint64_t i = 0; i < N; ++i) rayvis[i] = (float)((ray_bits[i * words + k / 32] >> (k % 32)) & 1u);
+        }
         ora_project_texture(&pp, apos, anrm, araster, shadow, vw->image, mask, rayvis, acc, accw, best, source_view);
         free(floored);
         free(shadow);
@@ -1143,4 +1157,66 @@ double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C, c
             }
         }
     return loss * (double)weight / denom;
+}
+
+/* ---- ray-query visibility ------------------------------------------------------------------ */
+
+/* shaders/project_ray_visibility.hlsl:14-55 for one camera: the ray set-up in fp32 as the shader
+ * writes it, then every triangle tested in double precision (Moller-Trumbore). State per texel: 1 when
+ * the camera is visible, 0 when a triangle is hit with margin (barycentrics and t at least 1e-5 inside)
+ * or the texel is not covered, -1 when a triangle lies within that margin of the ray without a clear
+ * hit: a ray tracer may decide those texels either way. */
+int ora_ray_visibility(const float* pos3, uint32_t V, const uint32_t* idx, uint32_t T, const float* apos,
+                       const float* anrm, const float* araster, uint64_t N, const float camera[3], float bias,
+                       int8_t* state) {
+    if (!pos3 || !idx || !apos || !anrm || !araster || !camera || !state) return ORA_INVALID;
+    for (uint64_t k = 0; k < (uint64_t)T * 3; ++k)
+        if (idx[k] >= V) return ORA_RANGE;
+    const double eps = 1e-5;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t ii = 0; ii < (int64_t)N; ++ii) {
+        const uint64_t i = (uint64_t)ii;
+        if (f2u_sat(rintf(araster[i * 4 + 3])) == 0) {
+            state[i] = 0;
+            continue;
+        }
+        const float px = apos[i * 3], py = apos[i * 3 + 1], pz = apos[i * 3 + 2];
+        const float nx0 = anrm[i * 3], ny0 = anrm[i * 3 + 1], nz0 = anrm[i * 3 + 2];
+        const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
+        const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
+        const float vx = camera[0] - px, vy = camera[1] - py, vz = camera[2] - pz;
+        const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
+        if (dist <= bias * 2.0f) {
+            state[i] = 1;
+            continue;
+        }
+        const float dxf = vx / dist, dyf = vy / dist, dzf = vz / dist;
+        const float sgn = (nx * dxf + ny * dyf + nz * dzf) >= 0.0f ? 1.0f : -1.0f;
+        const double ox = px + nx * (bias * sgn), oy = py + ny * (bias * sgn), oz = pz + nz * (bias * sgn);
+        const double dx = dxf, dy = dyf, dz = dzf;
+        const double t0 = bias;
+        const double t1 = fmaxf(bias, dist - bias * 2.0f);
+        int hit = 0, near = 0;
+        for (uint32_t t = 0; t < T && !hit; ++t) {
+            const float* a = pos3 + (size_t)idx[t * 3] * 3;
+            const float* b = pos3 + (size_t)idx[t * 3 + 1] * 3;
+            const float* c = pos3 + (size_t)idx[t * 3 + 2] * 3;
+            const double e1x = (double)b[0] - a[0], e1y = (double)b[1] - a[1], e1z = (double)b[2] - a[2];
+            const double e2x = (double)c[0] - a[0], e2y = (double)c[1] - a[1], e2z = (double)c[2] - a[2];
+            const double qx0 = dy * e2z - dz * e2y, qy0 = dz * e2x - dx * e2z, qz0 = dx * e2y - dy * e2x;
+            const double det = e1x * qx0 + e1y * qy0 + e1z * qz0;
+            if (det == 0.0) continue;
+            const double inv = 1.0 / det;
+            const double sx = ox - a[0], sy = oy - a[1], sz = oz - a[2];
+            const double u = (sx * qx0 + sy * qy0 + sz * qz0) * inv;
+            const double rx = sy * e1z - sz * e1y, ry = sz * e1x - sx * e1z, rz = sx * e1y - sy * e1x;
+            const double v = (dx * rx + dy * ry + dz * rz) * inv;
+            const double tt = (e2x * rx + e2y * ry + e2z * rz) * inv;
+            const double te = eps * (fabs(tt) > 1.0 ? fabs(tt) : 1.0);
+            if (u > eps && v > eps && u + v < 1.0 - eps && tt > t0 + te && tt < t1 - te) hit = 1;
+            else if (u > -eps && v > -eps && u + v < 1.0 + eps && tt > t0 - te && tt < t1 + te) near = 1;
+        }
+        state[i] = hit ? 0 : (near ? -1 : 1);
+    }
+    return 0;
 }

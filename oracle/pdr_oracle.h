@@ -115,6 +115,20 @@ int ora_bake(const float* pos3, const float* nrm3, const float* uv2, uint32_t V,
              float* color4, float* confidence, uint32_t* source_view, float* valid_mask,
              float* coverage_mask, uint32_t* face_ids);
 
+/* ora_bake with ray visibility: visibility_mode 1 (ray x shadow map) or 2 (ray) taking the camera
+ * visibility of texel i and view k from bit k % 32 of ray_bits[i * ceil(nviews / 32) + k / 32]. */
+int ora_bake_ex(const float* pos3, const float* nrm3, const float* uv2, uint32_t V, const uint32_t* idx,
+                uint32_t T, const ora_view* views, uint32_t nviews, uint32_t atlas_w, uint32_t atlas_h,
+                uint32_t blend_mode, uint32_t pcf_radius, float mask_floor, float softmax_scale,
+                uint32_t visibility_mode, const uint32_t* ray_bits,
+                float* color4, float* confidence, uint32_t* source_view, float* valid_mask,
+                float* coverage_mask, uint32_t* face_ids);
+/* shaders/project_ray_visibility.hlsl:14-55, triangles tested in double: 1 visible, 0 occluded (or
+ * texel not covered), -1 undecided (a triangle within 1e-5 of the ray without a clear hit). */
+int ora_ray_visibility(const float* pos3, uint32_t V, const uint32_t* idx, uint32_t T, const float* apos,
+                       const float* anrm, const float* araster, uint64_t N, const float camera[3], float bias,
+                       int8_t* state);
+
 /* atlas_photometric_gradient.hlsl for one view; grad is accumulated; returns loss added. */
 float ora_photometric_gradient(const float* tex3, uint32_t tw, uint32_t th, const float* uv,
                                const float* target3, const float* mask, uint32_t P, float eps,

@@ -59,6 +59,11 @@ _SIGNATURES = {
     "pdr_atlas_clip_positions": (_i32, [_vp, _u32, _vp, _vp]),
     "pdr_project_views": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp,
                                  _vp]),
+    "pdr_bvh_sizes": (_i32, [_u32, _vp, _vp]),
+    "pdr_bvh_build": (_i32, [_vp, _u32, _vp, _u32, _vp, _sz, _vp, _sz, _vp]),
+    "pdr_ray_visibility": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, C.c_float, _vp, _vp]),
+    "pdr_project_views_bits": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp,
+                                      _vp, _vp, _vp]),
     "pdr_refine_prepare_view": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "pdr_refine_photometric": (_i32, [_vp, _u32, _u32, _vp, _u32, _u64, _u32, _u32, C.c_float, C.c_float, _vp, _vp,
                                       _vp]),

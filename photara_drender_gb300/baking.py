@@ -288,6 +288,9 @@ class TextureBaker:
         if effective_visibility != 2:
             clip = self._transform(pos, torch.from_numpy(mats).to(ctx.device))
             shadows = self._rasters(clip, idx, sizes, vps)
+        ray_bits = None
+        if effective_visibility != 0:
+            ray_bits = self._ray_visibility(pos, idx, apos, anrm, araster, cams, ray_origin_bias)
 
         table = (ProjectionViewC * n)()
         for k in range(n):
@@ -314,9 +317,14 @@ class TextureBaker:
         valid = torch.empty((h, w), dtype=torch.float32, device=ctx.device)
         cov = torch.empty((h, w), dtype=torch.float32, device=ctx.device)
         faces = torch.empty((h, w), dtype=torch.int32, device=ctx.device)
-        _native.call("pdr_project_views", _ptr(apos), _ptr(anrm), _ptr(araster), N, _ptr(table_dev), n,
-                     BLEND_MODES[blend_mode], int(pcf_radius), effective_visibility, _ptr(color), _ptr(conf),
-                     _ptr(src), _ptr(valid), _ptr(cov), _ptr(faces), ctx.stream())
+        if ray_bits is None:
+            _native.call("pdr_project_views", _ptr(apos), _ptr(anrm), _ptr(araster), N, _ptr(table_dev), n,
+                         BLEND_MODES[blend_mode], int(pcf_radius), effective_visibility, _ptr(color), _ptr(conf),
+                         _ptr(src), _ptr(valid), _ptr(cov), _ptr(faces), ctx.stream())
+        else:
+            _native.call("pdr_project_views_bits", _ptr(apos), _ptr(anrm), _ptr(araster), N, _ptr(table_dev), n,
+                         BLEND_MODES[blend_mode], int(pcf_radius), effective_visibility, _ptr(ray_bits), _ptr(color),
+                         _ptr(conf), _ptr(src), _ptr(valid), _ptr(cov), _ptr(faces), ctx.stream())
         host = io.numpy or not isinstance(positions, torch.Tensor)
 
         def out(t, u32=False):
@@ -326,7 +334,27 @@ class TextureBaker:
             return t
 
         return TextureBakeOutput(w, h, out(color), out(conf), out(src, True), out(valid), out(cov), out(faces, True),
-                                 False)
+                                 ray_bits is not None)
+
+    def _ray_visibility(self, pos: torch.Tensor, idx: torch.Tensor, apos, anrm, araster, cams, bias: float):
+        """project_ray_visibility.hlsl through a device BVH: camera-visibility bits [texels, ceil(views/32)]."""
+        ctx = self.context
+        V, T = pos.shape[0], idx.shape[0]
+        bvh_bytes, build_bytes = C.c_size_t(), C.c_size_t()
+        _native.call("pdr_bvh_sizes", T, C.byref(bvh_bytes), C.byref(build_bytes))
+        bvh = torch.empty(bvh_bytes.value, dtype=torch.uint8, device=ctx.device)
+        scratch = torch.empty(build_bytes.value, dtype=torch.uint8, device=ctx.device)
+        _native.call("pdr_bvh_build", _ptr(pos), V, _ptr(idx), T, _ptr(bvh), bvh_bytes.value, _ptr(scratch),
+                     build_bytes.value, ctx.stream())
+        del scratch
+        n = cams.shape[0]
+        cam4 = torch.zeros((n, 4), dtype=torch.float32, device=ctx.device)
+        cam4[:, :3] = torch.from_numpy(np.ascontiguousarray(cams, dtype=np.float32)).to(ctx.device)
+        N = araster.numel() // 4
+        bits = torch.empty((N, (n + 31) // 32), dtype=torch.int32, device=ctx.device)
+        _native.call("pdr_ray_visibility", _ptr(bvh), T, _ptr(apos), _ptr(anrm), _ptr(araster), N, _ptr(cam4), n,
+                     float(bias), _ptr(bits), ctx.stream())
+        return bits
 
     # -- refine ----------------------------------------------------------------------------------
     def refine_texture(self, initial_texture, positions, uv, indices, images, world_to_clip, visibility_masks=None,

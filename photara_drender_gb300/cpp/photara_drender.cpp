@@ -98,7 +98,7 @@ DeviceInfo query_device(std::uint32_t index) {
     info.vendor_id = vendor;
     info.device_id = device;
     info.api_version = api;
-    info.supports_ray_query = false;
+    info.supports_ray_query = true;  // the library's BVH ray caster (csrc/bvh.cu)
     return info;
 }
 
@@ -526,7 +526,25 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
         scale = suggest_softmax_scale(positions, cams);
         if (!(scale > 0.0F) || !std::isfinite(scale)) scale = 1.0F;
     }
-    // shadow rasters, one per view
+    // ray visibility bits (visibility modes 1 and 2): BVH of the world-space mesh, one ray per texel and view
+    const std::uint32_t vis_mode = static_cast<std::uint32_t>(options.visibility_mode);
+    DeviceArray<std::uint32_t> ray_bits;
+    if (vis_mode != 0) {
+        std::size_t bvh_bytes = 0, build_bytes = 0;
+        check(pdr_bvh_sizes(T, &bvh_bytes, &build_bytes));
+        DeviceArray<unsigned char> bvh(bvh_bytes), scratch(build_bytes);
+        check(pdr_bvh_build(d_pos.get(), Vu, d_idx.get(), T, bvh.get(), bvh_bytes, scratch.get(), build_bytes, s));
+        std::vector<float> cams(views.size() * 4, 0.0F);
+        for (std::size_t i = 0; i < views.size(); ++i)
+            std::copy_n(views[i].camera_position.begin(), 3, cams.begin() + static_cast<std::ptrdiff_t>(i * 4));
+        DeviceArray<float> d_cams(cams.data(), cams.size(), s);
+        ray_bits = DeviceArray<std::uint32_t>(N * ((views.size() + 31) / 32));
+        check(pdr_ray_visibility(bvh.get(), T, d_apos.get(), d_anrm.get(), d_araster.get(),
+                                 static_cast<std::uint32_t>(N), d_cams.get(), static_cast<std::uint32_t>(views.size()),
+                                 options.ray_origin_bias, ray_bits.get(), s));
+        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+    // shadow rasters, one per view (not needed for ray-only visibility)
     std::vector<DeviceArray<float>> images, masks, shadows;
     std::vector<pdr_projection_view> table(views.size());
     DeviceArray<float> d_clip(V * 4);
@@ -537,8 +555,10 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
         check(pdr_transform_positions(d_pos.get(), Vu, d_m.get(), 1, d_clip.get(), s));
         const float vp4[4] = {vps[k].x, vps[k].y, vps[k].width, vps[k].height};
         DeviceArray<float> d_vvp(vp4, 4, s);
-        DeviceArray<float> shadow(P * 4);
-        rasterize_device(ctx, d_clip.get(), 1, Vu, d_idx.get(), T, v.width, v.height, d_vvp.get(), 0, shadow.get(), nullptr);
+        DeviceArray<float> shadow(vis_mode == 2 ? 0 : P * 4);
+        if (vis_mode != 2)
+            rasterize_device(ctx, d_clip.get(), 1, Vu, d_idx.get(), T, v.width, v.height, d_vvp.get(), 0,
+                             shadow.get(), nullptr);
         images.push_back(upload(std::span<const float>(v.image), s));
         masks.push_back(upload(std::span<const float>(v.visibility_mask), s));
         pdr_projection_view& t = table[k];
@@ -567,11 +587,19 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
                                        table.size() * sizeof(pdr_projection_view), s);
     DeviceArray<float> d_color(N * 4), d_conf(N), d_valid(N), d_cov(N);
     DeviceArray<std::uint32_t> d_src(N), d_faces(N);
-    check(pdr_project_views(d_apos.get(), d_anrm.get(), d_araster.get(), static_cast<std::uint32_t>(N),
-                            reinterpret_cast<const pdr_projection_view*>(d_table.get()),
-                            static_cast<std::uint32_t>(views.size()), static_cast<std::uint32_t>(options.blend_mode),
-                            options.pcf_radius, 0, d_color.get(), d_conf.get(), d_src.get(), d_valid.get(), d_cov.get(),
-                            d_faces.get(), s));
+    if (vis_mode == 0)
+        check(pdr_project_views(d_apos.get(), d_anrm.get(), d_araster.get(), static_cast<std::uint32_t>(N),
+                                reinterpret_cast<const pdr_projection_view*>(d_table.get()),
+                                static_cast<std::uint32_t>(views.size()), static_cast<std::uint32_t>(options.blend_mode),
+                                options.pcf_radius, 0, d_color.get(), d_conf.get(), d_src.get(), d_valid.get(),
+                                d_cov.get(), d_faces.get(), s));
+    else
+        check(pdr_project_views_bits(d_apos.get(), d_anrm.get(), d_araster.get(), static_cast<std::uint32_t>(N),
+                                     reinterpret_cast<const pdr_projection_view*>(d_table.get()),
+                                     static_cast<std::uint32_t>(views.size()),
+                                     static_cast<std::uint32_t>(options.blend_mode), options.pcf_radius, vis_mode,
+                                     ray_bits.get(), d_color.get(), d_conf.get(), d_src.get(), d_valid.get(),
+                                     d_cov.get(), d_faces.get(), s));
     TextureBakeOutput out;
     out.width = AW;
     out.height = AH;
@@ -581,7 +609,7 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
     out.valid_mask = d_valid.download(s);
     out.coverage_mask = d_cov.download(s);
     out.face_ids = d_faces.download(s);
-    out.used_ray_query = false;
+    out.used_ray_query = vis_mode != 0;
     return out;
 }
 

@@ -80,7 +80,8 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
                                      uint32_t blend_mode, uint32_t pcf_radius, uint32_t visibility_mode,
                                      float* __restrict__ color4, float* __restrict__ confidence,
                                      uint32_t* __restrict__ source_view, float* __restrict__ valid_mask,
-                                     float* __restrict__ coverage_mask, uint32_t* __restrict__ face_ids) {
+                                     float* __restrict__ coverage_mask, uint32_t* __restrict__ face_ids,
+                                     const uint32_t* __restrict__ vis_bits, uint32_t vis_words) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float rw = araster[i].w;
@@ -113,7 +114,9 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
             const float vl = sqrtf(vx0 * vx0 + vy0 * vy0 + vz0 * vz0);
             const float cosv = nx * (vx0 / vl) + ny * (vy0 / vl) + nz * (vz0 / vl);
             if (cosv < v.min_view_cosine) continue;
-            float vis = v.ray_visibility ? __ldg(v.ray_visibility + i) : 1.0f;
+            // ray visibility: one bit per (texel, view) from the BVH ray caster, or a per-view array
+            float vis = vis_bits ? (float)((__ldg(vis_bits + (size_t)i * vis_words + (k >> 5)) >> (k & 31u)) & 1u)
+                                 : (v.ray_visibility ? __ldg(v.ray_visibility + i) : 1.0f);
             if (visibility_mode == 0) vis = shadow_visibility(v, ppx, ppy, ndz, (int32_t)pcf_radius);
             else if (visibility_mode == 1) vis *= shadow_visibility(v, ppx, ppy, ndz, (int32_t)pcf_radius);
             if (v.has_mask) vis *= clamp_hlsl(sample_mask(v, ppx, ppy, v.mask_floor), 0.0f, 1.0f);
@@ -208,10 +211,10 @@ cudaError_t launch_project_views(const float* apos, const float* anrm, const flo
                                  const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,
                                  uint32_t pcf_radius, uint32_t visibility_mode, float* color4, float* confidence,
                                  uint32_t* source_view, float* valid_mask, float* coverage_mask, uint32_t* face_ids,
-                                 cudaStream_t stream) {
+                                 cudaStream_t stream, const uint32_t* vis_bits, uint32_t vis_words) {
     project_views_kernel<<<(N + 127) / 128, 128, 0, stream>>>(
         apos, anrm, reinterpret_cast<const float4*>(araster), N, views, nviews, blend_mode, pcf_radius,
-        visibility_mode, color4, confidence, source_view, valid_mask, coverage_mask, face_ids);
+        visibility_mode, color4, confidence, source_view, valid_mask, coverage_mask, face_ids, vis_bits, vis_words);
     return cudaGetLastError();
 }
 

@@ -88,7 +88,8 @@ cudaError_t launch_project_views(const float* apos, const float* anrm, const flo
                                  const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,
                                  uint32_t pcf_radius, uint32_t visibility_mode, float* color4, float* confidence,
                                  uint32_t* source_view, float* valid_mask, float* coverage_mask, uint32_t* face_ids,
-                                 cudaStream_t stream);
+                                 cudaStream_t stream, const uint32_t* vis_bits = nullptr,
+                                 uint32_t vis_words = 0);
 cudaError_t launch_transform_positions(const float* pos3, uint32_t V, const float* mats, uint32_t views, float* clip,
                                        cudaStream_t stream);
 cudaError_t launch_atlas_clip(const float* uv, uint32_t V, float* clip, cudaStream_t stream);

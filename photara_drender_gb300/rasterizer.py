@@ -64,7 +64,8 @@ def _device_info(index: int) -> DeviceInfo:
     vendor, dev, api = C.c_uint32(), C.c_uint32(), C.c_uint32()
     sms = C.c_int32()
     _native.call("pdr_device_info", index, name, 256, C.byref(vendor), C.byref(dev), C.byref(api), C.byref(sms))
-    return DeviceInfo(name.value.decode(), vendor.value, dev.value, api.value, False)
+    # ray queries run through the library's own BVH ray caster (csrc/bvh.cu) on every CUDA device
+    return DeviceInfo(name.value.decode(), vendor.value, dev.value, api.value, True)
 
 
 def _ptr(t: Optional[torch.Tensor]):

@@ -52,12 +52,17 @@ def test_bake_matches_oracle(baker, blend, mask_floor):
         assert np.array_equal(out.source_view, src) and same_bits(out.valid_mask, valid)
 
 
-def test_bake_default_visibility_falls_back_to_shadow_map(baker):
+def test_bake_default_visibility_uses_ray_queries(baker):
+    # the default visibility mode is ray_query (types.hpp:161); the device supports it through the BVH
+    # ray caster, so no fallback happens and allow_visibility_fallback=False is accepted
     pos3, nrm, uv, idx, images, mats, eyes, masks = bake_scene(views=2)
+    assert baker.device_info.supports_ray_query
     res = baker.bake(pos3, nrm, uv, idx, images, mats, eyes, resolution=(32, 32))
+    assert res[5] is True
+    res = baker.bake(pos3, nrm, uv, idx, images, mats, eyes, resolution=(32, 32), allow_visibility_fallback=False)
+    assert res[5] is True and res[3].any()
+    res = baker.bake(pos3, nrm, uv, idx, images, mats, eyes, resolution=(32, 32), visibility_mode="shadow_map")
     assert res[5] is False
-    with pytest.raises(RuntimeError):
-        baker.bake(pos3, nrm, uv, idx, images, mats, eyes, resolution=(32, 32), allow_visibility_fallback=False)
 
 
 def test_bake_known_answers(baker):
