@@ -50,6 +50,8 @@ typedef int32_t pdr_status;
 #define PDR_STATUS_TEXEL_ERROR 4   /* 1 non-finite uv on a covered pixel, 2 texel position beyond 1e9 */
 #define PDR_STATUS_INDEX_ERROR 5   /* 1 when a triangle index is >= the vertex count */
 #define PDR_STATUS_PRECOND_TIMEOUT 6 /* 1 when a tensor-core wait of the preconditioner MLP gave up */
+#define PDR_STATUS_PAD_ERROR 7     /* padding / surface fill: 1 a sweep wait gave up, 2 face id out of range,
+                                      4 degenerate edge, 8 non-manifold edge */
 
 PDR_API const char* pdr_last_error(void);
 PDR_API int32_t pdr_version(void);
@@ -461,6 +463,35 @@ PDR_API pdr_status pdr_project_views_bits(const float* atlas_positions, const fl
                                           uint32_t pcf_radius, uint32_t visibility_mode, const uint32_t* visibility,
                                           float* color, float* confidence, uint32_t* source_view, float* valid_mask,
                                           float* coverage_mask, uint32_t* face_ids, void* stream);
+
+/* ---- atlas padding and surface fill (src/texture_padding.cpp) --------------------------------------- */
+
+/* Workspace of pdr_pad_texture_atlas for a width x height atlas of `channels` channels. */
+PDR_API pdr_status pdr_pad_workspace_bytes(uint32_t width, uint32_t height, uint32_t channels, size_t* bytes);
+/* Replaces pad_texture_atlas (texture_padding.cpp:226-351; include/photara_drender/texture_padding.hpp:62-67)
+ * on the device, in place on color [height][width][channels] and filled_mask [height][width] (its
+ * previous contents are the output's earlier filled_mask, zeros when there was none). coverage_mask may
+ * be NULL. stats (5 device uint64): valid, gutter, unobserved, remaining_unobserved, filled texels. Sets
+ * status[PDR_STATUS_PAD_ERROR] bit 1 if a sweep wait gave up. Enqueues only; no host synchronisation. */
+PDR_API pdr_status pdr_pad_texture_atlas(float* color, uint32_t channels, const float* valid_mask,
+                                         const float* coverage_mask, float* filled_mask, uint32_t width,
+                                         uint32_t height, uint32_t margin, uint32_t fill_unobserved,
+                                         uint32_t maximum_fill_distance, float valid_threshold, void* workspace,
+                                         size_t workspace_bytes, uint64_t* stats, uint32_t* status, void* stream);
+/* Workspace of pdr_fill_texture_on_surface. */
+PDR_API pdr_status pdr_surface_fill_workspace_bytes(uint32_t width, uint32_t height, uint32_t triangle_count,
+                                                    size_t* bytes);
+/* Replaces fill_texture_on_surface (texture_padding.cpp:100-184; texture_padding.hpp:17-23) on the
+ * device. face_ids [height][width] (0xFFFFFFFF outside the mesh), indices [triangle_count][3] of the
+ * original (seam-free) mesh. stats (4 device uint64): filled texels, remaining texels, measured faces,
+ * propagated faces. Data errors set status[PDR_STATUS_PAD_ERROR] bits 2 (face id out of range), 4
+ * (degenerate edge), 8 (non-manifold edge) and then leave colour and filled_mask untouched; the
+ * reference raises them in that order of precedence. */
+PDR_API pdr_status pdr_fill_texture_on_surface(float* color, uint32_t channels, const float* valid_mask,
+                                               const uint32_t* face_ids, float* filled_mask, uint32_t width,
+                                               uint32_t height, const uint32_t* indices, uint32_t triangle_count,
+                                               void* workspace, size_t workspace_bytes, uint64_t* stats,
+                                               uint32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -398,3 +398,62 @@ def ray_visibility(positions, indices, atlas_positions, atlas_normals, atlas_ras
     _check(lib().ora_ray_visibility(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], _p(ap), _p(an), _p(ar),
                                     C.c_uint64(N), _p(cam), C.c_float(bias), state.ctypes.data_as(C.POINTER(C.c_int8))))
     return state
+
+
+# ---- atlas padding / surface fill (src/texture_padding.cpp) -------------------------------------
+
+PAD_REASONS = {1: "cannot pad an empty atlas", 2: "atlas dimensions exceed the supported maximum",
+               4: "atlas color must have 3 or 4 channels", 6: "valid_threshold must be within (0, 1]"}
+FILL_REASONS = {1: "surface fill requires mesh face IDs and a valid atlas",
+                2: "surface fill requires RGB or RGBA colours", 3: "surface fill has too many faces",
+                4: "atlas face ID is out of range", 5: "surface fill mesh has a degenerate edge",
+                6: "surface fill requires manifold edges"}
+
+
+def nearest_field(source_mask, threshold=0.5):
+    """texture_padding.cpp:37-95: int16 offsets (x, y) [H, W] from each texel to its nearest source."""
+    m = _f(source_mask)
+    h, w = m.shape
+    ox = np.empty((h, w), np.int16)
+    oy = np.empty((h, w), np.int16)
+    _check(lib().ora_nearest_field_offsets(_p(m), w, h, C.c_float(threshold), ox.ctypes.data_as(C.c_void_p),
+                                           oy.ctypes.data_as(C.c_void_p)))
+    return ox, oy
+
+
+def pad_texture_atlas(color, valid_mask, margin=4, *, coverage_mask=None, filled_mask=None, fill_unobserved=True,
+                      maximum_fill_distance=0, valid_threshold=0.5):
+    """texture_padding.cpp:226-351 on copies: (color, filled_mask, stats) with stats = (valid, gutter,
+    unobserved, remaining_unobserved, filled)."""
+    col = np.array(color, dtype=np.float32, copy=True, order="C")
+    h, w, ch = col.shape
+    valid = _f(valid_mask)
+    cov = None if coverage_mask is None else _f(coverage_mask)
+    filled = np.zeros((h, w), np.float32) if filled_mask is None else np.array(filled_mask, np.float32, copy=True)
+    stats = np.zeros(5, np.uint64)
+    reason = C.c_int(0)
+    rc = lib().ora_pad_texture_atlas(_p(col), ch, _p(valid), _p(cov) if cov is not None else None, _p(filled), w, h,
+                                     int(margin), int(bool(fill_unobserved)), int(maximum_fill_distance),
+                                     C.c_float(valid_threshold), stats.ctypes.data_as(C.c_void_p), C.byref(reason))
+    if rc < 0:
+        raise ValueError(PAD_REASONS.get(reason.value, "invalid padding input"))
+    return col, filled, tuple(int(s) for s in stats)
+
+
+def fill_texture_on_surface(color, valid_mask, face_ids, indices, *, filled_mask=None):
+    """texture_padding.cpp:100-184 on copies: (color, filled_mask, stats) with stats = (filled,
+    remaining, measured faces, propagated faces)."""
+    col = np.array(color, dtype=np.float32, copy=True, order="C")
+    h, w, ch = col.shape
+    valid = _f(valid_mask)
+    faces = np.ascontiguousarray(face_ids, dtype=np.uint32)
+    idx = _u(indices)
+    filled = np.zeros((h, w), np.float32) if filled_mask is None else np.array(filled_mask, np.float32, copy=True)
+    stats = np.zeros(4, np.uint64)
+    reason = C.c_int(0)
+    rc = lib().ora_fill_texture_on_surface(_p(col), ch, _p(valid), _p(faces, _u32p), _p(filled), w, h,
+                                           _p(idx, _u32p), idx.size // 3, stats.ctypes.data_as(C.c_void_p),
+                                           C.byref(reason))
+    if rc < 0:
+        raise ValueError(FILL_REASONS.get(reason.value, "invalid surface fill input"))
+    return col, filled, tuple(int(s) for s in stats)

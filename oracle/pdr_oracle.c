@@ -1220,3 +1220,210 @@ int ora_ray_visibility(const float* pos3, uint32_t V, const uint32_t* idx, uint3
     }
     return 0;
 }
+
+/* ---- atlas padding and surface fill: src/texture_padding.cpp:37-351 --------------------- */
+
+#define ORA_PAD_FAR 12000 /* texture_padding.cpp:20, offset of texels with no source yet */
+#define ORA_PAD_MAX_SIDE 16384 /* texture_padding.cpp:18, offsets are clamped to +-this */
+
+typedef struct {
+    int32_t w, h;
+    int16_t* ox;
+    int16_t* oy;
+} ora_field;
+
+/* One relaxation step of texture_padding.cpp:54-78: adopt the neighbour's nearest source when it is
+ * strictly closer (squared length of the offset; ties keep the current one). */
+static void ora_relax(ora_field* f, int32_t x, int32_t y, int32_t nx, int32_t ny) {
+    if (nx < 0 || ny < 0 || nx >= f->w || ny >= f->h) return;
+    const uint64_t c = (uint64_t)y * (uint64_t)f->w + (uint64_t)x;
+    const uint64_t n = (uint64_t)ny * (uint64_t)f->w + (uint64_t)nx;
+    const int32_t cx = (int32_t)f->ox[n] + (nx - x), cy = (int32_t)f->oy[n] + (ny - y);
+    const int64_t cand = (int64_t)cx * cx + (int64_t)cy * cy;
+    const int64_t cur = (int64_t)f->ox[c] * f->ox[c] + (int64_t)f->oy[c] * f->oy[c];
+    if (cand >= cur) return;
+    f->ox[c] = (int16_t)clampi(cx, -ORA_PAD_MAX_SIDE, ORA_PAD_MAX_SIDE);
+    f->oy[c] = (int16_t)clampi(cy, -ORA_PAD_MAX_SIDE, ORA_PAD_MAX_SIDE);
+}
+
+/* texture_padding.cpp:37-95: Danielsson 8SSEDT, one raster-order sweep and one reverse sweep. */
+static void ora_nearest_field(ora_field* f, const float* source_mask, float threshold) {
+    const uint64_t n = (uint64_t)f->w * (uint64_t)f->h;
+    for (uint64_t i = 0; i < n; ++i) {
+        const int src = source_mask[i] >= threshold;
+        f->ox[i] = src ? 0 : ORA_PAD_FAR;
+        f->oy[i] = src ? 0 : ORA_PAD_FAR;
+    }
+    for (int32_t y = 0; y < f->h; ++y)
+        for (int32_t x = 0; x < f->w; ++x) {
+            ora_relax(f, x, y, x - 1, y);
+            ora_relax(f, x, y, x, y - 1);
+            ora_relax(f, x, y, x - 1, y - 1);
+            ora_relax(f, x, y, x + 1, y - 1);
+        }
+    for (int32_t y = f->h - 1; y >= 0; --y)
+        for (int32_t x = f->w - 1; x >= 0; --x) {
+            ora_relax(f, x, y, x + 1, y);
+            ora_relax(f, x, y, x, y + 1);
+            ora_relax(f, x, y, x + 1, y + 1);
+            ora_relax(f, x, y, x - 1, y + 1);
+        }
+}
+
+int ora_nearest_field_offsets(const float* source_mask, uint32_t width, uint32_t height, float threshold,
+                              int16_t* offset_x, int16_t* offset_y) {
+    if (width == 0 || height == 0 || width > ORA_PAD_MAX_SIDE || height > ORA_PAD_MAX_SIDE) return ORA_INVALID;
+    ora_field f = {(int32_t)width, (int32_t)height, offset_x, offset_y};
+    ora_nearest_field(&f, source_mask, threshold);
+    return ORA_OK;
+}
+
+int ora_pad_texture_atlas(float* color, uint32_t channels, const float* valid, const float* coverage, float* filled,
+                          uint32_t width, uint32_t height, uint32_t margin, int fill_unobserved,
+                          uint32_t maximum_fill_distance, float threshold, uint64_t stats[5], int* reason) {
+    /* texture_padding.cpp:226-351; stats = valid, gutter, unobserved, remaining_unobserved, filled */
+    *reason = 0;
+    for (int k = 0; k < 5; ++k) stats[k] = 0;
+    if (width == 0 || height == 0) { *reason = 1; return ORA_INVALID; }
+    if (width > ORA_PAD_MAX_SIDE || height > ORA_PAD_MAX_SIDE) { *reason = 2; return ORA_INVALID; }
+    if (channels != 3 && channels != 4) { *reason = 4; return ORA_INVALID; }
+    if (!isfinite(threshold) || threshold <= 0.0f || threshold > 1.0f) { *reason = 6; return ORA_INVALID; }
+    const uint64_t n = (uint64_t)width * height;
+    float* source = (float*)malloc(n * sizeof(float));
+    memcpy(source, valid, n * sizeof(float));
+    for (uint64_t i = 0; i < n; ++i) {
+        if (valid[i] >= threshold) {
+            ++stats[0];
+        } else if (filled[i] > 0.5f && coverage && coverage[i] > 0.5f) {
+            source[i] = 1.0f;
+            ++stats[2];
+            ++stats[4];
+        } else {
+            filled[i] = 0.0f;
+        }
+    }
+    if (stats[0] == 0 && stats[4] == 0) { free(source); return ORA_OK; }
+    ora_field f = {(int32_t)width, (int32_t)height, (int16_t*)malloc(n * 2), (int16_t*)malloc(n * 2)};
+    ora_nearest_field(&f, source, threshold);
+    const int64_t margin2 = (int64_t)margin * margin;
+    const int64_t limit2 = maximum_fill_distance == 0 ? INT64_MAX
+                                                       : (int64_t)maximum_fill_distance * maximum_fill_distance;
+    const int64_t none2 = 2LL * ORA_PAD_FAR * ORA_PAD_FAR;
+    for (uint32_t y = 0; y < height; ++y)
+        for (uint32_t x = 0; x < width; ++x) {
+            const uint64_t p = (uint64_t)y * width + x;
+            if (source[p] >= threshold) continue;
+            const int32_t ox = f.ox[p], oy = f.oy[p];
+            const int64_t d2 = (int64_t)ox * ox + (int64_t)oy * oy;
+            if (d2 >= none2) continue;
+            const int32_t sx = (int32_t)x + ox, sy = (int32_t)y + oy;
+            if (sx < 0 || sy < 0 || sx >= (int32_t)width || sy >= (int32_t)height) continue;
+            const uint64_t s = (uint64_t)sy * width + (uint32_t)sx;
+            const int covered = coverage && coverage[p] > 0.5f;
+            int fill = 0;
+            if (!covered) fill = margin > 0 && d2 <= margin2;
+            else if (fill_unobserved) fill = d2 <= limit2;
+            if (!fill) {
+                if (covered) ++stats[3];
+                continue;
+            }
+            for (uint32_t c = 0; c < channels; ++c) color[p * channels + c] = color[s * channels + c];
+            if (channels == 4) color[p * 4 + 3] = 1.0f;
+            filled[p] = 1.0f;
+            ++stats[4];
+            ++stats[covered ? 2 : 1];
+        }
+    free(f.ox);
+    free(f.oy);
+    free(source);
+    return ORA_OK;
+}
+
+typedef struct {
+    uint64_t key;
+    uint32_t face, slot;
+} ora_edge;
+
+static int ora_edge_cmp(const void* a, const void* b) {
+    const uint64_t x = ((const ora_edge*)a)->key, y = ((const ora_edge*)b)->key;
+    return x < y ? -1 : x > y;
+}
+
+int ora_fill_texture_on_surface(float* color, uint32_t channels, const float* valid, const uint32_t* face_ids,
+                                float* filled, uint32_t width, uint32_t height, const uint32_t* indices,
+                                uint32_t triangle_count, uint64_t stats[4], int* reason) {
+    /* texture_padding.cpp:100-184; stats = filled, remaining, measured faces, propagated faces */
+    const uint32_t none = 0xFFFFFFFFu;
+    const uint64_t n = (uint64_t)width * height;
+    *reason = 0;
+    for (int k = 0; k < 4; ++k) stats[k] = 0;
+    if (n == 0 || triangle_count == 0) { *reason = 1; return ORA_INVALID; }
+    if (channels != 3 && channels != 4) { *reason = 2; return ORA_INVALID; }
+    if (triangle_count >= none) { *reason = 3; return ORA_INVALID; }
+    const uint32_t faces = triangle_count;
+    double* means = (double*)calloc((size_t)faces * 3, sizeof(double));
+    uint32_t* counts = (uint32_t*)calloc(faces, sizeof(uint32_t));
+    for (uint64_t p = 0; p < n; ++p) {
+        const uint32_t f = face_ids[p];
+        if (f == none) continue;
+        if (f >= faces) { *reason = 4; free(means); free(counts); return ORA_INVALID; }
+        if (valid[p] < 0.5f) continue;
+        ++counts[f];
+        for (int c = 0; c < 3; ++c) means[(uint64_t)f * 3 + c] += color[p * channels + c];
+    }
+    ora_edge* edges = (ora_edge*)malloc((size_t)faces * 3 * sizeof(ora_edge));
+    for (uint32_t f = 0; f < faces; ++f)
+        for (uint32_t e = 0; e < 3; ++e) {
+            const uint32_t a = indices[(uint64_t)f * 3 + e], b = indices[(uint64_t)f * 3 + (e + 1) % 3];
+            if (a == b) { *reason = 5; free(means); free(counts); free(edges); return ORA_INVALID; }
+            const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+            edges[(uint64_t)f * 3 + e] = (ora_edge){((uint64_t)lo << 32) | hi, f, e};
+        }
+    qsort(edges, (size_t)faces * 3, sizeof(ora_edge), ora_edge_cmp);
+    uint32_t* nb = (uint32_t*)malloc((size_t)faces * 3 * sizeof(uint32_t));
+    for (uint64_t i = 0; i < (uint64_t)faces * 3; ++i) nb[i] = none;
+    for (uint64_t b = 0; b < (uint64_t)faces * 3;) {
+        uint64_t e = b + 1;
+        while (e < (uint64_t)faces * 3 && edges[e].key == edges[b].key) ++e;
+        if (e - b > 2) { *reason = 6; free(means); free(counts); free(edges); free(nb); return ORA_INVALID; }
+        if (e - b == 2) {
+            nb[(uint64_t)edges[b].face * 3 + edges[b].slot] = edges[b + 1].face;
+            nb[(uint64_t)edges[b + 1].face * 3 + edges[b + 1].slot] = edges[b].face;
+        }
+        b = e;
+    }
+    free(edges);
+    uint32_t* sources = (uint32_t*)malloc((size_t)faces * sizeof(uint32_t));
+    uint32_t* queue = (uint32_t*)malloc((size_t)faces * sizeof(uint32_t));
+    uint64_t tail = 0;
+    for (uint32_t f = 0; f < faces; ++f) {
+        sources[f] = none;
+        if (counts[f] == 0) continue;
+        for (int c = 0; c < 3; ++c) means[(uint64_t)f * 3 + c] /= counts[f];
+        sources[f] = f;
+        queue[tail++] = f;
+        ++stats[2];
+    }
+    for (uint64_t head = 0; head < tail; ++head) {
+        const uint32_t f = queue[head];
+        for (int s = 0; s < 3; ++s) {
+            const uint32_t g = nb[(uint64_t)f * 3 + s];
+            if (g == none || sources[g] != none) continue;
+            sources[g] = sources[f];
+            queue[tail++] = g;
+            ++stats[3];
+        }
+    }
+    for (uint64_t p = 0; p < n; ++p) {
+        const uint32_t f = face_ids[p];
+        if (f == none || valid[p] >= 0.5f) continue;
+        const uint32_t s = sources[f];
+        if (s == none) { ++stats[1]; continue; }
+        for (int c = 0; c < 3; ++c) color[p * channels + c] = (float)means[(uint64_t)s * 3 + c];
+        if (channels == 4) color[p * 4 + 3] = 1.0f;
+        filled[p] = 1.0f;
+        ++stats[0];
+    }
+    free(means); free(counts); free(nb); free(sources); free(queue);
+    return ORA_OK;
+}

@@ -166,6 +166,23 @@ double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C,
                        const uint8_t* valid, const int32_t* chart, float eps, float weight,
                        float* grad);
 
+/* src/texture_padding.cpp:37-95: the 8SSEDT nearest-source offsets (sources: mask >= threshold). */
+int ora_nearest_field_offsets(const float* source_mask, uint32_t width, uint32_t height, float threshold,
+                              int16_t* offset_x, int16_t* offset_y);
+/* src/texture_padding.cpp:226-351 pad_texture_atlas, in place on color [H][W][channels] and filled
+ * [H][W] (pass zeros for an absent filled_mask). coverage may be NULL. stats: valid, gutter,
+ * unobserved, remaining_unobserved, filled. reason (on ORA_INVALID): 1 empty atlas, 2 too large,
+ * 4 channel count, 6 threshold. */
+int ora_pad_texture_atlas(float* color, uint32_t channels, const float* valid, const float* coverage, float* filled,
+                          uint32_t width, uint32_t height, uint32_t margin, int fill_unobserved,
+                          uint32_t maximum_fill_distance, float threshold, uint64_t stats[5], int* reason);
+/* src/texture_padding.cpp:100-184 fill_texture_on_surface. stats: filled, remaining, measured faces,
+ * propagated faces. reason: 1 empty atlas or mesh, 2 channel count, 3 too many faces, 4 face id out
+ * of range, 5 degenerate edge, 6 non-manifold edge. */
+int ora_fill_texture_on_surface(float* color, uint32_t channels, const float* valid, const uint32_t* face_ids,
+                                float* filled, uint32_t width, uint32_t height, const uint32_t* indices,
+                                uint32_t triangle_count, uint64_t stats[4], int* reason);
+
 #ifdef __cplusplus
 }
 #endif

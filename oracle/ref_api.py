@@ -202,3 +202,38 @@ def adam_update(tex, grad, m, v, lr, b1, b2, eps, bc1, bc2, cmin, cmax):
 def suggest_softmax_scale(positions, camera_positions):
     pos, cams = api._f(positions), api._f(camera_positions)
     return float(_L().ref_suggest_softmax_scale(_p(pos), pos.shape[0], _p(cams), cams.shape[0]))
+
+
+def pad_texture_atlas(color, valid_mask, margin=4, *, coverage_mask=None, filled_mask=None, fill_unobserved=True,
+                      maximum_fill_distance=0, valid_threshold=0.5):
+    """The reference's pad_texture_atlas on copies: (color, filled_mask, stats) as oracle.api."""
+    col = np.array(color, dtype=np.float32, copy=True, order="C")
+    h, w, ch = col.shape
+    valid = api._f(valid_mask)
+    cov = None if coverage_mask is None else api._f(coverage_mask)
+    filled = np.zeros((h, w), np.float32) if filled_mask is None else np.array(filled_mask, np.float32, copy=True)
+    stats = np.zeros(5, np.uint64)
+    msg = C.create_string_buffer(256)
+    rc = _L().ref_pad_texture_atlas(_p(col), ch, _p(valid), _p(cov) if cov is not None else None, _p(filled), w, h,
+                                    int(margin), int(bool(fill_unobserved)), int(maximum_fill_distance),
+                                    C.c_float(valid_threshold), stats.ctypes.data_as(C.c_void_p), msg, 256)
+    if rc < 0:
+        raise ValueError(msg.value.decode())
+    return col, filled, tuple(int(s) for s in stats)
+
+
+def fill_texture_on_surface(color, valid_mask, face_ids, indices, *, filled_mask=None):
+    """The reference's fill_texture_on_surface on copies: (color, filled_mask, stats) as oracle.api."""
+    col = np.array(color, dtype=np.float32, copy=True, order="C")
+    h, w, ch = col.shape
+    valid = api._f(valid_mask)
+    faces = np.ascontiguousarray(face_ids, dtype=np.uint32)
+    idx = api._u(indices)
+    filled = np.zeros((h, w), np.float32) if filled_mask is None else np.array(filled_mask, np.float32, copy=True)
+    stats = np.zeros(4, np.uint64)
+    msg = C.create_string_buffer(256)
+    rc = _L().ref_fill_texture_on_surface(_p(col), ch, _p(valid), _p(faces, _u32p), _p(filled), w, h, _p(idx, _u32p),
+                                          idx.size // 3, stats.ctypes.data_as(C.c_void_p), msg, 256)
+    if rc < 0:
+        raise ValueError(msg.value.decode())
+    return col, filled, tuple(int(s) for s in stats)

@@ -26,6 +26,7 @@ STATUS_TILE_OVERFLOW = 2
 STATUS_TEXEL_ERROR = 4
 STATUS_INDEX_ERROR = 5
 STATUS_PRECOND_TIMEOUT = 6
+STATUS_PAD_ERROR = 7
 
 _vp = C.c_void_p
 _u32 = C.c_uint32
@@ -64,6 +65,11 @@ _SIGNATURES = {
     "pdr_ray_visibility": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, C.c_float, _vp, _vp]),
     "pdr_project_views_bits": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp, _vp]),
+    "pdr_pad_workspace_bytes": (_i32, [_u32, _u32, _u32, _vp]),
+    "pdr_pad_texture_atlas": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _u32, C.c_float, _vp, _sz, _vp,
+                                     _vp, _vp]),
+    "pdr_surface_fill_workspace_bytes": (_i32, [_u32, _u32, _u32, _vp]),
+    "pdr_fill_texture_on_surface": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _u32, _vp, _u32, _vp, _sz, _vp, _vp, _vp]),
     "pdr_refine_prepare_view": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "pdr_refine_photometric": (_i32, [_vp, _u32, _u32, _vp, _u32, _u64, _u32, _u32, C.c_float, C.c_float, _vp, _vp,
                                       _vp]),

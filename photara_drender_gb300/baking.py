@@ -90,6 +90,7 @@ class TextureBakeOutput:
     coverage_mask: np.ndarray
     face_ids: np.ndarray
     used_ray_query: bool = False
+    filled_mask: Optional[np.ndarray] = None  # texels extrapolated by padding / surface fill
 
 
 class BakedTexture(NamedTuple):
@@ -520,5 +521,10 @@ def project_texture_atlas(mesh: UnwrappedMesh, images: Sequence[np.ndarray], wor
                      mask_floor=float(mask_floor))
     baked = BakedTexture(*out)
     if padding or fill_unobserved:
-        raise NotImplementedError("atlas padding (pad_texture_atlas) is not part of this build")
+        from .padding import pad_texture_atlas
+
+        baked = baked._replace(color=pad_texture_atlas(baked.color, baked.valid_mask, padding,
+                                                       coverage_mask=baked.coverage_mask,
+                                                       fill_unobserved=fill_unobserved,
+                                                       maximum_fill_distance=maximum_fill_distance))
     return baked

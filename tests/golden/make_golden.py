@@ -12,7 +12,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))  # the repository root
 
 from oracle import api, ref_api  # noqa: E402
 from photara_drender_gb300 import synthetic as S  # noqa: E402
@@ -135,6 +135,33 @@ def projection_case():
     np.savez_compressed(os.path.join(HERE, "projection_small.npz"), **out)
 
 
+def padding_case():
+    """pad_texture_atlas and fill_texture_on_surface of the reference's texture_padding.cpp."""
+    from tests.padding_cases import chart_atlas, surface_case
+
+    rng = np.random.default_rng(21)
+    out = {}
+    settings = [(4, True, 0, 0.5), (2, False, 0, 0.5), (0, True, 3, 0.5), (6, True, 0, 1.0), (1, True, 8, 0.25)]
+    for k, (margin, fill, limit, thr) in enumerate(settings):
+        h, w = [(40, 48), (33, 61), (64, 31), (45, 45), (17, 70)][k]
+        color, valid, cov, filled = chart_atlas(rng, h, w, 4 if k % 2 == 0 else 3)
+        c, f, st = ref_api.pad_texture_atlas(color, valid, margin, coverage_mask=cov if k != 3 else None,
+                                             filled_mask=filled, fill_unobserved=fill, maximum_fill_distance=limit,
+                                             valid_threshold=thr)
+        out.update({f"p{k}_color": color, f"p{k}_valid": valid, f"p{k}_cov": cov, f"p{k}_filled": filled,
+                    f"p{k}_args": np.array([margin, fill, limit], np.int64), f"p{k}_thr": np.float32(thr),
+                    f"p{k}_out": c, f"p{k}_out_filled": f, f"p{k}_stats": np.array(st, np.uint64)})
+    pos3, idx = S.icosphere(2)
+    uv = S.spherical_uv(pos3)
+    for k in range(2):
+        color, valid, faces = surface_case(rng, pos3, idx, uv, (48, 56), 4 - k)
+        c, f, st = ref_api.fill_texture_on_surface(color, valid, faces, idx)
+        out.update({f"s{k}_color": color, f"s{k}_valid": valid, f"s{k}_faces": faces, f"s{k}_out": c,
+                    f"s{k}_out_filled": f, f"s{k}_stats": np.array(st, np.uint64)})
+    out["s_idx"] = idx.astype(np.uint32)
+    np.savez_compressed(os.path.join(HERE, "padding_small.npz"), **out)
+
+
 if __name__ == "__main__":
     if not ref_api.available():
         raise SystemExit("reference sources not available")
@@ -142,6 +169,7 @@ if __name__ == "__main__":
     sphere_case()
     atlas_case()
     projection_case()
+    padding_case()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
