@@ -30,6 +30,7 @@ WORKLOAD = dict(name="c2_fwdbwd_200k_64x1024sq_atlas4096", triangles=200_000, vi
                 attributes=3, atlas=4096, channels=4, seed=0)
 METRIC = "fwd+bwd Mpix/s"
 CPU_SAMPLE_SECONDS = 10.0  # bounded CPU-baseline sample: whole views until this much oracle time
+SKIP_CPU_PAD = False  # set by --skip-cpu: no oracle padding beside the GPU padding
 
 
 def scene(w=WORKLOAD):
@@ -304,14 +305,17 @@ def c1_leg(dev, hbm):
 
 
 def bake_leg(dev, hbm):
-    """C2 bake: weighted-average projection of 64 noisy views with PCF shadow-map visibility."""
+    """C2 bake: weighted-average projection of 64 noisy views, PCF 1, in the reference's default ray-query
+    visibility (device BVH + any-hit rays per texel and view) and with shadow maps; then padding
+    (margin 4, unobserved texels filled) and surface fill of the ray-query atlas."""
     import torch
 
     from photara_drender_gb300 import TextureBaker
+    from photara_drender_gb300 import padding as PAD
     from photara_drender_gb300 import synthetic as S
 
     b = BAKE
-    pos3, nrm, uv, idx, _, _ = S.displaced_sphere(b["triangles"], seed=b["seed"], atlas_size=b["atlas"])
+    pos3, nrm, uv, idx, _, remap = S.displaced_sphere(b["triangles"], seed=b["seed"], atlas_size=b["atlas"])
     mats, eyes = S.orbit_cameras(b["views"], radius=3.0, fov_y_deg=45.0, aspect=b["width"] / b["height"])
     baker = TextureBaker(dev.index or 0)
     t_pos, t_nrm, t_uv = (torch.tensor(a, device=dev) for a in (pos3, nrm, uv))
@@ -321,34 +325,73 @@ def bake_leg(dev, hbm):
     g = torch.Generator(device=dev).manual_seed(b["seed"])
     images = (color + 0.01 * torch.randn(color.shape, device=dev, generator=g)).contiguous()
     views = [images[k] for k in range(b["views"])]
-
-    def run():
-        return baker.bake_output(t_pos, t_nrm, t_uv, t_idx, views, mats, eyes, resolution=(b["atlas"], b["atlas"]),
-                                 blend_mode="weighted_average", visibility_mode="shadow_map", pcf_radius=1)
-
-    out = run()
-    torch.cuda.synchronize(dev)
-    reps, times = 3, []
-    for _ in range(reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize(dev)
-        e0.record()
-        out = run()
-        e1.record()
-        torch.cuda.synchronize(dev)
-        times.append(e0.elapsed_time(e1) / 1e3)
-    s = float(np.median(times))
     N = b["atlas"] ** 2
     P = b["views"] * b["height"] * b["width"]
-    # atlas G-buffer read 28 B/texel, outputs 36 B/texel, per view pixel: shadow depth 4 + photo 12 + mask 4
-    alg = N * (28 + 36) + P * 20
-    valid = out.valid_mask > 0.5
-    err = (out.color[..., :3] - gt).abs()[valid].mean().item() if bool(valid.any()) else None
-    return {"workload": b["name"], "seconds": s, "gtexel_views_per_s": N * b["views"] / s / 1e9,
-            "algorithmic_bytes": alg, "achieved_gbs": alg / s / 1e9, "frac": alg / s / 1e9 / hbm,
-            "valid_texels": int(valid.sum().item()), "mean_abs_error_vs_ground_truth": err,
-            "timing": "median of 3 TextureBaker.bake_output calls on device-resident views (host validation and "
-                      "the per-view shadow rasters included)"}
+
+    def timed(fn, reps=3):
+        out = fn()
+        torch.cuda.synchronize(dev)
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            out = fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return out, float(np.median(times))
+
+    res = {"workload": b["name"], "timing": "median of 3 TextureBaker.bake_output calls on device-resident views "
+                                            "(host validation, BVH build or per-view shadow rasters included)"}
+    outs = {}
+    for mode in ("ray_query", "shadow_map"):
+        out, s = timed(lambda: baker.bake_output(t_pos, t_nrm, t_uv, t_idx, views, mats, eyes,
+                                                 resolution=(b["atlas"], b["atlas"]), blend_mode="weighted_average",
+                                                 visibility_mode=mode, pcf_radius=1))
+        # atlas G-buffer read 28 B/texel, outputs 36 B/texel, per view pixel: photo 12 + mask 4 (+ shadow depth 4)
+        alg = N * (28 + 36) + P * (16 if mode == "ray_query" else 20)
+        valid = out.valid_mask > 0.5
+        err = (out.color[..., :3] - gt).abs()[valid].mean().item() if bool(valid.any()) else None
+        res[mode] = {"seconds": s, "gtexel_views_per_s": N * b["views"] / s / 1e9, "algorithmic_bytes": alg,
+                     "achieved_gbs": alg / s / 1e9, "frac": alg / s / 1e9 / hbm,
+                     "valid_texels": int(valid.sum().item()), "mean_abs_error_vs_ground_truth": err}
+        outs[mode] = out
+    out = outs["ray_query"]
+    cov = out.coverage_mask.contiguous()
+    valid = out.valid_mask.contiguous()
+    work = out.color.clone()
+    filled = torch.zeros_like(valid)
+
+    def pad():
+        work.copy_(out.color)
+        filled.zero_()
+        return PAD.pad_texture_atlas_device(work, valid, 4, cov, True, 0, filled_mask=filled)
+
+    st, s_pad = timed(pad)
+    copy_s = timed(lambda: work.copy_(out.color))[1]
+    s_pad = max(s_pad - copy_s, 1e-9)
+    # colour read once and written once, valid / coverage / filled read, filled written: 16+16+4+4+4+4 B
+    pad_bytes = N * 48
+    res["padding"] = {"seconds": s_pad, "texels_per_s": N / s_pad, "stats": list(st), "algorithmic_bytes": pad_bytes,
+                      "achieved_gbs": pad_bytes / s_pad / 1e9,
+                      "note": "pad_texture_atlas(margin=4, fill_unobserved) on the ray-query atlas; the copy that "
+                              "restores the input each repetition is timed separately and subtracted"}
+    welded = torch.tensor(remap[idx].astype(np.int32), device=dev)
+    faces = out.face_ids.contiguous()
+    sf, s_fill = timed(lambda: PAD.fill_texture_on_surface(out.color, valid, faces, welded))
+    res["surface_fill"] = {"seconds": s_fill, "stats": list(sf[2]),
+                           "note": "fill_texture_on_surface on the ray-query atlas with the welded mesh topology "
+                                   "(copies of colour and filled_mask included)"}
+    if not SKIP_CPU_PAD:
+        from oracle import api as oracle_api
+
+        host = (out.color.cpu().numpy(), valid.cpu().numpy(), cov.cpu().numpy())
+        t0 = time.perf_counter()
+        oracle_api.pad_texture_atlas(host[0], host[1], 4, coverage_mask=host[2], fill_unobserved=True)
+        res["padding"]["cpu_oracle_seconds"] = time.perf_counter() - t0
+        res["padding"]["cpu_oracle"] = "oracle restatement of texture_padding.cpp, one host thread (as the reference)"
+    return res
 
 
 def refine_scene(c, dev, baker):
@@ -804,6 +847,8 @@ def run_gpu(args, world, rank, local):
             "clocks": clocks.summary(),
         }
         if world == 1:
+            global SKIP_CPU_PAD
+            SKIP_CPU_PAD = args.skip_cpu
             for key, skip, leg in (("c1", args.skip_c1, c1_leg), ("bake", args.skip_bake, bake_leg),
                                    ("refine", args.skip_refine, refine_leg), ("c4", args.skip_c4, c4_leg),
                                    ("precond", args.skip_precond, c5_leg)):

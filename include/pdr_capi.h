@@ -455,6 +455,14 @@ PDR_API pdr_status pdr_ray_visibility(const void* bvh, uint32_t triangle_count, 
                                       const float* atlas_normals, const float* atlas_raster, uint32_t atlas_texels,
                                       const float* cameras, uint32_t view_count, float ray_origin_bias,
                                       uint32_t* visibility, void* stream);
+/* pdr_ray_visibility for the texel-views the projection reads: views (device memory, the projection's
+ * table) whose camera the texel faces by min_view_cosine and whose clip volume and viewport contain it.
+ * The other bits are 0; pdr_project_views_bits never reads them, so the bake is unchanged. */
+PDR_API pdr_status pdr_ray_visibility_views(const void* bvh, uint32_t triangle_count, const float* atlas_positions,
+                                            const float* atlas_normals, const float* atlas_raster,
+                                            uint32_t atlas_texels, const pdr_projection_view* views,
+                                            uint32_t view_count, float ray_origin_bias, uint32_t* visibility,
+                                            void* stream);
 /* pdr_project_views for visibility modes 1 (ray x shadow map) and 2 (ray) with the visibility bits of
  * pdr_ray_visibility instead of per-view arrays. */
 PDR_API pdr_status pdr_project_views_bits(const float* atlas_positions, const float* atlas_normals,

@@ -63,6 +63,7 @@ _SIGNATURES = {
     "pdr_bvh_sizes": (_i32, [_u32, _vp, _vp]),
     "pdr_bvh_build": (_i32, [_vp, _u32, _vp, _u32, _vp, _sz, _vp, _sz, _vp]),
     "pdr_ray_visibility": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, C.c_float, _vp, _vp]),
+    "pdr_ray_visibility_views": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, C.c_float, _vp, _vp]),
     "pdr_project_views_bits": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp, _vp]),
     "pdr_pad_workspace_bytes": (_i32, [_u32, _u32, _u32, _vp]),

@@ -289,10 +289,6 @@ class TextureBaker:
         if effective_visibility != 2:
             clip = self._transform(pos, torch.from_numpy(mats).to(ctx.device))
             shadows = self._rasters(clip, idx, sizes, vps)
-        ray_bits = None
-        if effective_visibility != 0:
-            ray_bits = self._ray_visibility(pos, idx, apos, anrm, araster, cams, ray_origin_bias)
-
         table = (ProjectionViewC * n)()
         for k in range(n):
             v = table[k]
@@ -310,6 +306,9 @@ class TextureBaker:
             v.shadow_raster = shadows[k].data_ptr() if shadows[k] is not None else None
             v.ray_visibility = None
         table_dev = torch.frombuffer(bytearray(bytes(table)), dtype=torch.uint8).to(ctx.device)
+        ray_bits = None
+        if effective_visibility != 0:
+            ray_bits = self._ray_visibility(pos, idx, apos, anrm, araster, cams, ray_origin_bias, views=table_dev)
 
         N = h * w
         color = torch.empty((h, w, 4), dtype=torch.float32, device=ctx.device)
@@ -337,8 +336,11 @@ class TextureBaker:
         return TextureBakeOutput(w, h, out(color), out(conf), out(src, True), out(valid), out(cov), out(faces, True),
                                  ray_bits is not None)
 
-    def _ray_visibility(self, pos: torch.Tensor, idx: torch.Tensor, apos, anrm, araster, cams, bias: float):
-        """project_ray_visibility.hlsl through a device BVH: camera-visibility bits [texels, ceil(views/32)]."""
+    def _ray_visibility(self, pos: torch.Tensor, idx: torch.Tensor, apos, anrm, araster, cams, bias: float,
+                        views: Optional[torch.Tensor] = None):
+        """project_ray_visibility.hlsl through a device BVH: camera-visibility bits [texels, ceil(views/32)].
+        With `views` (the projection's device table) only the texel-views the projection reads are traced;
+        the other bits are 0."""
         ctx = self.context
         V, T = pos.shape[0], idx.shape[0]
         bvh_bytes, build_bytes = C.c_size_t(), C.c_size_t()
@@ -349,10 +351,14 @@ class TextureBaker:
                      build_bytes.value, ctx.stream())
         del scratch
         n = cams.shape[0]
-        cam4 = torch.zeros((n, 4), dtype=torch.float32, device=ctx.device)
-        cam4[:, :3] = torch.from_numpy(np.ascontiguousarray(cams, dtype=np.float32)).to(ctx.device)
         N = araster.numel() // 4
         bits = torch.empty((N, (n + 31) // 32), dtype=torch.int32, device=ctx.device)
+        if views is not None:
+            _native.call("pdr_ray_visibility_views", _ptr(bvh), T, _ptr(apos), _ptr(anrm), _ptr(araster), N,
+                         _ptr(views), n, float(bias), _ptr(bits), ctx.stream())
+            return bits
+        cam4 = torch.zeros((n, 4), dtype=torch.float32, device=ctx.device)
+        cam4[:, :3] = torch.from_numpy(np.ascontiguousarray(cams, dtype=np.float32)).to(ctx.device)
         _native.call("pdr_ray_visibility", _ptr(bvh), T, _ptr(apos), _ptr(anrm), _ptr(araster), N, _ptr(cam4), n,
                      float(bias), _ptr(bits), ctx.stream())
         return bits

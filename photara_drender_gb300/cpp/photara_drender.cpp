@@ -418,6 +418,117 @@ TextureGradients Rasterizer::texture_backward(std::span<const float> texture, co
     return out;
 }
 
+// ---- atlas padding and surface fill (src/texture_padding.cpp:100-184,226-351) -----------------
+
+namespace {
+
+// A stream on the current device for the free padding functions, which take no Context.
+struct ScopedStream {
+    cudaStream_t s = nullptr;
+    ScopedStream() { check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate"); }
+    ~ScopedStream() {
+        if (s) cudaStreamDestroy(s);
+    }
+    ScopedStream(const ScopedStream&) = delete;
+    ScopedStream& operator=(const ScopedStream&) = delete;
+};
+
+std::uint32_t pad_status(const DeviceArray<std::uint32_t>& status, cudaStream_t s) {
+    return status.download(s)[PDR_STATUS_PAD_ERROR];
+}
+
+}  // namespace
+
+SurfaceFillStats fill_texture_on_surface(TextureBakeOutput& output, std::span<const std::uint32_t> triangle_indices) {
+    const std::size_t pixels = static_cast<std::size_t>(output.width) * output.height;
+    if (pixels == 0 || triangle_indices.empty() || triangle_indices.size() % 3 != 0 ||
+        output.face_ids.size() != pixels || output.valid_mask.size() != pixels || output.color.size() % pixels != 0)
+        throw std::invalid_argument("surface fill requires mesh face IDs and a valid atlas");
+    const std::size_t channels = output.color.size() / pixels;
+    if (channels != 3 && channels != 4) throw std::invalid_argument("surface fill requires RGB or RGBA colours");
+    const std::size_t faces = triangle_indices.size() / 3;
+    if (faces >= UINT32_MAX / 3) throw std::invalid_argument("surface fill has too many faces");
+    ScopedStream stream;
+    const cudaStream_t s = stream.s;
+    std::vector<float> filled = output.filled_mask.size() == pixels ? output.filled_mask
+                                                                   : std::vector<float>(pixels, 0.0F);
+    DeviceArray<float> d_color(output.color.data(), output.color.size(), s);
+    DeviceArray<float> d_valid(output.valid_mask.data(), pixels, s);
+    DeviceArray<std::uint32_t> d_faces(output.face_ids.data(), pixels, s);
+    DeviceArray<float> d_filled(filled.data(), pixels, s);
+    DeviceArray<std::uint32_t> d_idx(triangle_indices.data(), triangle_indices.size(), s);
+    std::size_t bytes = 0;
+    check(pdr_surface_fill_workspace_bytes(output.width, output.height, static_cast<std::uint32_t>(faces), &bytes));
+    DeviceArray<unsigned char> ws(bytes);
+    DeviceArray<std::uint64_t> d_stats(4);
+    DeviceArray<std::uint32_t> status(PDR_STATUS_WORDS);
+    status.zero(s);
+    check(pdr_fill_texture_on_surface(d_color.get(), static_cast<std::uint32_t>(channels), d_valid.get(),
+                                      d_faces.get(), d_filled.get(), output.width, output.height, d_idx.get(),
+                                      static_cast<std::uint32_t>(faces), ws.get(), bytes, d_stats.get(),
+                                      status.get(), s));
+    const std::uint32_t err = pad_status(status, s);
+    if (err & 2u) throw std::invalid_argument("atlas face ID is out of range");
+    if (err & 4u) throw std::invalid_argument("surface fill mesh has a degenerate edge");
+    if (err & 8u) throw std::invalid_argument("surface fill requires manifold edges");
+    const auto st = d_stats.download(s);
+    output.color = d_color.download(s);
+    output.filled_mask = d_filled.download(s);
+    SurfaceFillStats out;
+    out.filled_texels = st[0];
+    out.remaining_texels = st[1];
+    out.measured_faces = st[2];
+    out.propagated_faces = st[3];
+    return out;
+}
+
+TexturePaddingStats pad_texture_atlas(TextureBakeOutput& output, const TexturePaddingOptions& options) {
+    const auto start = std::chrono::steady_clock::now();
+    const std::uint32_t width = output.width, height = output.height;
+    if (width == 0 || height == 0) throw std::invalid_argument("cannot pad an empty atlas");
+    if (width > 16384 || height > 16384) throw std::invalid_argument("atlas dimensions exceed the supported maximum");
+    const std::size_t pixels = static_cast<std::size_t>(width) * height;
+    if (output.color.size() % pixels != 0)
+        throw std::invalid_argument("atlas color size does not match its dimensions");
+    const std::size_t channels = output.color.size() / pixels;
+    if (channels != 3 && channels != 4) throw std::invalid_argument("atlas color must have 3 or 4 channels");
+    if (output.valid_mask.size() != pixels)
+        throw std::invalid_argument("atlas valid_mask must match the atlas dimensions");
+    if (!std::isfinite(options.valid_threshold) || options.valid_threshold <= 0.0F || options.valid_threshold > 1.0F)
+        throw std::invalid_argument("valid_threshold must be within (0, 1]");
+    if (output.filled_mask.size() != pixels) output.filled_mask.assign(pixels, 0.0F);
+    const bool has_coverage = output.coverage_mask.size() == pixels;
+    ScopedStream stream;
+    const cudaStream_t s = stream.s;
+    DeviceArray<float> d_color(output.color.data(), output.color.size(), s);
+    DeviceArray<float> d_valid(output.valid_mask.data(), pixels, s);
+    DeviceArray<float> d_cov = has_coverage ? DeviceArray<float>(output.coverage_mask.data(), pixels, s)
+                                            : DeviceArray<float>();
+    DeviceArray<float> d_filled(output.filled_mask.data(), pixels, s);
+    std::size_t bytes = 0;
+    check(pdr_pad_workspace_bytes(width, height, static_cast<std::uint32_t>(channels), &bytes));
+    DeviceArray<unsigned char> ws(bytes);
+    DeviceArray<std::uint64_t> d_stats(5);
+    DeviceArray<std::uint32_t> status(PDR_STATUS_WORDS);
+    status.zero(s);
+    check(pdr_pad_texture_atlas(d_color.get(), static_cast<std::uint32_t>(channels), d_valid.get(),
+                                has_coverage ? d_cov.get() : nullptr, d_filled.get(), width, height, options.margin,
+                                options.fill_unobserved ? 1u : 0u, options.maximum_fill_distance,
+                                options.valid_threshold, ws.get(), bytes, d_stats.get(), status.get(), s));
+    if (pad_status(status, s) & 1u) throw std::runtime_error("atlas padding sweep did not complete");
+    const auto st = d_stats.download(s);
+    output.color = d_color.download(s);
+    output.filled_mask = d_filled.download(s);
+    TexturePaddingStats out;
+    out.valid_texels = st[0];
+    out.gutter_texels = st[1];
+    out.unobserved_texels = st[2];
+    out.remaining_unobserved = st[3];
+    out.filled_texels = st[4];
+    out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    return out;
+}
+
 // ---- softmax scale (src/texture_padding.cpp:187-224) ------------------------------------------
 
 float suggest_softmax_scale(std::span<const float> positions, std::span<const float> camera_positions) {
@@ -526,24 +637,7 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
         scale = suggest_softmax_scale(positions, cams);
         if (!(scale > 0.0F) || !std::isfinite(scale)) scale = 1.0F;
     }
-    // ray visibility bits (visibility modes 1 and 2): BVH of the world-space mesh, one ray per texel and view
     const std::uint32_t vis_mode = static_cast<std::uint32_t>(options.visibility_mode);
-    DeviceArray<std::uint32_t> ray_bits;
-    if (vis_mode != 0) {
-        std::size_t bvh_bytes = 0, build_bytes = 0;
-        check(pdr_bvh_sizes(T, &bvh_bytes, &build_bytes));
-        DeviceArray<unsigned char> bvh(bvh_bytes), scratch(build_bytes);
-        check(pdr_bvh_build(d_pos.get(), Vu, d_idx.get(), T, bvh.get(), bvh_bytes, scratch.get(), build_bytes, s));
-        std::vector<float> cams(views.size() * 4, 0.0F);
-        for (std::size_t i = 0; i < views.size(); ++i)
-            std::copy_n(views[i].camera_position.begin(), 3, cams.begin() + static_cast<std::ptrdiff_t>(i * 4));
-        DeviceArray<float> d_cams(cams.data(), cams.size(), s);
-        ray_bits = DeviceArray<std::uint32_t>(N * ((views.size() + 31) / 32));
-        check(pdr_ray_visibility(bvh.get(), T, d_apos.get(), d_anrm.get(), d_araster.get(),
-                                 static_cast<std::uint32_t>(N), d_cams.get(), static_cast<std::uint32_t>(views.size()),
-                                 options.ray_origin_bias, ray_bits.get(), s));
-        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    }
     // shadow rasters, one per view (not needed for ray-only visibility)
     std::vector<DeviceArray<float>> images, masks, shadows;
     std::vector<pdr_projection_view> table(views.size());
@@ -585,6 +679,22 @@ TextureBakeOutput TextureBaker::bake(std::span<const float> positions, std::span
     }
     DeviceArray<unsigned char> d_table(reinterpret_cast<const unsigned char*>(table.data()),
                                        table.size() * sizeof(pdr_projection_view), s);
+    // ray visibility bits (visibility modes 1 and 2): BVH of the world-space mesh, one ray per texel and
+    // view that the projection reads
+    DeviceArray<std::uint32_t> ray_bits;
+    if (vis_mode != 0) {
+        std::size_t bvh_bytes = 0, build_bytes = 0;
+        check(pdr_bvh_sizes(T, &bvh_bytes, &build_bytes));
+        DeviceArray<unsigned char> bvh(bvh_bytes), scratch(build_bytes);
+        check(pdr_bvh_build(d_pos.get(), Vu, d_idx.get(), T, bvh.get(), bvh_bytes, scratch.get(), build_bytes, s));
+        ray_bits = DeviceArray<std::uint32_t>(N * ((views.size() + 31) / 32));
+        check(pdr_ray_visibility_views(bvh.get(), T, d_apos.get(), d_anrm.get(), d_araster.get(),
+                                       static_cast<std::uint32_t>(N),
+                                       reinterpret_cast<const pdr_projection_view*>(d_table.get()),
+                                       static_cast<std::uint32_t>(views.size()), options.ray_origin_bias,
+                                       ray_bits.get(), s));
+        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
     DeviceArray<float> d_color(N * 4), d_conf(N), d_valid(N), d_cov(N);
     DeviceArray<std::uint32_t> d_src(N), d_faces(N);
     if (vis_mode == 0)

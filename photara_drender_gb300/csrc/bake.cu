@@ -12,6 +12,7 @@
 #include "../../include/pdr_capi.h"
 #include "pdr_common.cuh"
 #include "pdr_internal.h"
+#include "projection.cuh"
 
 namespace pdr {
 namespace {
@@ -94,26 +95,9 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
         const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
         for (uint32_t k = 0; k < nviews; ++k) {
             const pdr_projection_view& v = views[k];
-            const float* M = v.world_to_clip;
-            const float cw = M[12] * px + M[13] * py + M[14] * pz + M[15] * 1.0f;
-            if (cw <= 1e-8f) continue;
-            const float cx = M[0] * px + M[1] * py + M[2] * pz + M[3] * 1.0f;
-            const float cy = M[4] * px + M[5] * py + M[6] * pz + M[7] * 1.0f;
-            const float cz = M[8] * px + M[9] * py + M[10] * pz + M[11] * 1.0f;
-            const float ndx = cx / cw, ndy = cy / cw, ndz = cz / cw;
-            if (ndx < -1.0f || ndy < -1.0f || ndx > 1.0f || ndy > 1.0f || ndz < -1.0f || ndz > 1.0f) continue;
-            const float ppx = v.viewport[0] + (ndx * 0.5f + 0.5f) * v.viewport[2];
-            const float ppy = v.viewport[1] + (ndy * 0.5f + 0.5f) * v.viewport[3];
-            if (ppx < v.viewport[0] || ppy < v.viewport[1] || ppx >= v.viewport[0] + v.viewport[2] ||
-                ppy >= v.viewport[1] + v.viewport[3])
-                continue;
-            // view direction first: the facing test rejects half of all texel-views before the
-            // visibility work, with the same outcome as the reference's order
-            const float vx0 = v.camera_position[0] - px, vy0 = v.camera_position[1] - py;
-            const float vz0 = v.camera_position[2] - pz;
-            const float vl = sqrtf(vx0 * vx0 + vy0 * vy0 + vz0 * vz0);
-            const float cosv = nx * (vx0 / vl) + ny * (vy0 / vl) + nz * (vz0 / vl);
-            if (cosv < v.min_view_cosine) continue;
+            ProjectedTexel pt;
+            if (!project_texel(v, px, py, pz, nx, ny, nz, pt)) continue;
+            const float ppx = pt.ppx, ppy = pt.ppy, ndz = pt.ndz, vl = pt.vl, cosv = pt.cosv;
             // ray visibility: one bit per (texel, view) from the BVH ray caster, or a per-view array
             float vis = vis_bits ? (float)((__ldg(vis_bits + (size_t)i * vis_words + (k >> 5)) >> (k & 31u)) & 1u)
                                  : (v.ray_visibility ? __ldg(v.ray_visibility + i) : 1.0f);

@@ -22,6 +22,7 @@
 #include "../../include/pdr_capi.h"
 #include "pdr_common.cuh"
 #include "pdr_internal.h"
+#include "projection.cuh"
 
 namespace pdr {
 namespace {
@@ -267,16 +268,6 @@ __global__ void header_kernel(BvhHeader* h, uint32_t T) {
 
 // ---- traversal ----------------------------------------------------------------------------------
 
-__device__ __forceinline__ bool slab(float lox, float loy, float loz, float hix, float hiy, float hiz, float ox,
-                                     float oy, float oz, float ix, float iy, float iz, float t0, float t1) {
-    const float tx0 = (lox - ox) * ix, tx1 = (hix - ox) * ix;
-    const float ty0 = (loy - oy) * iy, ty1 = (hiy - oy) * iy;
-    const float tz0 = (loz - oz) * iz, tz1 = (hiz - oz) * iz;
-    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), t0));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), t1));
-    return tn <= tf;
-}
-
 // Moller-Trumbore: any hit with t in [t0, t1], either face.
 __device__ __forceinline__ bool hits_triangle(const float4* __restrict__ tri, float ox, float oy, float oz, float dx,
                                               float dy, float dz, float t0, float t1) {
@@ -299,20 +290,50 @@ __device__ __forceinline__ bool hits_triangle(const float4* __restrict__ tri, fl
 
 constexpr int kStack = 64;
 
-__device__ bool occluded(const BvhView& bvh, float ox, float oy, float oz, float dx, float dy, float dz, float t0,
-                         float t1) {
-    const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-    const int root = bvh.header->root;
-    if (root < 0) return hits_triangle(bvh.tris + (size_t)(~root) * 3, ox, oy, oz, dx, dy, dz, t0, t1);
+__device__ __forceinline__ bool load_texel(const float* __restrict__ apos, const float* __restrict__ anrm,
+                                           const float4* __restrict__ araster, uint32_t i, float& px, float& py,
+                                           float& pz, float& nx, float& ny, float& nz) {
+    if (raster_id(araster[i].w) == 0) return false;
+    px = apos[(size_t)i * 3];
+    py = apos[(size_t)i * 3 + 1];
+    pz = apos[(size_t)i * 3 + 2];
+    const float nx0 = anrm[(size_t)i * 3], ny0 = anrm[(size_t)i * 3 + 1], nz0 = anrm[(size_t)i * 3 + 2];
+    const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
+    nx = nx0 / nl;
+    ny = ny0 / nl;
+    nz = nz0 / nl;
+    return true;
+}
+
+// Slab test with each plane distance formed by one FMA: t = lo * (1/d) + (-o/d). Leaf boxes are padded
+// by 1e-6, more than the rounding difference to (lo - o) / d, so no box holding a hit is pruned.
+__device__ __forceinline__ bool slab_fma(float lox, float loy, float loz, float hix, float hiy, float hiz, float ix,
+                                         float iy, float iz, float bx, float by, float bz, float t0, float t1) {
+    const float tx0 = __fmaf_rn(lox, ix, bx), tx1 = __fmaf_rn(hix, ix, bx);
+    const float ty0 = __fmaf_rn(loy, iy, by), ty1 = __fmaf_rn(hiy, iy, by);
+    const float tz0 = __fmaf_rn(loz, iz, bz), tz1 = __fmaf_rn(hiz, iz, bz);
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), t0));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), t1));
+    return tn <= tf;
+}
+
+__device__ __forceinline__ float safe_inverse(float d) { return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d)); }
+
+// Any hit with t in [t0, t1] below the root (an inner node); complete traversal, so the answer does not
+// depend on the visiting order.
+__device__ bool occluded(const BvhView& bvh, int root, float ox, float oy, float oz, float dx, float dy, float dz,
+                         float t0, float t1) {
+    const float ix = safe_inverse(dx), iy = safe_inverse(dy), iz = safe_inverse(dz);
+    const float bx = -ox * ix, by = -oy * iy, bz = -oz * iz;
     int stack[kStack];
     int sp = 0;
     int node = root;
-    while (true) {
+    for (;;) {
         const BvhNode nd = bvh.nodes[node];
-        const bool hl = slab(nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y, ox, oy, oz, ix, iy, iz, t0, t1);
-        const bool hr = slab(nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w, ox, oy, oz, ix, iy, iz, t0, t1);
-        int next = -1;
+        const bool hl = slab_fma(nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y, ix, iy, iz, bx, by, bz, t0, t1);
+        const bool hr = slab_fma(nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w, ix, iy, iz, bx, by, bz, t0, t1);
         const int cl = nd.d.x, cr = nd.d.y;
+        int next = -1;
         if (hl) {
             if (cl < 0) {
                 if (hits_triangle(bvh.tris + (size_t)(~cl) * 3, ox, oy, oz, dx, dy, dz, t0, t1)) return true;
@@ -329,42 +350,68 @@ __device__ bool occluded(const BvhView& bvh, float ox, float oy, float oz, float
                 stack[sp++] = cr;
             }
         }
-        if (next >= 0) {
-            node = next;
-        } else {
-            if (sp == 0) return false;
-            node = stack[--sp];
-        }
+        if (next >= 0) node = next;
+        else if (sp > 0) node = stack[--sp];
+        else return false;
     }
 }
 
-// shaders/project_ray_visibility.hlsl:14-55 for texel i and view blockIdx.y; sets bit (view & 31)
-// of word i * words + view / 32 when the camera is visible.
-__global__ void ray_visibility_kernel(BvhView bvh, const float* __restrict__ apos, const float* __restrict__ anrm,
-                                      const float4* __restrict__ araster, uint32_t N,
-                                      const float4* __restrict__ cameras, float bias, uint32_t words,
-                                      uint32_t* __restrict__ bits) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t view = blockIdx.y;
-    if (i >= N) return;
-    if (raster_id(araster[i].w) == 0) return;
-    const float px = apos[(size_t)i * 3], py = apos[(size_t)i * 3 + 1], pz = apos[(size_t)i * 3 + 2];
-    const float nx0 = anrm[(size_t)i * 3], ny0 = anrm[(size_t)i * 3 + 1], nz0 = anrm[(size_t)i * 3 + 2];
-    const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
-    const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
-    const float4 cam = cameras[view];
-    const float vx = cam.x - px, vy = cam.y - py, vz = cam.z - pz;
+// project_ray_visibility.hlsl:35-54 for surface point p with unit normal n and one camera.
+__device__ __forceinline__ bool camera_visible(const BvhView& bvh, int root, float4 p, float4 n, float cx, float cy,
+                                               float cz, float bias) {
+    const float vx = cx - p.x, vy = cy - p.y, vz = cz - p.z;
     const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
-    bool visible = true;
-    if (!(dist <= bias * 2.0f)) {
-        const float dx = vx / dist, dy = vy / dist, dz = vz / dist;
-        const float sgn = (nx * dx + ny * dy + nz * dz) >= 0.0f ? 1.0f : -1.0f;
-        const float ox = px + nx * (bias * sgn), oy = py + ny * (bias * sgn), oz = pz + nz * (bias * sgn);
-        const float t0 = bias;
-        const float t1 = fmaxf(t0, dist - bias * 2.0f);
-        visible = !occluded(bvh, ox, oy, oz, dx, dy, dz, t0, t1);
+    if (dist <= bias * 2.0f) return true;
+    const float dx = vx / dist, dy = vy / dist, dz = vz / dist;
+    const float sgn = (n.x * dx + n.y * dy + n.z * dz) >= 0.0f ? 1.0f : -1.0f;
+    const float ox = p.x + n.x * (bias * sgn), oy = p.y + n.y * (bias * sgn), oz = p.z + n.z * (bias * sgn);
+    const float t0 = bias;
+    const float t1 = fmaxf(t0, dist - bias * 2.0f);
+    if (root < 0) return !hits_triangle(bvh.tris + (size_t)(~root) * 3, ox, oy, oz, dx, dy, dz, t0, t1);
+    return !occluded(bvh, root, ox, oy, oz, dx, dy, dz, t0, t1);
+}
+
+// shaders/project_ray_visibility.hlsl:14-55 for texel i and the 32 views of word blockIdx.y: bit
+// (view & 31) of word i * words + view / 32 is set when the camera is visible. One thread builds the
+// whole word in a register (no atomics; uncovered texels get 0, as the shader writes). kGated traces
+// only the texel-views the projection reads (project_texel passes); the others report 0. The lanes of
+// a warp are neighbouring texels tracing toward the same camera, so their node fetches coincide.
+template <bool kGated>
+__global__ void __launch_bounds__(128) trace_words_kernel(BvhView bvh, const float* __restrict__ apos,
+                                                          const float* __restrict__ anrm,
+                                                          const float4* __restrict__ araster, uint32_t N,
+                                                          const float4* __restrict__ cameras,
+                                                          const pdr_projection_view* __restrict__ views,
+                                                          uint32_t nviews, float bias, uint32_t words,
+                                                          uint32_t* __restrict__ bits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t w = blockIdx.y;
+    if (i >= N) return;
+    uint32_t word = 0;
+    float px, py, pz, nx, ny, nz;
+    if (load_texel(apos, anrm, araster, i, px, py, pz, nx, ny, nz)) {
+        const float4 p = make_float4(px, py, pz, 1.0f), n = make_float4(nx, ny, nz, 0.0f);
+        const int root = bvh.header->root;
+        const uint32_t end = min(nviews, (w + 1) * 32);
+        for (uint32_t k = w * 32; k < end; ++k) {
+            float cx, cy, cz;
+            if (kGated) {
+                const pdr_projection_view& v = views[k];
+                ProjectedTexel pt;
+                if (!project_texel(v, px, py, pz, nx, ny, nz, pt)) continue;
+                cx = v.camera_position[0];
+                cy = v.camera_position[1];
+                cz = v.camera_position[2];
+            } else {
+                const float4 c = cameras[k];
+                cx = c.x;
+                cy = c.y;
+                cz = c.z;
+            }
+            if (camera_visible(bvh, root, p, n, cx, cy, cz, bias)) word |= 1u << (k & 31u);
+        }
     }
-    if (visible) atomicOr(bits + (size_t)i * words + (view >> 5), 1u << (view & 31u));
+    bits[(size_t)i * words + w] = word;
 }
 
 }  // namespace
@@ -462,17 +509,32 @@ pdr_status pdr_ray_visibility(const void* bvh, uint32_t triangle_count, const fl
     if (view_count == 0 || view_count > 65535u) return set_error(PDR_INVALID_ARGUMENT, "view count must be 1..65535");
     if (!(ray_origin_bias > 0.0f) || !isfinite(ray_origin_bias))
         return set_error(PDR_INVALID_ARGUMENT, "ray_origin_bias must be positive and finite");
-    const uint32_t words = (view_count + 31) / 32;
-    const cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = cudaMemsetAsync(visibility, 0, (size_t)atlas_texels * words * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return set_cuda_error(e, "ray_visibility(memset)");
     if (atlas_texels == 0) return PDR_OK;
-    const dim3 grid((atlas_texels + 127) / 128, view_count);
-    ray_visibility_kernel<<<grid, 128, 0, s>>>(bvh_view(bvh, triangle_count), atlas_positions, atlas_normals,
-                                               reinterpret_cast<const float4*>(atlas_raster), atlas_texels,
-                                               reinterpret_cast<const float4*>(cameras), ray_origin_bias, words,
-                                               visibility);
+    const uint32_t words = (view_count + 31) / 32;
+    const dim3 grid((atlas_texels + 127) / 128, words);
+    trace_words_kernel<false><<<grid, 128, 0, (cudaStream_t)stream>>>(
+        bvh_view(bvh, triangle_count), atlas_positions, atlas_normals, reinterpret_cast<const float4*>(atlas_raster),
+        atlas_texels, reinterpret_cast<const float4*>(cameras), nullptr, view_count, ray_origin_bias, words,
+        visibility);
     return set_cuda_error(cudaGetLastError(), "ray_visibility");
+}
+
+pdr_status pdr_ray_visibility_views(const void* bvh, uint32_t triangle_count, const float* atlas_positions,
+                                    const float* atlas_normals, const float* atlas_raster, uint32_t atlas_texels,
+                                    const pdr_projection_view* views, uint32_t view_count, float ray_origin_bias,
+                                    uint32_t* visibility, void* stream) {
+    if (!bvh || !atlas_positions || !atlas_normals || !atlas_raster || !views || !visibility || triangle_count == 0)
+        return set_error(PDR_INVALID_ARGUMENT, "ray visibility needs the BVH, the atlas G-buffer and an output");
+    if (view_count == 0 || view_count > 65535u) return set_error(PDR_INVALID_ARGUMENT, "view count must be 1..65535");
+    if (!(ray_origin_bias > 0.0f) || !isfinite(ray_origin_bias))
+        return set_error(PDR_INVALID_ARGUMENT, "ray_origin_bias must be positive and finite");
+    if (atlas_texels == 0) return PDR_OK;
+    const uint32_t words = (view_count + 31) / 32;
+    const dim3 grid((atlas_texels + 127) / 128, words);
+    trace_words_kernel<true><<<grid, 128, 0, (cudaStream_t)stream>>>(
+        bvh_view(bvh, triangle_count), atlas_positions, atlas_normals, reinterpret_cast<const float4*>(atlas_raster),
+        atlas_texels, nullptr, views, view_count, ray_origin_bias, words, visibility);
+    return set_cuda_error(cudaGetLastError(), "ray_visibility_views");
 }
 
 pdr_status pdr_project_views_bits(const float* apos, const float* anrm, const float* araster, uint32_t N,

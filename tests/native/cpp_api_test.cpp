@@ -3,7 +3,8 @@
 // Part 1 checks the properties the reference's tests/native_tests.cpp checks through the same API:
 // output sizes, coverage, finite-difference agreement of the raster, uv and texture gradients,
 // viewport clipping, the single-triangle bake (colour, face ids), the near view winning a softmax
-// bake, and a refinement whose loss falls. It also checks the exception types of invalid calls.
+// bake, a refinement whose loss falls, and the padding / surface-fill regressions of
+// tests/native_tests.cpp and tests/texture_surface_fill_test.cpp. It also checks the exception types of invalid calls.
 //
 // Part 2 (when given an input directory) reads a mesh and gradients written by the pytest driver,
 // runs forward, backward, interpolate and texture through the C++ API and writes the raw outputs
@@ -318,6 +319,74 @@ void file_pass(const std::string& in, const std::string& out, pd::Rasterizer& r)
 
 }  // namespace
 
+// tests/native_tests.cpp:34-117 (padding) and tests/texture_surface_fill_test.cpp through the C++ API.
+void padding_checks() {
+    constexpr std::uint32_t n = 24;
+    const auto at = [](std::uint32_t x, std::uint32_t y) { return static_cast<std::size_t>(y) * n + x; };
+    pd::TextureBakeOutput out;
+    out.width = out.height = n;
+    out.color.assign(n * n * 4, 0.0F);
+    out.valid_mask.assign(n * n, 0.0F);
+    out.coverage_mask.assign(n * n, 0.0F);
+    const std::array<float, 4> src{0.25F, 0.5F, 0.75F, 1.0F};
+    for (std::uint32_t y = 2; y < 6; ++y)
+        for (std::uint32_t x = 2; x < 6; ++x) {
+            out.valid_mask[at(x, y)] = out.coverage_mask[at(x, y)] = 1.0F;
+            std::copy(src.begin(), src.end(), out.color.begin() + at(x, y) * 4);
+        }
+    for (std::uint32_t y = 10; y < 18; ++y)
+        for (std::uint32_t x = 10; x < 18; ++x) out.coverage_mask[at(x, y)] = 1.0F;
+    pd::TextureBakeOutput untouched = out;
+    pd::TexturePaddingOptions opt;
+    opt.margin = 3;
+    const auto st = pd::pad_texture_atlas(out, opt);
+    expect(st.valid_texels == 16 && st.unobserved_texels == 64 && st.remaining_unobserved == 0, "padding counts");
+    expect(st.gutter_texels > 0 && st.filled_texels == st.gutter_texels + st.unobserved_texels, "padding totals");
+    const auto is_src = [&](std::uint32_t x, std::uint32_t y) {
+        const float* p = out.color.data() + at(x, y) * 4;
+        return std::abs(p[0] - src[0]) < 1e-6F && std::abs(p[1] - src[1]) < 1e-6F &&
+               std::abs(p[2] - src[2]) < 1e-6F && p[3] == 1.0F;
+    };
+    expect(is_src(2, 6) && is_src(10, 10), "gutter and unobserved texels take the source colour");
+    expect(out.filled_mask[at(10, 10)] > 0.5F && out.filled_mask[at(2, 2)] < 0.5F, "filled_mask provenance");
+    expect(out.valid_mask[at(10, 10)] < 0.5F && out.color[at(2, 12) * 4] == 0.0F, "padding stays in bounds");
+    pd::TexturePaddingOptions off;
+    off.margin = 0;
+    off.fill_unobserved = false;
+    const auto none = pd::pad_texture_atlas(untouched, off);
+    expect(none.filled_texels == 0 && none.remaining_unobserved == 64, "disabled padding");
+    pd::TextureBakeOutput empty;
+    expect_throws<std::invalid_argument>([&] { (void)pd::pad_texture_atlas(empty); }, "padding an empty atlas");
+
+    pd::TextureBakeOutput atlas;
+    atlas.width = 7;
+    atlas.height = 1;
+    atlas.color.assign(7 * 4, 0.0F);
+    atlas.valid_mask = {1, 0, 1, 0, 0, 0, 0};
+    atlas.coverage_mask = {1, 1, 1, 1, 1, 0, 0};
+    atlas.face_ids = {0, 0, 2, 1, 3, UINT32_MAX, UINT32_MAX};
+    atlas.color[0] = 0.8F;
+    atlas.color[3] = 1.0F;
+    atlas.color[2 * 4 + 2] = 0.6F;
+    atlas.color[2 * 4 + 3] = 1.0F;
+    const std::uint32_t topology[] = {0, 1, 2, 2, 1, 3, 4, 5, 6, 7, 8, 9};
+    const auto fs = pd::fill_texture_on_surface(atlas, topology);
+    expect(fs.measured_faces == 2 && fs.propagated_faces == 1 && fs.filled_texels == 2 && fs.remaining_texels == 1,
+           "surface fill statistics");
+    expect(atlas.color[4] == 0.8F && atlas.color[3 * 4] == 0.8F && atlas.color[3 * 4 + 2] == 0.0F,
+           "surface fill crosses the mesh edge, not the UV island");
+    pd::TexturePaddingOptions guard;
+    guard.margin = 2;
+    guard.fill_unobserved = false;
+    const auto padded = pd::pad_texture_atlas(atlas, guard);
+    expect(padded.unobserved_texels == 2 && padded.remaining_unobserved == 1, "padding keeps surface fills");
+    expect(atlas.color[5 * 4] == 0.8F && atlas.color[4 * 4] == 0.0F && atlas.filled_mask[3] == 1.0F, "gutter colour");
+    auto bad = atlas;
+    bad.face_ids[1] = 100;
+    expect_throws<std::invalid_argument>([&] { (void)pd::fill_texture_on_surface(bad, topology); },
+                                         "a face id beyond the mesh");
+}
+
 int main(int argc, char** argv) {
     try {
         expect_throws<std::out_of_range>([] { pd::Context bad(pd::ContextOptions{4096, false}); },
@@ -329,6 +398,7 @@ int main(int argc, char** argv) {
         raster_checks(r);
         bake_checks(ctx);
         refine_checks(ctx);
+        padding_checks();
         if (argc == 3) file_pass(argv[1], argv[2], r);
         std::printf("cpp_api_test: %d checks passed\n", g_checks);
         return 0;
