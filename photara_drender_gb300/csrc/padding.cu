@@ -40,7 +40,8 @@ constexpr int32_t kFar = 12000;      // texture_padding.cpp:20: offset of texels
 constexpr int32_t kMaxSide = 16384;  // texture_padding.cpp:18: offsets are clamped to +-kMaxSide
 constexpr uint32_t kMarker = 0x80808080u;  // int16 halves -32640: never a stored offset
 constexpr uint32_t kNone = 0xFFFFFFFFu;
-constexpr int kRing = 8;             // sweep steps of prefetch
+constexpr int kRing = 4;             // sweep steps of prefetch
+constexpr int kLead = 8;             // columns a waiting band lets the previous band get ahead
 constexpr long long kWaitCycles = 1ll << 32;  // about two seconds at GB300 clocks
 constexpr int kStatThreads = 256;
 
@@ -141,34 +142,63 @@ __device__ uint32_t wait_boundary(const uint32_t* p, uint32_t* control) {
     }
 }
 
-// One 8SSEDT sweep (texture_padding.cpp:80-94). kBack = the reverse sweep, run in place on the forward
-// field. control: [0] forward ticket, [1] reverse ticket, [2] failure flag.
-template <bool kBack>
+// Field layout: band-major, [band][step][lane] with W + 62 steps per band, so each sweep step stores one
+// 128-byte line. Forward band b, lane r is row 32b + r and reaches column x at step x + 2r. The reverse
+// sweep mirrors it: its band b' takes the rows of forward band B = bands - 1 - b' bottom-up (lane r' is
+// row 32B + 31 - r') and its step t' is column W - 1 - (t' - 2r'), which the forward band stored at step
+// W + 61 - t' for every lane: one coalesced line per step again.
+__device__ __forceinline__ uint32_t field_index(uint32_t band, uint32_t steps, uint32_t t, uint32_t lane) {
+    return (band * steps + t) * 32u + lane;
+}
+
+// The reverse-sweep (final) offset of texel (x, y).
+__device__ __forceinline__ uint32_t final_index(uint32_t x, uint32_t y, uint32_t W, uint32_t bands) {
+    const uint32_t r = 31u - (y & 31u);
+    return field_index(bands - 1u - (y >> 5), W + 62u, (W - 1u - x) + 2u * r, r);
+}
+
+// One 8SSEDT sweep (texture_padding.cpp:80-94): the forward sweep writes `out` from the source bits, the
+// reverse sweep (kBack) reads the forward field `in` and writes the final field `out`. control: [0]
+// forward ticket, [1] reverse ticket, [2] failure flag.
+//
+// kExact keeps the reference's relaxations one by one, with their clamp of offsets to +-16384. Without
+// it (atlas sides <= 4384) no offset component can exceed +-16383 (a real source is closer than the atlas
+// side, an offset inherited from a texel without source is at most 12000 + side - 1), so no candidate is
+// ever clamped, and the sequential relaxations equal "the first of [own, left, up, up-left, up-right] with
+// the smallest squared length": everything but the left neighbour is reduced off the step's critical path.
+template <bool kBack, bool kExact>
 __global__ void __launch_bounds__(32) pad_sweep_kernel(const uint32_t* __restrict__ src_bits, uint32_t words_per_row,
-                                                       uint32_t* field, uint32_t* __restrict__ boundary,
-                                                       uint32_t* control, uint32_t* status, int32_t W, int32_t H) {
+                                                       const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                       uint32_t* __restrict__ boundary, uint32_t* control,
+                                                       uint32_t* status, int32_t W, int32_t H) {
     const int lane = threadIdx.x;
     uint32_t band = 0;
     if (lane == 0) band = atomicAdd(&control[kBack ? 1 : 0], 1u);
     band = __shfl_sync(0xFFFFFFFFu, band, 0);
-    const int32_t s = (int32_t)band * 32 + lane;  // row in sweep order
-    const bool row_ok = s < H;
-    const int32_t y = kBack ? H - 1 - s : s;
+    const uint32_t bands = ((uint32_t)H + 31u) / 32u;
+    const uint32_t steps = (uint32_t)W + 62u;
+    // this lane's row and whether the row processed before it (above / below) exists
+    const int32_t y = kBack ? (int32_t)((bands - 1u - band) * 32u + 31u) - lane : (int32_t)(band * 32u) + lane;
+    const bool row_ok = y < H;
+    const bool has_prev_row = kBack ? y + 1 < H : y >= 1;
     const int32_t dx = kBack ? -1 : 1, dy = kBack ? -1 : 1;
-    const uint64_t row_base = row_ok ? (uint64_t)y * (uint32_t)W : 0;
-    const uint32_t* prev_boundary = boundary + (uint64_t)(band ? band - 1 : 0) * (uint32_t)W;
-    uint32_t* my_boundary = boundary + (uint64_t)band * (uint32_t)W;
-    const bool publish = lane == 31 && (int32_t)(band + 1) * 32 < H;
-    const bool reads_boundary = lane == 0 && band > 0;
-    const int32_t steps = W + 62;
+    const uint32_t* prev_boundary = boundary + (size_t)(band ? band - 1 : 0) * (uint32_t)W;
+    uint32_t* my_boundary = boundary + (size_t)band * (uint32_t)W;
+    const bool publish = lane == 31 && band + 1 < bands;
+    // lane 0 reads the previous band's last row; in the reverse sweep's first band (a partial forward band)
+    // lane 0 may have no row, and then neither it nor its band has a row below
+    const bool reads_boundary = lane == 0 && band > 0 && row_ok;
+    const uint32_t yc = row_ok ? (uint32_t)y : 0u;
+    const uint32_t mirror = bands - 1u - band;
 
-    // initial value of this lane's texel at step t (fwd: source bit; reverse: the forward field)
+    // initial value of this lane's texel at step t (forward: source bit; reverse: the forward field)
     auto init_at = [&](int32_t t) -> uint32_t {
-        const int32_t i = t - 2 * lane;
-        if (!row_ok || i < 0 || i >= W) return 0u;
-        const int32_t x = kBack ? W - 1 - i : i;
-        if (kBack) return field[row_base + x];
-        const uint32_t w = src_bits[(uint64_t)y * words_per_row + ((uint32_t)x >> 5)];
+        if (kBack) {
+            const int32_t tf = min(max((int32_t)steps - 1 - t, 0), (int32_t)steps - 1);
+            return in[field_index(mirror, steps, (uint32_t)tf, 31u - lane)];
+        }
+        const int32_t x = min(max(t - 2 * lane, 0), W - 1);
+        const uint32_t w = src_bits[yc * words_per_row + ((uint32_t)x >> 5)];
         return ((w >> (x & 31)) & 1u) ? 0u : pack(kFar, kFar);
     };
     // lane 0: the previous band's last row at sweep index t + 1 (may still be the marker)
@@ -178,11 +208,13 @@ __global__ void __launch_bounds__(32) pad_sweep_kernel(const uint32_t* __restric
         return ld_relaxed(prev_boundary + j);
     };
 
-    uint32_t ring[kRing], bring[kRing];
+    // ring: this lane's initial values for the next kRing steps. cur / nxt: lane 0's boundary values
+    // (row above, sweep index t + 1) for this chunk and the next one, loaded a chunk ahead.
+    uint32_t ring[kRing], cur[kRing], nxt[kRing];
 #pragma unroll
     for (int k = 0; k < kRing; ++k) {
         ring[k] = init_at(k);
-        bring[k] = boundary_at(k);
+        nxt[k] = boundary_at(k);
     }
     int32_t mx = 0, my = 0;                       // this lane's value at the previous step (index i - 1)
     int32_t nrx = 0, nry = 0, rx = 0, ry = 0, prx = 0, pry = 0;  // row above at i + 1, i, i - 1
@@ -194,21 +226,45 @@ __global__ void __launch_bounds__(32) pad_sweep_kernel(const uint32_t* __restric
         nrx = unpack_x(v);
         nry = unpack_y(v);
     }
-    for (int32_t t0 = 0; t0 < steps; t0 += kRing) {
+    for (int32_t t0 = 0; t0 < (int32_t)steps; t0 += kRing) {
+        if (reads_boundary) {
+            bool ready = true;
+#pragma unroll
+            for (int k = 0; k < kRing; ++k) {
+                cur[k] = nxt[k];
+                ready &= t0 + k + 1 >= W || cur[k] != kMarker;
+            }
+            if (!ready && !failed) {
+                // The previous band has not reached this chunk: wait until it is kLead columns further
+                // on, so the chunks after this one find their values written, then reload this chunk.
+                // Stores of another SM may become visible out of order, so every value is re-checked.
+                const int32_t far = min(t0 + kRing + kLead, W - 1);
+                failed = wait_boundary(prev_boundary + far, control) == kMarker;
+#pragma unroll
+                for (int k = 0; k < kRing; ++k) {
+                    const int32_t j = t0 + k + 1;
+                    if (j < W) cur[k] = ld_relaxed(prev_boundary + j);
+                }
+#pragma unroll
+                for (int k = 0; k < kRing; ++k) {
+                    const int32_t j = t0 + k + 1;
+                    if (j < W && cur[k] == kMarker && !failed) {
+                        cur[k] = wait_boundary(prev_boundary + j, control);
+                        failed |= cur[k] == kMarker;
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kRing; ++k) nxt[k] = boundary_at(t0 + kRing + k);
+        }
 #pragma unroll
         for (int k = 0; k < kRing; ++k) {
             const int32_t t = t0 + k;
             int32_t ux = __shfl_up_sync(0xFFFFFFFFu, mx, 1);
             int32_t uy = __shfl_up_sync(0xFFFFFFFFu, my, 1);
             if (reads_boundary) {
-                uint32_t v = bring[k];
-                if (t + 1 < W && v == kMarker && !failed) {
-                    v = wait_boundary(prev_boundary + t + 1, control);
-                    failed = v == kMarker;
-                }
-                ux = unpack_x(v);
-                uy = unpack_y(v);
-                bring[k] = boundary_at(t + kRing);
+                ux = unpack_x(cur[k]);
+                uy = unpack_y(cur[k]);
             }
             prx = rx; pry = ry;
             rx = nrx; ry = nry;
@@ -216,21 +272,47 @@ __global__ void __launch_bounds__(32) pad_sweep_kernel(const uint32_t* __restric
             const uint32_t init = ring[k];
             ring[k] = init_at(t + kRing);
             const int32_t i = t - 2 * lane;
-            if (row_ok && i >= 0 && i < W) {
-                int32_t hx = unpack_x(init), hy = unpack_y(init);
-                int32_t hk = hx * hx + hy * hy;
-                if (i >= 1) relax(hx, hy, hk, mx - dx, my);
-                if (s >= 1) {
-                    relax(hx, hy, hk, rx, ry - dy);
-                    if (i >= 1) relax(hx, hy, hk, prx - dx, pry - dy);
-                    if (i + 1 < W) relax(hx, hy, hk, nrx + dx, nry - dy);
+            const bool active = row_ok && i >= 0 && i < W;
+            const bool up = has_prev_row, left = i >= 1, right = i + 1 < W;
+            const int32_t ix = unpack_x(init), iy = unpack_y(init);
+            const int32_t lcx = mx - dx, lcy = my;                     // left (previous texel of the row)
+            const int32_t rcx = rx, rcy = ry - dy;                     // up
+            const int32_t pcx = prx - dx, pcy = pry - dy;              // up-left
+            const int32_t ncx = nrx + dx, ncy = nry - dy;              // up-right
+            int32_t hx, hy;
+            if (kExact) {
+                hx = ix;
+                hy = iy;
+                int32_t hk = ix * ix + iy * iy;
+                if (left) relax(hx, hy, hk, lcx, lcy);
+                if (up) {
+                    relax(hx, hy, hk, rcx, rcy);
+                    if (left) relax(hx, hy, hk, pcx, pcy);
+                    if (right) relax(hx, hy, hk, ncx, ncy);
                 }
-                mx = hx;
-                my = hy;
-                const uint32_t packed = pack(hx, hy);
-                field[row_base + (kBack ? W - 1 - i : i)] = packed;
-                if (publish) st_relaxed(my_boundary + i, packed);
+            } else {
+                constexpr int32_t kInf = 0x7FFFFFFF;
+                const int32_t ki = ix * ix + iy * iy;
+                const int32_t kr = up ? rcx * rcx + rcy * rcy : kInf;
+                const int32_t kp = up && left ? pcx * pcx + pcy * pcy : kInf;
+                const int32_t kn = up && right ? ncx * ncx + ncy * ncy : kInf;
+                // first minimum of the up candidates, then of [own, that]: own wins ties
+                int32_t ax = rcx, ay = rcy, ka = kr;
+                if (kp < ka) { ax = pcx; ay = pcy; ka = kp; }
+                if (kn < ka) { ax = ncx; ay = ncy; ka = kn; }
+                const bool own = ki <= ka;
+                const int32_t bx = own ? ix : ax, by = own ? iy : ay;
+                // the left candidate comes after own (must be strictly shorter) and before the up ones
+                const int32_t thr = own ? ki : ka + 1;
+                const int32_t kl = left ? lcx * lcx + lcy * lcy : kInf;
+                hx = kl < thr ? lcx : bx;
+                hy = kl < thr ? lcy : by;
             }
+            mx = active ? hx : mx;
+            my = active ? hy : my;
+            const uint32_t packed = pack(hx, hy);
+            if (active) out[field_index(band, steps, (uint32_t)t, (uint32_t)lane)] = packed;
+            if (active && publish) st_relaxed(my_boundary + i, packed);
         }
         if (__any_sync(0xFFFFFFFFu, failed)) {
             if (lane == 0) atomicOr(status + PDR_STATUS_PAD_ERROR, kErrTimeout);
@@ -245,8 +327,8 @@ struct FillParams {
     const float* coverage;
     float* filled;
     const uint32_t* src_bits;
-    const uint32_t* field;
-    uint32_t channels, words_per_row, margin, fill_unobserved;
+    const uint32_t* field;  // final offsets, band-major (final_index)
+    uint32_t channels, words_per_row, margin, fill_unobserved, bands;
     int32_t W, H;
     unsigned long long margin2, limit2;
 };
@@ -259,7 +341,7 @@ __device__ __forceinline__ bool is_source(const FillParams& P, uint32_t x, uint3
 __device__ __forceinline__ int fill_decision(const FillParams& P, uint32_t x, uint32_t y, uint64_t& src,
                                              bool& covered) {
     const uint64_t p = (uint64_t)y * (uint32_t)P.W + x;
-    const uint32_t f = P.field[p];
+    const uint32_t f = P.field[final_index(x, y, (uint32_t)P.W, P.bands)];
     const int32_t ox = unpack_x(f), oy = unpack_y(f);
     const int32_t d2 = ox * ox + oy * oy;
     if (d2 >= 2 * kFar * kFar) return 0;
@@ -532,7 +614,7 @@ uint32_t stat_blocks(uint64_t work) {
 }
 
 struct PadLayout {
-    size_t control, counters, bits, field, boundary, snapshot, total;
+    size_t control, counters, bits, field, field2, boundary, snapshot, total;
 };
 
 PadLayout pad_layout(uint32_t W, uint32_t H, uint32_t C) {
@@ -545,8 +627,11 @@ PadLayout pad_layout(uint32_t W, uint32_t H, uint32_t C) {
     o += align_up(4 * sizeof(unsigned long long));
     L.bits = o;
     o += align_up(words * sizeof(uint32_t));
+    const size_t field_words = bands * ((size_t)W + 62) * 32;
     L.field = o;
-    o += align_up((size_t)W * H * sizeof(uint32_t));
+    o += align_up(field_words * sizeof(uint32_t));
+    L.field2 = o;
+    o += align_up(field_words * sizeof(uint32_t));
     L.boundary = o;
     o += align_up(2 * bands * W * sizeof(uint32_t));
     L.snapshot = o;
@@ -653,10 +738,18 @@ pdr_status pdr_pad_texture_atlas(float* color, uint32_t channels, const float* v
     const uint64_t words = (uint64_t)wpr * height;
     pad_classify_kernel<<<stat_blocks(words * 32), kStatThreads, 0, s>>>(valid_mask, coverage_mask, filled_mask, bits,
                                                                          wpr, width, height, valid_threshold, st64);
-    pad_sweep_kernel<false><<<bands, 32, 0, s>>>(bits, wpr, field, boundary, control, status, (int32_t)width,
-                                                 (int32_t)height);
-    pad_sweep_kernel<true><<<bands, 32, 0, s>>>(bits, wpr, field, boundary + (size_t)bands * width, control, status,
-                                                (int32_t)width, (int32_t)height);
+    uint32_t* field2 = reinterpret_cast<uint32_t*>(ws + L.field2);
+    if (width > 4384 || height > 4384) {
+        pad_sweep_kernel<false, true><<<bands, 32, 0, s>>>(bits, wpr, nullptr, field, boundary, control, status,
+                                                           (int32_t)width, (int32_t)height);
+        pad_sweep_kernel<true, true><<<bands, 32, 0, s>>>(bits, wpr, field, field2, boundary + (size_t)bands * width,
+                                                          control, status, (int32_t)width, (int32_t)height);
+    } else {
+        pad_sweep_kernel<false, false><<<bands, 32, 0, s>>>(bits, wpr, nullptr, field, boundary, control, status,
+                                                            (int32_t)width, (int32_t)height);
+        pad_sweep_kernel<true, false><<<bands, 32, 0, s>>>(bits, wpr, field, field2, boundary + (size_t)bands * width,
+                                                           control, status, (int32_t)width, (int32_t)height);
+    }
     if (snapshot) {
         e = cudaMemcpyAsync(ws + L.snapshot, color, (size_t)width * height * channels * sizeof(float),
                             cudaMemcpyDeviceToDevice, s);
@@ -668,7 +761,8 @@ pdr_status pdr_pad_texture_atlas(float* color, uint32_t channels, const float* v
     P.coverage = coverage_mask;
     P.filled = filled_mask;
     P.src_bits = bits;
-    P.field = field;
+    P.field = field2;
+    P.bands = bands;
     P.channels = channels;
     P.words_per_row = wpr;
     P.margin = margin;
