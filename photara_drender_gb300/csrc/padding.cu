@@ -42,6 +42,7 @@ constexpr uint32_t kMarker = 0x80808080u;  // int16 halves -32640: never a store
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kRing = 4;             // sweep steps of prefetch
 constexpr int kLead = 8;             // columns a waiting band lets the previous band get ahead
+constexpr int kL2Ahead = 64;         // steps the reverse sweep prefetches the forward field into L2
 constexpr long long kWaitCycles = 1ll << 32;  // about two seconds at GB300 clocks
 constexpr int kStatThreads = 256;
 
@@ -271,6 +272,12 @@ __global__ void __launch_bounds__(32) pad_sweep_kernel(const uint32_t* __restric
             nrx = ux; nry = uy;
             const uint32_t init = ring[k];
             ring[k] = init_at(t + kRing);
+            if (kBack && lane == 0 && t + kL2Ahead < (int32_t)steps) {
+                // the forward field line kL2Ahead steps ahead (all 32 lanes' values of that step): into L2
+                // now, so the ring's load a few steps before its use finds it there instead of in DRAM
+                const uint32_t* line = in + field_index(mirror, steps, steps - 1u - (uint32_t)(t + kL2Ahead), 0u);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(line));
+            }
             const int32_t i = t - 2 * lane;
             const bool active = row_ok && i >= 0 && i < W;
             const bool up = has_prev_row, left = i >= 1, right = i + 1 < W;
