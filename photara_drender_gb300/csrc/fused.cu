@@ -107,6 +107,10 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
         return set_error(PDR_INVALID_ARGUMENT, "attribute gradients need grad_interpolated and grad_attributes");
     if (a->texture && (!a->uv || !a->grad_sampled || !a->grad_texture || !a->grad_uv_attributes || !a->uv_attributes))
         return set_error(PDR_INVALID_ARGUMENT, "texture gradients need uv, grad_sampled and gradient outputs");
+    // the adjoint adds vertex gradients with vector reductions: clip gradients as float4, uv as float2
+    if (((uintptr_t)a->grad_clip_positions & 15u) || ((uintptr_t)a->grad_uv_attributes & 7u) ||
+        ((uintptr_t)a->grad_texture & 15u))
+        return set_error(PDR_INVALID_ARGUMENT, "gradient outputs must be 16-byte (clip, texture) / 8-byte (uv) aligned");
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t err = cudaMemsetAsync(a->grad_clip_positions, 0, (size_t)a->views * a->vertex_count * 4 * sizeof(float), s);
     if (err == cudaSuccess && a->grad_attributes)
