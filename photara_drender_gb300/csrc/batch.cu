@@ -251,9 +251,9 @@ pdr_status plan_batch(const pdr_render_mesh* meshes, uint32_t n, const pdr_batch
                 return set_error(PDR_INVALID_ARGUMENT, "batch backward needs the gradient buffers of every mesh");
             // vertex gradients are added with vector reductions: clip as float4, uv as float2
             if (((uintptr_t)M.grad_clip_positions & 15u) || ((uintptr_t)M.grad_uv_attributes & 7u) ||
-                ((uintptr_t)M.grad_texture & 15u))
+                ((uintptr_t)M.grad_texture & 15u) || ((uintptr_t)M.grad_attributes & 15u))
                 return set_error(PDR_INVALID_ARGUMENT,
-                                 "gradient outputs must be 16-byte (clip, texture) / 8-byte (uv) aligned");
+                                 "gradient outputs must be 16-byte (clip, texture, attributes) / 8-byte (uv) aligned");
         }
         const size_t P = (size_t)M.width * M.height;
         const uint32_t tcx = (M.width + cfg->tile_width - 1) / cfg->tile_width;

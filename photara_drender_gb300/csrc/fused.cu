@@ -21,7 +21,7 @@ namespace pdr {
 namespace {
 
 template <int kA>
-__global__ void __launch_bounds__(kFusedThreads, 4)
+__global__ void __launch_bounds__(kFusedThreads, 5)
 render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
                        const float* __restrict__ attrs, const float2* __restrict__ uv_attrs,
@@ -109,8 +109,8 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
         return set_error(PDR_INVALID_ARGUMENT, "texture gradients need uv, grad_sampled and gradient outputs");
     // the adjoint adds vertex gradients with vector reductions: clip gradients as float4, uv as float2
     if (((uintptr_t)a->grad_clip_positions & 15u) || ((uintptr_t)a->grad_uv_attributes & 7u) ||
-        ((uintptr_t)a->grad_texture & 15u))
-        return set_error(PDR_INVALID_ARGUMENT, "gradient outputs must be 16-byte (clip, texture) / 8-byte (uv) aligned");
+        ((uintptr_t)a->grad_texture & 15u) || ((uintptr_t)a->grad_attributes & 15u))
+        return set_error(PDR_INVALID_ARGUMENT, "gradient outputs must be 16-byte (clip, texture, attributes) / 8-byte (uv) aligned");
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t err = cudaMemsetAsync(a->grad_clip_positions, 0, (size_t)a->views * a->vertex_count * 4 * sizeof(float), s);
     if (err == cudaSuccess && a->grad_attributes)

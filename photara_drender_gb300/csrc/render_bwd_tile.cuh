@@ -294,8 +294,18 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
             const uint32_t v = corners[k];
             if (v >= V) continue;
             if (g_uv) red_v2(g_uv + (size_t)v * 2, cv[k][0], cv[k][1]);
+            float* ga = g_attr + (size_t)v * kA;
+            if (kA % 4 == 0) {  // rows of 4k floats: 16-byte aligned
 #pragma unroll
-            for (int a = 0; a < kA; ++a) atomicAdd(g_attr + (size_t)v * kA + a, cv[k][2 + a]);
+                for (int a = 0; a < kA; a += 4)
+                    red_v4(ga + a, make_float4(cv[k][2 + a], cv[k][3 + a], cv[k][4 + a], cv[k][5 + a]));
+            } else if (kA % 2 == 0) {
+#pragma unroll
+                for (int a = 0; a < kA; a += 2) red_v2(ga + a, cv[k][2 + a], cv[k][3 + a]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < kA; ++a) atomicAdd(ga + a, cv[k][2 + a]);
+            }
             // z of the clip gradient stays 0 (rasterize_backward.hlsl writes no depth gradient)
             red_v4(g_clip + (size_t)v * 4, make_float4(cv[k][2 + kA], cv[k][3 + kA], 0.0f, cv[k][4 + kA]));
         }
