@@ -720,10 +720,8 @@ def run_gpu(args, world, rank, local):
     stage_ms = np.zeros(len(STAGES))
     a = pipe._args(clip, t_attrs, t_uv, tex, g_attr, g_samp)
     timed = [
-        lambda: _native.check(L.pdr_bin_tiles(_ptr(clip), views, V, _ptr(pipe.idx), T, W, H, _ptr(pipe.vps),
-                                              _ptr(pipe.offsets), _ptr(pipe.list), pipe.capacity, _ptr(pipe.ws),
-                                              pipe.ws_bytes, _ptr(pipe.status), stream)),
-        lambda: _native.check(L.pdr_render_forward(C.addressof(a), stream)),
+        lambda: _native.check(L.pdr_render_bin(C.addressof(a), stream)),
+        lambda: _native.check(L.pdr_render_raster(C.addressof(a), stream)),
         lambda: _native.check(L.pdr_render_backward(C.addressof(a), stream)),
     ]
     for _ in range(reps):
@@ -736,7 +734,6 @@ def run_gpu(args, world, rank, local):
             torch.cuda.synchronize(dev)
             stage_ms[i] += e0.elapsed_time(e1)
     stage_ms /= reps
-    stage_ms[1] = max(stage_ms[1] - stage_ms[0], 1e-6)  # render_forward includes the binning
     hbm, peak_kind = load_peaks()
     sbytes = stage_bytes(w, T, V, entries)
     dom = int(np.argmax(stage_ms))

@@ -284,6 +284,11 @@ PDR_API size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_coun
  * texture_forward, bit-identical to the separate calls. The raster does not depend on the order of
  * a tile's triangles, so tile_triangles holds each tile's triangles unsorted (pdr_bin_tiles sorts). */
 PDR_API pdr_status pdr_render_forward(const pdr_render_args* args, void* stream);
+/* pdr_render_forward in two parts: the tile binning alone (tile_offsets, tile_triangles, status), and the
+ * raster launch with its epilogue over bins already made. A caller whose clip positions do not change
+ * between calls (texture or attribute optimisation) bins once and rasterizes many times. */
+PDR_API pdr_status pdr_render_bin(const pdr_render_args* args, void* stream);
+PDR_API pdr_status pdr_render_raster(const pdr_render_args* args, void* stream);
 /* The adjoints of the forward in one pixel pass: texture_backward, interpolate_backward for both
  * attribute sets (raster gradients summed) and rasterize_backward. */
 PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream);

@@ -55,6 +55,8 @@ _SIGNATURES = {
                                     _vp]),
     "pdr_render_workspace_bytes": (_sz, [_u32, _u32, _u32, _u32, _u64]),
     "pdr_render_forward": (_i32, [_vp, _vp]),
+    "pdr_render_bin": (_i32, [_vp, _vp]),
+    "pdr_render_raster": (_i32, [_vp, _vp]),
     "pdr_render_backward": (_i32, [_vp, _vp]),
     "pdr_transform_positions": (_i32, [_vp, _u32, _vp, _u32, _vp, _vp]),
     "pdr_atlas_clip_positions": (_i32, [_vp, _u32, _vp, _vp]),

@@ -72,7 +72,9 @@ size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint3
     return bins_workspace_bytes(views, triangle_count, width, height, capacity);
 }
 
-pdr_status pdr_render_forward(const pdr_render_args* a, void* stream) {
+namespace {
+
+pdr_status check_render_forward(const pdr_render_args* a) {
     if (!a || !a->clip_positions || !a->indices || !a->viewports || !a->raster || !a->tile_offsets ||
         !a->tile_triangles || !a->workspace || !a->status)
         return set_error(PDR_INVALID_ARGUMENT, "render arguments are incomplete");
@@ -85,18 +87,36 @@ pdr_status pdr_render_forward(const pdr_render_args* a, void* stream) {
         return set_error(PDR_INVALID_ARGUMENT, "texture sampling needs uv attributes and uv/sampled outputs");
     if (a->workspace_bytes < bins_workspace_bytes(a->views, a->triangle_count, a->width, a->height, a->capacity))
         return set_error(PDR_INVALID_ARGUMENT, "workspace is smaller than pdr_render_workspace_bytes()");
-    cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t err = launch_bin_tiles(a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count,
-                                       a->width, a->height, a->viewports, a->tile_offsets, a->tile_triangles,
-                                       a->capacity, a->workspace, a->status, s, /*sorted=*/false);
-    if (err != cudaSuccess) return set_cuda_error(err, "render_forward(bins)");
+    return PDR_OK;
+}
+
+}  // namespace
+
+pdr_status pdr_render_bin(const pdr_render_args* a, void* stream) {
+    const pdr_status st = check_render_forward(a);
+    if (st) return st;
+    const cudaError_t err = launch_bin_tiles(a->clip_positions, a->views, a->vertex_count, a->indices,
+                                             a->triangle_count, a->width, a->height, a->viewports, a->tile_offsets,
+                                             a->tile_triangles, a->capacity, a->workspace, a->status,
+                                             (cudaStream_t)stream, /*sorted=*/false);
+    return set_cuda_error(err, "render_bin");
+}
+
+pdr_status pdr_render_raster(const pdr_render_args* a, void* stream) {
+    const pdr_status st = check_render_forward(a);
+    if (st) return st;
     RasterShade shade{a->attributes, a->attribute_count, a->interpolated, a->uv_attributes, a->uv, a->texture,
                       a->texture_width, a->texture_height, a->address_mode, a->sampled};
-    err = launch_raster_forward(a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count, a->width,
-                                a->height, a->viewports, a->cull_mode, a->tile_offsets, a->tile_triangles, a->capacity,
-                                a->raster, a->barycentric_derivatives, s,
-                                (a->attributes || a->uv_attributes) ? &shade : nullptr);
-    return set_cuda_error(err, "render_forward");
+    const cudaError_t err = launch_raster_forward(
+        a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count, a->width, a->height,
+        a->viewports, a->cull_mode, a->tile_offsets, a->tile_triangles, a->capacity, a->raster,
+        a->barycentric_derivatives, (cudaStream_t)stream, (a->attributes || a->uv_attributes) ? &shade : nullptr);
+    return set_cuda_error(err, "render_raster");
+}
+
+pdr_status pdr_render_forward(const pdr_render_args* a, void* stream) {
+    const pdr_status st = pdr_render_bin(a, stream);
+    return st ? st : pdr_render_raster(a, stream);
 }
 
 pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {

@@ -80,3 +80,44 @@ def test_fused_matches_separate_kernels_and_oracle(mode):
                          ("grad_uv_attr", "gu32", "gu64", "guabs")):
         grad_check(f[key], o[a], o[b], o[c], name=f"fused {key}")
         grad_check(s[key], o[a], o[b], o[c], name=f"separate {key}")
+
+
+def test_bin_once_raster_many():
+    """pdr_render_bin + pdr_render_raster equal pdr_render_forward, and bins made once serve later rasters
+    with other attributes and textures (the geometry is unchanged)."""
+    from photara_drender_gb300 import Rasterizer, _native
+    from photara_drender_gb300.pipeline import RenderFwdBwd
+
+    rng = np.random.default_rng(3)
+    pos3, idx = S.icosphere(3)
+    mats, _ = S.orbit_cameras(2)
+    clip = S.clip_positions(pos3, mats)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    uva = t(S.spherical_uv(pos3).astype(np.float32))
+    H, W = 72, 88
+    V = pos3.shape[0]
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    L = _native.lib()
+    outs = []
+    p = RenderFwdBwd(Rasterizer(0), torch.tensor(idx.astype(np.int32)), V, 2, H, W, 3, (32, 40, 4))
+    tclip = t(clip)
+    for k in range(3):
+        attrs = t(rng.uniform(size=(V, 3)).astype(np.float32))
+        tex = t(rng.uniform(size=(32, 40, 4)).astype(np.float32))
+        a = p._args(tclip, attrs, uva, tex, None, None)  # the tensors above stay referenced while a is used
+        if k == 0:
+            _native.check(L.pdr_render_forward(C.addressof(a), stream))
+        else:
+            if k == 1:
+                _native.check(L.pdr_render_bin(C.addressof(a), stream))
+            _native.check(L.pdr_render_raster(C.addressof(a), stream))
+        torch.cuda.synchronize()
+        got = {n: getattr(p, n).cpu().numpy().copy() for n in ("raster", "attr_out", "sampled")}
+        _native.check(L.pdr_render_forward(C.addressof(a), stream))
+        torch.cuda.synchronize()
+        want = {n: getattr(p, n).cpu().numpy() for n in ("raster", "attr_out", "sampled")}
+        for n in got:
+            assert same_bits(got[n], want[n]), (k, n)
+        outs.append(want["sampled"])
+    assert not np.array_equal(outs[1], outs[2])
