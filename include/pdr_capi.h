@@ -94,6 +94,16 @@ PDR_API pdr_status pdr_rasterize_backward(const float* clip_positions, uint32_t 
                                           const uint32_t* indices, uint32_t triangle_count, uint32_t width,
                                           uint32_t height, const float* viewports, const float* raster,
                                           const float* grad_raster, float* grad_clip_positions, void* stream);
+/* pdr_rasterize_backward plus the gradient through the barycentric pixel derivatives
+ * (grad_barycentric_derivatives [views][H][W][4], d/d of [du/dx, du/dy, dv/dx, dv/dy]), which the
+ * reference rejects (src/rasterizer.cpp:459-462). Either gradient may be NULL (then it is zero). */
+PDR_API pdr_status pdr_rasterize_backward_derivatives(const float* clip_positions, uint32_t views,
+                                                      uint32_t vertex_count, const uint32_t* indices,
+                                                      uint32_t triangle_count, uint32_t width, uint32_t height,
+                                                      const float* viewports, const float* raster,
+                                                      const float* grad_raster,
+                                                      const float* grad_barycentric_derivatives,
+                                                      float* grad_clip_positions, void* stream);
 
 /* Rasterizer::interpolate_forward (src/rasterizer.cpp:539-601 + shaders/interpolate_forward.hlsl).
  * attribute_view_stride = 0 shares one [V][A] table across views, else floats between views. */

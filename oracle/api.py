@@ -457,3 +457,121 @@ def fill_texture_on_surface(color, valid_mask, face_ids, indices, *, filled_mask
     if rc < 0:
         raise ValueError(FILL_REASONS.get(reason.value, "invalid surface fill input"))
     return col, filled, tuple(int(s) for s in stats)
+
+
+# ---- gradient through the barycentric pixel derivatives (no reference counterpart) ----------------------
+
+def _deriv_setup(clip, idx, raster, viewport, dtype=np.float64):
+    """Per covered pixel: vertex ids and sample position (rasterize_forward.hlsl's pixel centre), in
+    float64, or in float32 with the kernels' sample_ndc order of operations."""
+    idx = np.asarray(idx, np.int64).reshape(-1, 3)
+    h, w = raster.shape[:2]
+    ids = np.rint(raster[..., 3]).astype(np.int64).reshape(-1)
+    pix = np.flatnonzero((ids > 0) & (ids <= idx.shape[0]))
+    tri = idx[ids[pix] - 1]
+    vp = np.asarray(_vp(viewport, w, h), dtype)
+    x, y = (pix % w).astype(dtype), (pix // w).astype(dtype)
+    one, half, two = dtype(1.0), dtype(0.5), dtype(2.0)
+    sx = ((x - vp[0] + half) * two / vp[2] - one).astype(dtype)
+    sy = ((y - vp[1] + half) * two / vp[3] - one).astype(dtype)
+    return np.asarray(clip, dtype), tri, pix, sx, sy, vp
+
+
+def barycentric_derivatives_f64(clip, idx, raster, viewport=None):
+    """The derivative output of rasterize_forward.hlsl in float64 for the triangles `raster` assigns to
+    its pixels, as a function of the clip positions: [H, W, 4] (zeros where uncovered)."""
+    clip, tri, pix, sx, sy, vp = _deriv_setup(clip, idx, raster, viewport)
+    p0, p1, p2 = (clip[tri[:, k]] for k in range(3))
+    q = [(p[:, 0] - sx * p[:, 3], p[:, 1] - sy * p[:, 3]) for p in (p0, p1, p2)]
+    cr = lambda a, b: a[0] * b[1] - a[1] * b[0]  # noqa: E731
+    a0, a1, a2 = cr(q[1], q[2]), cr(q[2], q[0]), cr(q[0], q[1])
+    binv = 1.0 / (a0 + a1 + a2)
+    b0, b1 = np.clip(a0 * binv, 0, 1), np.clip(a1 * binv, 0, 1)
+    d0x, d0y = -p1[:, 3] * p2[:, 1] + p2[:, 3] * p1[:, 1], -p1[:, 0] * p2[:, 3] + p1[:, 3] * p2[:, 0]
+    d1x, d1y = -p2[:, 3] * p0[:, 1] + p2[:, 1] * p0[:, 3], -p2[:, 0] * p0[:, 3] + p2[:, 3] * p0[:, 0]
+    d2x, d2y = -p0[:, 3] * p1[:, 1] + p0[:, 1] * p1[:, 3], -p0[:, 0] * p1[:, 3] + p0[:, 3] * p1[:, 0]
+    dAx, dAy = d0x + d1x + d2x, d0y + d1y + d2y
+    kx, ky = 2.0 / vp[2], 2.0 / vp[3]
+    out = np.zeros((raster.shape[0] * raster.shape[1], 4))
+    out[pix] = np.stack([(d0x - b0 * dAx) * binv * kx, (d0y - b0 * dAy) * binv * ky,
+                         (d1x - b1 * dAx) * binv * kx, (d1y - b1 * dAy) * binv * ky], 1)
+    return out.reshape(raster.shape)
+
+
+def _clamp_gates32(clip, tri, pix, w, vp):
+    """Whether b0 / b1 = a_i / A lie strictly inside (0, 1) when computed in fp32 in the kernel's order
+    (sample_ndc, q = p.xy - s p.w, a_i = cross(q_j, q_k), A = a0 + a1 + a2, b = a_i * (1 / A)): the clamp
+    decides whether a pixel's barycentric passes a gradient, and at a triangle edge fp32 and fp64 can
+    decide differently."""
+    f = np.float32
+    c = np.asarray(clip, np.float32)
+    x, y = (pix % w).astype(np.float32), (pix // w).astype(np.float32)
+    v = np.asarray(vp, np.float32)
+    sx = ((x - v[0] + f(0.5)) * f(2.0) / v[2] - f(1.0)).astype(np.float32)
+    sy = ((y - v[1] + f(0.5)) * f(2.0) / v[3] - f(1.0)).astype(np.float32)
+    q = [(c[tri[:, k], 0] - sx * c[tri[:, k], 3], c[tri[:, k], 1] - sy * c[tri[:, k], 3]) for k in range(3)]
+    cr = lambda a, b: a[0] * b[1] - a[1] * b[0]  # noqa: E731
+    a0, a1, a2 = cr(q[1], q[2]), cr(q[2], q[0]), cr(q[0], q[1])
+    binv = f(1.0) / (a0 + a1 + a2)
+    r0, r1 = a0 * binv, a1 * binv
+    return (r0 > 0) & (r0 < 1), (r1 > 0) & (r1 < 1)
+
+
+def barycentric_derivatives_backward_f64(clip, idx, raster, grad, viewport=None, abs_terms=False, dtype=np.float64):
+    """d(sum grad * derivatives)/d clip [V, 4] in float64 (z stays 0). With abs_terms the per-pixel
+    contributions are accumulated as absolute values (a bound for summation-order error). Whether a
+    clamped barycentric passes gradient is decided in fp32 as the kernel decides it. dtype=np.float32
+    evaluates the per-pixel adjoint in fp32 with the kernel's operations (an estimate of fp32 error)."""
+    clip, tri, pix, sx, sy, vp = _deriv_setup(clip, idx, raster, viewport, dtype)
+    gate0, gate1 = _clamp_gates32(clip, tri, pix, raster.shape[1], vp)
+    g = np.asarray(grad, dtype).reshape(-1, 4)[pix]
+    p0, p1, p2 = (clip[tri[:, k]] for k in range(3))
+    q0 = (p0[:, 0] - sx * p0[:, 3], p0[:, 1] - sy * p0[:, 3])
+    q1 = (p1[:, 0] - sx * p1[:, 3], p1[:, 1] - sy * p1[:, 3])
+    q2 = (p2[:, 0] - sx * p2[:, 3], p2[:, 1] - sy * p2[:, 3])
+    a0 = q1[0] * q2[1] - q1[1] * q2[0]
+    a1 = q2[0] * q0[1] - q2[1] * q0[0]
+    a2 = q0[0] * q1[1] - q0[1] * q1[0]
+    binv = dtype(1.0) / (a0 + a1 + a2)
+    r0, r1 = a0 * binv, a1 * binv
+    b0, b1 = np.clip(r0, 0, 1).astype(dtype), np.clip(r1, 0, 1).astype(dtype)
+    d0x, d0y = -p1[:, 3] * p2[:, 1] + p2[:, 3] * p1[:, 1], -p1[:, 0] * p2[:, 3] + p1[:, 3] * p2[:, 0]
+    d1x, d1y = -p2[:, 3] * p0[:, 1] + p2[:, 1] * p0[:, 3], -p2[:, 0] * p0[:, 3] + p2[:, 3] * p0[:, 0]
+    d2x, d2y = -p0[:, 3] * p1[:, 1] + p0[:, 1] * p1[:, 3], -p0[:, 0] * p1[:, 3] + p0[:, 3] * p1[:, 0]
+    dAx, dAy = d0x + d1x + d2x, d0y + d1y + d2y
+    kx, ky = dtype(2.0) / vp[2], dtype(2.0) / vp[3]
+    gx, gy, gz, gw = g[:, 0], g[:, 1], g[:, 2], g[:, 3]
+    gdAx = -(gx * b0 + gz * b1) * binv * kx
+    gdAy = -(gy * b0 + gw * b1) * binv * ky
+    G0x, G1x, G2x = gx * binv * kx + gdAx, gz * binv * kx + gdAx, gdAx
+    G0y, G1y, G2y = gy * binv * ky + gdAy, gw * binv * ky + gdAy, gdAy
+    gb0 = np.where(gate0, -(gx * dAx * kx + gy * dAy * ky) * binv, dtype(0.0))
+    gb1 = np.where(gate1, -(gz * dAx * kx + gw * dAy * ky) * binv, dtype(0.0))
+    gbinv = (gx * (d0x - b0 * dAx) * kx + gy * (d0y - b0 * dAy) * ky + gz * (d1x - b1 * dAx) * kx +
+             gw * (d1y - b1 * dAy) * ky + gb0 * a0 + gb1 * a1)
+    gha = -gbinv * binv * binv
+    A0, A1, A2 = gb0 * binv + gha, gb1 * binv + gha, gha
+    gq = {k: np.zeros_like(sx) for k in ("0x", "0y", "1x", "1y", "2x", "2y")}
+    gq["1x"] += A0 * q2[1]; gq["2y"] += A0 * q1[0]; gq["1y"] -= A0 * q2[0]; gq["2x"] -= A0 * q1[1]  # noqa: E702
+    gq["2x"] += A1 * q0[1]; gq["0y"] += A1 * q2[0]; gq["2y"] -= A1 * q0[0]; gq["0x"] -= A1 * q2[1]  # noqa: E702
+    gq["0x"] += A2 * q1[1]; gq["1y"] += A2 * q0[0]; gq["0y"] -= A2 * q1[0]; gq["1x"] -= A2 * q0[1]  # noqa: E702
+    gp = [np.stack([gq[f"{k}x"], gq[f"{k}y"], -sx * gq[f"{k}x"] - sy * gq[f"{k}y"]], 1) for k in range(3)]
+    P = (p0, p1, p2)
+    # d0x = -p1.w p2.y + p2.w p1.y ; d0y = -p1.x p2.w + p1.w p2.x
+    gp[1][:, 2] += -G0x * P[2][:, 1] + G0y * P[2][:, 0]; gp[2][:, 1] += -G0x * P[1][:, 3]  # noqa: E702
+    gp[2][:, 2] += G0x * P[1][:, 1] - G0y * P[1][:, 0]; gp[1][:, 1] += G0x * P[2][:, 3]  # noqa: E702
+    gp[1][:, 0] += -G0y * P[2][:, 3]; gp[2][:, 0] += G0y * P[1][:, 3]  # noqa: E702
+    # d1x = -p2.w p0.y + p2.y p0.w ; d1y = -p2.x p0.w + p2.w p0.x
+    gp[2][:, 2] += -G1x * P[0][:, 1] + G1y * P[0][:, 0]; gp[0][:, 1] += -G1x * P[2][:, 3]  # noqa: E702
+    gp[2][:, 1] += G1x * P[0][:, 3]; gp[0][:, 2] += G1x * P[2][:, 1] - G1y * P[2][:, 0]  # noqa: E702
+    gp[2][:, 0] += -G1y * P[0][:, 3]; gp[0][:, 0] += G1y * P[2][:, 3]  # noqa: E702
+    # d2x = -p0.w p1.y + p0.y p1.w ; d2y = -p0.x p1.w + p0.w p1.x
+    gp[0][:, 2] += -G2x * P[1][:, 1] + G2y * P[1][:, 0]; gp[1][:, 1] += -G2x * P[0][:, 3]  # noqa: E702
+    gp[0][:, 1] += G2x * P[1][:, 3]; gp[1][:, 2] += G2x * P[0][:, 1] - G2y * P[0][:, 0]  # noqa: E702
+    gp[0][:, 0] += -G2y * P[1][:, 3]; gp[1][:, 0] += G2y * P[0][:, 3]  # noqa: E702
+    out = np.zeros((clip.shape[0], 4))
+    for k in range(3):
+        vals = np.abs(gp[k]) if abs_terms else gp[k]
+        for c, col in ((0, 0), (1, 1), (2, 3)):
+            np.add.at(out[:, col], tri[:, k], vals[:, c])
+    return out

@@ -251,9 +251,9 @@ std::vector<float> Rasterizer::backward(std::span<const float> clip_positions,
     if (forward_output.width == 0 || forward_output.height == 0 || forward_output.raster.size() != P * 4)
         throw std::invalid_argument("forward_output has inconsistent dimensions");
     if (grad_raster.size() != P * 4) throw std::invalid_argument("grad_raster must have shape [height, width, 4]");
-    if (!grad_barycentric_derivatives.empty())
-        throw std::invalid_argument(
-            "Gradient propagation through barycentric derivatives is not implemented in the portable baseline backend");
+    // the reference rejects a derivative gradient (rasterizer.cpp:459-462); this build propagates it
+    if (!grad_barycentric_derivatives.empty() && grad_barycentric_derivatives.size() != P * 4)
+        throw std::invalid_argument("grad_barycentric_derivatives must have shape [height, width, 4]");
     const Viewport vp = resolve_viewport(
         forward_output.width, forward_output.height,
         forward_output.viewport.width > 0.0F ? std::optional<Viewport>(forward_output.viewport) : std::nullopt);
@@ -268,9 +268,11 @@ std::vector<float> Rasterizer::backward(std::span<const float> clip_positions,
     const float vps[4] = {vp.x, vp.y, vp.width, vp.height};
     DeviceArray<float> d_vp(vps, 4, ctx.stream);
     DeviceArray<float> d_out(static_cast<std::size_t>(V) * 4);
-    check(pdr_rasterize_backward(d_clip.get(), 1, V, d_idx.get(), static_cast<std::uint32_t>(triangle_indices.size() / 3),
-                                 forward_output.width, forward_output.height, d_vp.get(), d_raster.get(), d_grad.get(),
-                                 d_out.get(), ctx.stream));
+    DeviceArray<float> d_gdb;
+    if (!grad_barycentric_derivatives.empty()) d_gdb = upload(grad_barycentric_derivatives, ctx.stream);
+    check(pdr_rasterize_backward_derivatives(
+        d_clip.get(), 1, V, d_idx.get(), static_cast<std::uint32_t>(triangle_indices.size() / 3), forward_output.width,
+        forward_output.height, d_vp.get(), d_raster.get(), d_grad.get(), d_gdb.get(), d_out.get(), ctx.stream));
     return d_out.download(ctx.stream);
 }
 

@@ -153,6 +153,20 @@ pdr_status pdr_rasterize_backward(const float* clip, uint32_t views, uint32_t V,
                        "rasterize_backward");
 }
 
+pdr_status pdr_rasterize_backward_derivatives(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx,
+                                              uint32_t T, uint32_t W, uint32_t H, const float* viewports,
+                                              const float* raster, const float* grad_raster, const float* grad_deriv,
+                                              float* grad_clip, void* stream) {
+    pdr_status st = check_raster_args(clip, views, V, idx, T, W, H, viewports);
+    if (st) return st;
+    if (!raster || !grad_clip) return fail(PDR_INVALID_ARGUMENT, "raster and grad_clip_positions are required");
+    if (!aligned(raster, 16) || (grad_raster && !aligned(grad_raster, 16)) || (grad_deriv && !aligned(grad_deriv, 16)))
+        return fail(PDR_INVALID_ARGUMENT, "raster buffers must be 16-byte aligned");
+    return cuda_status(launch_raster_backward(clip, views, V, idx, T, W, H, viewports, raster, grad_raster, grad_clip,
+                                              (cudaStream_t)stream, grad_deriv),
+                       "rasterize_backward_derivatives");
+}
+
 pdr_status pdr_interpolate_forward(const float* attr, uint64_t stride, uint32_t V, uint32_t A, const uint32_t* idx,
                                    uint32_t T, const float* raster, uint32_t views, uint64_t P, float* out,
                                    void* stream) {

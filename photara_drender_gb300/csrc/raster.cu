@@ -512,17 +512,116 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
     return cudaGetLastError();
 }
 
+// Gradient through the barycentric pixel derivatives (a capability the reference rejects,
+// src/rasterizer.cpp:459-462): the adjoint of rasterize_forward.hlsl's derivative output for the pixel's
+// winning triangle,
+//   D = ((da0/dx - b0 dA/dx) / A * 2/vp.z, (da0/dy - b0 dA/dy) / A * 2/vp.w,
+//        (da1/dx - b1 dA/dx) / A * 2/vp.z, (da1/dy - b1 dA/dy) / A * 2/vp.w),
+// with a_i = cross(q_j, q_k) of the sample-relative positions q = p.xy - s p.w, A = a0 + a1 + a2,
+// b_i = clamp(a_i / A, 0, 1) (no gradient through a clamped b_i) and da_i/dx, da_i/dy the products of
+// clip coordinates. Added to grad_clip (x, y, w; z has no influence) after the barycentric adjoint.
+__global__ void raster_deriv_backward_kernel(const float4* __restrict__ clip_all, uint32_t V,
+                                             const uint3* __restrict__ idx, uint32_t T, uint32_t W, uint32_t H,
+                                             const float4* __restrict__ viewports, const float4* __restrict__ raster,
+                                             const float4* __restrict__ grad_deriv, float* __restrict__ grad_clip) {
+    const uint32_t view = blockIdx.y;
+    const size_t P = (size_t)W * H;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const size_t pix = (size_t)view * P + p;
+    const uint32_t id = raster_id(raster[pix].w);
+    if (id == 0 || id > T) return;
+    const float4 g = grad_deriv[pix];
+    if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f && g.w == 0.0f) return;
+    const uint3 vi = idx[id - 1];
+    if (vi.x >= V || vi.y >= V || vi.z >= V) return;
+    const float4* __restrict__ clip = clip_all + (size_t)view * V;
+    const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+    const float4 vp = viewports[view];
+    const uint32_t x = (uint32_t)(p % W), y = (uint32_t)(p / W);
+    const float sx = sample_ndc(x, vp.x, vp.z);
+    const float sy = sample_ndc(y, vp.y, vp.w);
+    // forward quantities
+    const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+    const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+    const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+    const float a0 = cross2(q1x, q1y, q2x, q2y);
+    const float a1 = cross2(q2x, q2y, q0x, q0y);
+    const float a2 = cross2(q0x, q0y, q1x, q1y);
+    const float ha = a0 + a1 + a2;
+    if (fabsf(ha) <= 1e-12f) return;
+    const float binv = 1.0f / ha;
+    const float r0 = a0 * binv, r1 = a1 * binv;
+    const float b0 = clamp_hlsl(r0, 0.0f, 1.0f), b1 = clamp_hlsl(r1, 0.0f, 1.0f);
+    const float d0x = -p1.w * p2.y + p2.w * p1.y, d0y = -p1.x * p2.w + p1.w * p2.x;
+    const float d1x = -p2.w * p0.y + p2.y * p0.w, d1y = -p2.x * p0.w + p2.w * p0.x;
+    const float d2x = -p0.w * p1.y + p0.y * p1.w, d2y = -p0.x * p1.w + p0.w * p1.x;
+    const float dAx = d0x + d1x + d2x, dAy = d0y + d1y + d2y;
+    const float kx = 2.0f / vp.z, ky = 2.0f / vp.w;
+    // adjoints of D's inputs
+    const float gdAx = -(g.x * b0 + g.z * b1) * binv * kx;
+    const float gdAy = -(g.y * b0 + g.w * b1) * binv * ky;
+    const float G0x = g.x * binv * kx + gdAx, G1x = g.z * binv * kx + gdAx, G2x = gdAx;
+    const float G0y = g.y * binv * ky + gdAy, G1y = g.w * binv * ky + gdAy, G2y = gdAy;
+    float gb0 = -(g.x * dAx * kx + g.y * dAy * ky) * binv;
+    float gb1 = -(g.z * dAx * kx + g.w * dAy * ky) * binv;
+    float gbinv = g.x * (d0x - b0 * dAx) * kx + g.y * (d0y - b0 * dAy) * ky + g.z * (d1x - b1 * dAx) * kx +
+                  g.w * (d1y - b1 * dAy) * ky;
+    if (!(r0 > 0.0f && r0 < 1.0f)) gb0 = 0.0f;
+    if (!(r1 > 0.0f && r1 < 1.0f)) gb1 = 0.0f;
+    float A0 = gb0 * binv, A1 = gb1 * binv;
+    gbinv += gb0 * a0 + gb1 * a1;
+    const float gha = -gbinv * binv * binv;
+    A0 += gha;
+    A1 += gha;
+    const float A2 = gha;
+    // a_i -> q
+    float gq0x = 0.f, gq0y = 0.f, gq1x = 0.f, gq1y = 0.f, gq2x = 0.f, gq2y = 0.f;
+    gq1x += A0 * q2y; gq2y += A0 * q1x; gq1y -= A0 * q2x; gq2x -= A0 * q1y;
+    gq2x += A1 * q0y; gq0y += A1 * q2x; gq2y -= A1 * q0x; gq0x -= A1 * q2y;
+    gq0x += A2 * q1y; gq1y += A2 * q0x; gq0y -= A2 * q1x; gq1x -= A2 * q0y;
+    // q -> p, then the da products -> p
+    float g0[3] = {gq0x, gq0y, -sx * gq0x - sy * gq0y};  // x, y, w of vertex 0
+    float g1[3] = {gq1x, gq1y, -sx * gq1x - sy * gq1y};
+    float g2[3] = {gq2x, gq2y, -sx * gq2x - sy * gq2y};
+    // d0x = -p1.w p2.y + p2.w p1.y ; d0y = -p1.x p2.w + p1.w p2.x
+    g1[2] += -G0x * p2.y + G0y * p2.x; g2[1] += -G0x * p1.w; g2[2] += G0x * p1.y - G0y * p1.x; g1[1] += G0x * p2.w;
+    g1[0] += -G0y * p2.w; g2[0] += G0y * p1.w;
+    // d1x = -p2.w p0.y + p2.y p0.w ; d1y = -p2.x p0.w + p2.w p0.x
+    g2[2] += -G1x * p0.y + G1y * p0.x; g0[1] += -G1x * p2.w; g2[1] += G1x * p0.w; g0[2] += G1x * p2.y - G1y * p2.x;
+    g2[0] += -G1y * p0.w; g0[0] += G1y * p2.w;
+    // d2x = -p0.w p1.y + p0.y p1.w ; d2y = -p0.x p1.w + p0.w p1.x
+    g0[2] += -G2x * p1.y + G2y * p1.x; g1[1] += -G2x * p0.w; g0[1] += G2x * p1.w; g1[2] += G2x * p0.y - G2y * p0.x;
+    g0[0] += -G2y * p1.w; g1[0] += G2y * p0.w;
+    float* gv = grad_clip + (size_t)view * V * 4;
+    const uint32_t vs[3] = {vi.x, vi.y, vi.z};
+    const float* gs[3] = {g0, g1, g2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        atomicAdd(gv + (size_t)vs[k] * 4 + 0, gs[k][0]);
+        atomicAdd(gv + (size_t)vs[k] * 4 + 1, gs[k][1]);
+        atomicAdd(gv + (size_t)vs[k] * 4 + 3, gs[k][2]);
+    }
+}
+
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,
-                                   const float* grad_raster, float* grad_clip, cudaStream_t stream) {
+                                   const float* grad_raster, float* grad_clip, cudaStream_t stream,
+                                   const float* grad_derivatives) {
     cudaError_t err = cudaMemsetAsync(grad_clip, 0, (size_t)views * V * 4 * sizeof(float), stream);
     if (err != cudaSuccess) return err;
     const size_t P = (size_t)W * H;
     const dim3 grid((uint32_t)((P + 255) / 256), views);
-    raster_backward_kernel<<<grid, 256, 0, stream>>>(
+    if (grad_raster)
+        raster_backward_kernel<<<grid, 256, 0, stream>>>(
         reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
         reinterpret_cast<const float4*>(viewports), reinterpret_cast<const float4*>(raster),
         reinterpret_cast<const float4*>(grad_raster), grad_clip);
+    if (grad_derivatives)
+        raster_deriv_backward_kernel<<<grid, 256, 0, stream>>>(
+            reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
+            reinterpret_cast<const float4*>(viewports), reinterpret_cast<const float4*>(raster),
+            reinterpret_cast<const float4*>(grad_derivatives), grad_clip);
     return cudaGetLastError();
 }
 

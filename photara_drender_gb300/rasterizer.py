@@ -252,8 +252,10 @@ class Rasterizer:
                 raster, deriv = raster[0], deriv[0]
             return io.out(raster), io.out(deriv)
 
-    def backward(self, positions, indices, raster, grad_raster, viewport=None):
-        """Rasterizer::backward (src/rasterizer.cpp:444-537); returns d loss / d clip positions."""
+    def backward(self, positions, indices, raster, grad_raster, viewport=None, *, grad_barycentric_derivatives=None):
+        """Rasterizer::backward (src/rasterizer.cpp:444-537); returns d loss / d clip positions.
+        grad_barycentric_derivatives ([H, W, 4], like the forward's derivative output) adds the gradient
+        through the pixel derivatives, which the reference rejects (src/rasterizer.cpp:459-462)."""
         with self.context.lock:
             ctx = self.context
             io = _Io(ctx, positions, indices, raster, grad_raster)
@@ -272,8 +274,16 @@ class Rasterizer:
             h, w = r.shape[1], r.shape[2]
             vps, _ = _viewports(viewport, views, w, h, ctx.device)
             out = torch.empty((views, V, 4), dtype=torch.float32, device=ctx.device)
-            _native.call("pdr_rasterize_backward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h, _ptr(vps),
-                         _ptr(r), _ptr(g), _ptr(out), ctx.stream())
+            if grad_barycentric_derivatives is None:
+                _native.call("pdr_rasterize_backward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h,
+                             _ptr(vps), _ptr(r), _ptr(g), _ptr(out), ctx.stream())
+            else:
+                gd = io.f32(grad_barycentric_derivatives, "grad_barycentric_derivatives")
+                gd = gd.unsqueeze(0) if gd.ndim == 3 else gd
+                if gd.shape != r.shape:
+                    raise ValueError("grad_barycentric_derivatives must have shape [height, width, 4]")
+                _native.call("pdr_rasterize_backward_derivatives", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w,
+                             h, _ptr(vps), _ptr(r), _ptr(g), _ptr(gd), _ptr(out), ctx.stream())
             return io.out(out if batched else out[0])
 
     # -- interpolate --------------------------------------------------------------------------

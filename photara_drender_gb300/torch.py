@@ -26,7 +26,7 @@ def _rasterizer_for(device_index: int, enable_validation: bool) -> Rasterizer:
 class _RasterizeFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, positions, indices, resolution, rasterizer, cull_mode, output_barycentric_derivatives, viewport,
-                recompute):
+                recompute, differentiable_derivatives=False):
         if positions.dtype != torch.float32 or positions.ndim not in (2, 3) or positions.shape[-1] != 4:
             raise ValueError("positions must be a float32 tensor with shape [vertex_count, 4]")
         if indices.ndim != 2 or indices.shape[1] != 3:
@@ -38,24 +38,31 @@ class _RasterizeFunction(torch.autograd.Function):
         ctx.resolution = resolution
         ctx.cull_mode = cull_mode
         ctx.recompute = recompute
+        ctx.differentiable_derivatives = bool(differentiable_derivatives and output_barycentric_derivatives)
         if recompute:
             ctx.save_for_backward(positions.detach(), indices.detach())
         else:
             ctx.save_for_backward(positions.detach(), indices.detach(), raster.detach())
-        ctx.mark_non_differentiable(derivatives)
+        if not ctx.differentiable_derivatives:
+            ctx.mark_non_differentiable(derivatives)
         return raster, derivatives
 
     @staticmethod
-    def backward(ctx, grad_raster, _grad_derivatives):
-        if grad_raster is None:
-            return (None,) * 8
+    def backward(ctx, grad_raster, grad_derivatives):
+        use_deriv = ctx.differentiable_derivatives and grad_derivatives is not None
+        if grad_raster is None and not use_deriv:
+            return (None,) * 9
         if ctx.recompute:
             positions, indices = ctx.saved_tensors
             raster, _ = ctx.rasterizer.forward(positions, indices, ctx.resolution, ctx.cull_mode, False, ctx.viewport)
         else:
             positions, indices, raster = ctx.saved_tensors
-        grad_positions = ctx.rasterizer.backward(positions, indices, raster, grad_raster.contiguous(), ctx.viewport)
-        return grad_positions, None, None, None, None, None, None, None
+        if grad_raster is None:
+            grad_raster = torch.zeros_like(raster)
+        grad_positions = ctx.rasterizer.backward(
+            positions, indices, raster, grad_raster.contiguous(), ctx.viewport,
+            grad_barycentric_derivatives=grad_derivatives.contiguous() if use_deriv else None)
+        return grad_positions, None, None, None, None, None, None, None, None
 
 
 class _InterpolateFunction(torch.autograd.Function):
@@ -112,12 +119,14 @@ class _TextureFunction(torch.autograd.Function):
 def rasterize(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequence[int], *,
               rasterizer: Optional[Rasterizer] = None, device_index: int = 0, enable_validation: bool = False,
               cull_mode: str = "none", output_barycentric_derivatives: bool = True,
-              viewport: Optional[Sequence[float]] = None, recompute_in_backward: bool = False
-              ) -> Tuple[torch.Tensor, torch.Tensor]:
+              viewport: Optional[Sequence[float]] = None, recompute_in_backward: bool = False,
+              differentiable_derivatives: bool = False) -> Tuple[torch.Tensor, torch.Tensor]:
     """Rasterize clip-space vertices and connect the output to autograd (torch.py:181-216).
 
     Resolution uses ``(height, width)`` order. ``recompute_in_backward`` keeps only positions and
-    indices for the backward pass and rasterizes again there, instead of holding the raster."""
+    indices for the backward pass and rasterizes again there, instead of holding the raster.
+    ``differentiable_derivatives`` makes the barycentric derivative output differentiable (its gradient
+    reaches the positions); by default it is a constant, as in the reference."""
     if len(resolution) != 2 or int(resolution[0]) <= 0 or int(resolution[1]) <= 0:
         raise ValueError("resolution must be (height, width) with positive values")
     active = rasterizer or _rasterizer_for(device_index, enable_validation)
@@ -128,7 +137,8 @@ def rasterize(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequen
         else:
             normalized_viewport = [None if v is None else tuple(float(x) for x in v) for v in viewport]
     return _RasterizeFunction.apply(positions, indices, (int(resolution[0]), int(resolution[1])), active, cull_mode,
-                                    output_barycentric_derivatives, normalized_viewport, recompute_in_backward)
+                                    output_barycentric_derivatives, normalized_viewport, recompute_in_backward,
+                                    differentiable_derivatives)
 
 
 def interpolate(vertex_attributes: torch.Tensor, raster: torch.Tensor, indices: torch.Tensor, *,
