@@ -236,6 +236,9 @@ class _RenderFunction(torch.autograd.Function):
             out = _render_forward(r, clip, idx, h, w, attrs, uva, tex, vps, _MODES[cull_mode], _ADDRESS[address_mode])
         ctx.r, ctx.vps, ctx.batched, ctx.viewport = r, vps, batched, viewport
         ctx.mode = _ADDRESS[address_mode]
+        # outputs the loss does not use get no gradient (None), not a zero tensor: a zero raster or uv
+        # gradient would otherwise run the separate adjoints over every pixel for nothing
+        ctx.set_materialize_grads(False)
         ctx.save_for_backward(clip, idx, attrs, uva, tex, out["raster"], out["uv"])
         squeeze = (lambda t: t) if batched else (lambda t: t[0] if t is not None else None)
         result = (squeeze(out["raster"]), squeeze(out["deriv"]), squeeze(out["interp"]), squeeze(out["uv"]),
