@@ -516,6 +516,40 @@ PDR_API pdr_status pdr_fill_texture_on_surface(float* color, uint32_t channels, 
                                                void* workspace, size_t workspace_bytes, uint64_t* stats,
                                                uint32_t* status, void* stream);
 
+/* ---- mipmapped (trilinear) texture sampling: planned in the reference (README.md:141) ---------------- */
+
+/* Levels of the box-filtered pyramid of a width x height texture (at most max_level levels above level 0)
+ * and the texels of levels 1.. (level 0 is the caller's texture). */
+PDR_API pdr_status pdr_mip_pyramid_size(uint32_t width, uint32_t height, uint32_t max_level, uint32_t* levels,
+                                        uint64_t* pyramid_texels);
+/* Builds levels 1.. of texture [height][width][channels] into pyramid (pyramid_texels * channels floats). */
+PDR_API pdr_status pdr_mip_build(const float* texture, uint32_t width, uint32_t height, uint32_t channels,
+                                 uint32_t max_level, float* pyramid, void* stream);
+/* Trilinear sampling at uv [views][P][2] with uv_da [views][P][4] = (du/dx, du/dy, dv/dx, dv/dy): level of
+ * detail 0.5 log2 of the larger squared texel-space derivative, texture_forward.hlsl's bilinear per level;
+ * equal to pdr_texture_forward where the level of detail is <= 0. */
+PDR_API pdr_status pdr_texture_forward_mip(const float* texture, const float* pyramid, uint32_t width,
+                                           uint32_t height, uint32_t channels, uint32_t max_level,
+                                           uint32_t address_mode, const float* uv, const float* uv_da,
+                                           const float* raster, uint32_t views, uint64_t pixels_per_view,
+                                           float* sampled, void* stream);
+/* Adjoint of pdr_texture_forward_mip: grad_texture (level 0, overwritten) includes the folded gradient of the
+ * pyramid levels (grad_pyramid is scratch of the pyramid's size); grad_uv [views][P][2] may be NULL. The
+ * level of detail is a constant: uv_da receives no gradient. */
+PDR_API pdr_status pdr_texture_backward_mip(const float* texture, const float* pyramid, uint32_t width,
+                                            uint32_t height, uint32_t channels, uint32_t max_level,
+                                            uint32_t address_mode, const float* uv, const float* uv_da,
+                                            const float* raster, uint32_t views, uint64_t pixels_per_view,
+                                            const float* grad_sampled, float* grad_texture, float* grad_pyramid,
+                                            float* grad_uv, void* stream);
+/* Pixel derivatives of interpolated attributes from the raster's barycentric derivatives:
+ * attribute_derivatives [views][P][A][2] = (d/dx, d/dy) per attribute; zeros on uncovered pixels. */
+PDR_API pdr_status pdr_interpolate_derivatives(const float* attributes, uint32_t vertex_count,
+                                               uint32_t attribute_count, const uint32_t* indices,
+                                               uint32_t triangle_count, const float* raster,
+                                               const float* barycentric_derivatives, uint32_t views,
+                                               uint64_t pixels_per_view, float* attribute_derivatives, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -575,3 +575,119 @@ def barycentric_derivatives_backward_f64(clip, idx, raster, grad, viewport=None,
         for c, col in ((0, 0), (1, 1), (2, 3)):
             np.add.at(out[:, col], tri[:, k], vals[:, c])
     return out
+
+
+# ---- mipmapped texture sampling (no reference counterpart; README.md:141 lists it as planned) ---------
+
+def _address(c, size, mode):
+    """src/rasterizer.cpp:164-179 addressing of integer texel coordinates (numpy arrays)."""
+    c = np.asarray(c, np.int64)
+    if mode == 0:
+        return np.clip(c, 0, size - 1)
+    if mode == 1:
+        return np.mod(c, size)
+    m = np.mod(c, 2 * size)
+    return np.where(m < size, m, 2 * size - 1 - m)
+
+
+def mip_pyramid(texture, max_level=None):
+    """Levels 0.. of the box-filtered pyramid, each level summed as ((a + b) + (c + d)) * 0.25 in fp32
+    over children {2x, min(2x + 1, w - 1)} x {2y, min(2y + 1, h - 1)}."""
+    levels = [np.asarray(texture, np.float32)]
+    while (levels[-1].shape[0] > 1 or levels[-1].shape[1] > 1) and (max_level is None or len(levels) - 1 < max_level):
+        s = levels[-1]
+        h, w = s.shape[:2]
+        nh, nw = max(1, h >> 1), max(1, w >> 1)
+        y0, x0 = 2 * np.arange(nh), 2 * np.arange(nw)
+        y1, x1 = np.minimum(y0 + 1, h - 1), np.minimum(x0 + 1, w - 1)
+        a, b = s[y0][:, x0], s[y0][:, x1]
+        c, d = s[y1][:, x0], s[y1][:, x1]
+        levels.append((((a + b) + (c + d)) * np.float32(0.25)).astype(np.float32))
+    return levels
+
+
+def mip_lod32(uv_da, w0, h0, nlevels):
+    """The level of detail as the kernel computes it in fp32 (0.5 log2 of the larger squared texel-space
+    derivative, clamped to [0, levels - 1], NaN -> 0)."""
+    da = np.asarray(uv_da, np.float32)
+    ux, uy = da[..., 0] * np.float32(w0), da[..., 1] * np.float32(w0)
+    vx, vy = da[..., 2] * np.float32(h0), da[..., 3] * np.float32(h0)
+    m = np.maximum(ux * ux + vx * vx, uy * uy + vy * vy)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lod = np.float32(0.5) * np.log2(m)
+    return np.where(lod > 0, np.minimum(lod, np.float32(nlevels - 1)), np.float32(0)).astype(np.float32)
+
+
+def _bilinear_level(level, uv, mode):
+    h, w = level.shape[:2]
+    tx = uv[:, 0].astype(np.float64) * w - 0.5
+    ty = uv[:, 1].astype(np.float64) * h - 0.5
+    bx, by = np.floor(tx).astype(np.int64), np.floor(ty).astype(np.int64)
+    fx, fy = tx - np.floor(tx), ty - np.floor(ty)
+    x0, x1 = _address(bx, w, mode), _address(bx + 1, w, mode)
+    y0, y1 = _address(by, h, mode), _address(by + 1, h, mode)
+    return (x0, x1, y0, y1), (fx, fy)
+
+
+def texture_mip_forward(texture, uv, uv_da, raster, mode=0, max_level=None):
+    """Trilinear sample per pixel in float64 from the fp32 pyramid, the level chosen in fp32: [.., C]."""
+    lv = mip_pyramid(texture, max_level)
+    shape = np.asarray(uv).shape[:-1]
+    u = np.asarray(uv, np.float32).reshape(-1, 2)
+    lod = mip_lod32(uv_da, lv[0].shape[1], lv[0].shape[0], len(lv)).reshape(-1)
+    cov = np.rint(np.asarray(raster)[..., 3]).reshape(-1) != 0
+    C_ = lv[0].shape[2]
+    out = np.zeros((u.shape[0], C_))
+    l0 = np.floor(lod).astype(np.int64)
+    f = (lod - np.floor(lod)).astype(np.float64)
+    for k in range(len(lv)):
+        for which, wgt in ((l0 == k, np.where(f > 0, 1.0 - f, 1.0)), ((np.minimum(l0 + 1, len(lv) - 1) == k) & (f > 0), f)):
+            sel = np.flatnonzero(which & cov)
+            if sel.size == 0:
+                continue
+            (x0, x1, y0, y1), (fx, fy) = _bilinear_level(lv[k], u[sel], mode)
+            L = lv[k].astype(np.float64)
+            s = (L[y0, x0] * ((1 - fx) * (1 - fy))[:, None] + L[y0, x1] * (fx * (1 - fy))[:, None] +
+                 L[y1, x0] * ((1 - fx) * fy)[:, None] + L[y1, x1] * (fx * fy)[:, None])
+            out[sel] += wgt[sel][:, None] * s
+    return out.reshape(shape + (C_,)), lod.reshape(shape)
+
+
+def texture_mip_backward(texture, uv, uv_da, raster, grad, mode=0, max_level=None):
+    """(grad_texture [H, W, C], grad_uv [.., 2]) in float64: scatter into every sampled level, then fold
+    the pyramid gradient to level 0 (coarsest first); the level of detail is a constant."""
+    lv = mip_pyramid(texture, max_level)
+    shape = np.asarray(uv).shape[:-1]
+    u = np.asarray(uv, np.float32).reshape(-1, 2)
+    g = np.asarray(grad, np.float64).reshape(u.shape[0], -1)
+    lod = mip_lod32(uv_da, lv[0].shape[1], lv[0].shape[0], len(lv)).reshape(-1)
+    cov = np.rint(np.asarray(raster)[..., 3]).reshape(-1) != 0
+    gl = [np.zeros(x.shape, np.float64) for x in lv]
+    guv = np.zeros((u.shape[0], 2))
+    l0 = np.floor(lod).astype(np.int64)
+    f = (lod - np.floor(lod)).astype(np.float64)
+    for k in range(len(lv)):
+        for which, wgt in ((l0 == k, np.where(f > 0, 1.0 - f, 1.0)), ((np.minimum(l0 + 1, len(lv) - 1) == k) & (f > 0), f)):
+            sel = np.flatnonzero(which & cov)
+            if sel.size == 0:
+                continue
+            h, w = lv[k].shape[:2]
+            (x0, x1, y0, y1), (fx, fy) = _bilinear_level(lv[k], u[sel], mode)
+            gc = g[sel] * wgt[sel][:, None]
+            for (yy, xx), ww in (((y0, x0), (1 - fx) * (1 - fy)), ((y0, x1), fx * (1 - fy)),
+                                 ((y1, x0), (1 - fx) * fy), ((y1, x1), fx * fy)):
+                np.add.at(gl[k], (yy, xx), gc * ww[:, None])
+            L = lv[k].astype(np.float64)
+            c00, c10, c01, c11 = L[y0, x0], L[y0, x1], L[y1, x0], L[y1, x1]
+            guv[sel, 0] += (gc * (((1 - fy)[:, None] * (c10 - c00) + fy[:, None] * (c11 - c01)) * w)).sum(1)
+            guv[sel, 1] += (gc * (((1 - fx)[:, None] * (c01 - c00) + fx[:, None] * (c11 - c10)) * h)).sum(1)
+    for k in range(len(lv) - 1, 0, -1):
+        ph, pw = lv[k].shape[:2]
+        ch, cw = lv[k - 1].shape[:2]
+        y0, x0 = 2 * np.arange(ph), 2 * np.arange(pw)
+        y1, x1 = np.minimum(y0 + 1, ch - 1), np.minimum(x0 + 1, cw - 1)
+        q = gl[k] * 0.25
+        for yy in (y0, y1):
+            for xx in (x0, x1):
+                np.add.at(gl[k - 1], (yy[:, None], xx[None, :]), q)
+    return gl[0], guv.reshape(shape + (2,))

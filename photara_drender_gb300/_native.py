@@ -75,6 +75,12 @@ _SIGNATURES = {
                                      _vp, _vp]),
     "pdr_surface_fill_workspace_bytes": (_i32, [_u32, _u32, _u32, _vp]),
     "pdr_fill_texture_on_surface": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32, _u32, _vp, _u32, _vp, _sz, _vp, _vp, _vp]),
+    "pdr_mip_pyramid_size": (_i32, [_u32, _u32, _u32, _vp, _vp]),
+    "pdr_mip_build": (_i32, [_vp, _u32, _u32, _u32, _u32, _vp, _vp]),
+    "pdr_texture_forward_mip": (_i32, [_vp, _vp, _u32, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _u32, _u64, _vp, _vp]),
+    "pdr_texture_backward_mip": (_i32, [_vp, _vp, _u32, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _u32, _u64, _vp, _vp,
+                                        _vp, _vp, _vp]),
+    "pdr_interpolate_derivatives": (_i32, [_vp, _u32, _u32, _vp, _u32, _vp, _vp, _u32, _u64, _vp, _vp]),
     "pdr_refine_prepare_view": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "pdr_refine_photometric": (_i32, [_vp, _u32, _u32, _vp, _u32, _u64, _u32, _u32, C.c_float, C.c_float, _vp, _vp,
                                       _vp]),

@@ -148,9 +148,20 @@ def interpolate(vertex_attributes: torch.Tensor, raster: torch.Tensor, indices: 
 
 
 def texture(texture_values: torch.Tensor, uv: torch.Tensor, raster: torch.Tensor, *, rasterizer: Rasterizer,
-            address_mode: str = "clamp") -> torch.Tensor:
-    """Sample a texture bilinearly and propagate gradients to texels and UV coordinates (torch.py:231-241)."""
-    return _TextureFunction.apply(texture_values, uv, raster, rasterizer, address_mode)
+            address_mode: str = "clamp", filter_mode: str = "linear", uv_da: Optional[torch.Tensor] = None,
+            max_mip_level: Optional[int] = None) -> torch.Tensor:
+    """Sample a texture bilinearly and propagate gradients to texels and UV coordinates (torch.py:231-241).
+
+    ``filter_mode="linear-mipmap-linear"`` samples a box-filtered mip pyramid trilinearly instead, with the
+    level of detail from ``uv_da`` (du/dx, du/dy, dv/dx, dv/dy per pixel; ``mip.interpolate_derivatives``
+    makes it from the raster's barycentric derivatives). The reference has only bilinear sampling."""
+    if filter_mode == "linear":
+        return _TextureFunction.apply(texture_values, uv, raster, rasterizer, address_mode)
+    if filter_mode == "linear-mipmap-linear":
+        from .mip import texture_mip
+
+        return texture_mip(texture_values, uv, uv_da, raster, address_mode=address_mode, max_mip_level=max_mip_level)
+    raise ValueError("filter_mode must be 'linear' or 'linear-mipmap-linear'")
 
 
 # ---- fused rasterize -> interpolate -> texture ---------------------------------------------------------
