@@ -105,6 +105,34 @@ PDR_API pdr_status pdr_rasterize_backward_derivatives(const float* clip_position
                                                       const float* grad_barycentric_derivatives,
                                                       float* grad_clip_positions, void* stream);
 
+/* ---- near-plane clipping ------------------------------------------------------------------------
+ * The reference has none: it skips every triangle with a vertex at w <= 1e-8 and rasterizes the others
+ * unclipped (README.md:140, docs/architecture.md:62; Rasterizer::forward, src/rasterizer.cpp:373-442).
+ * Opt-in sequence: pdr_clip_near -> pdr_bin_tiles + pdr_rasterize_forward on the clipped mesh (vertex
+ * count 4 * T, triangle count 2 * T) -> pdr_remap_near; gradients with pdr_rasterize_backward_near. */
+#define PDR_NEAR_MAX_TRIANGLES 8388608u /* ids of the clipped mesh (up to 2 * T) stay exact in fp32 */
+/* Clips every triangle of every view against z + w = 0 into clipped_positions [views][4 * T][4] and the
+ * view-independent clipped_indices [2 * T][3] (slots 2k and 2k + 1 hold what is left of triangle k; a slot
+ * with nothing left touches a vertex with w = 0 and covers nothing). An index >= vertex_count leaves
+ * the triangle empty and sets status[PDR_STATUS_INDEX_ERROR] (status may be NULL). */
+PDR_API pdr_status pdr_clip_near(const float* clip_positions, uint32_t views, uint32_t vertex_count,
+                                 const uint32_t* indices, uint32_t triangle_count, float* clipped_positions,
+                                 uint32_t* clipped_indices, uint32_t* status, void* stream);
+/* In place on the raster (and derivatives, may be NULL) of the clipped mesh: ids become the original
+ * triangle's, and barycentrics, depth and derivatives are those of the original triangle at the pixel
+ * (rasterize_forward.hlsl's formulas); identical to pdr_rasterize_forward where no clipping happened. */
+PDR_API pdr_status pdr_remap_near(const float* clip_positions, uint32_t views, uint32_t vertex_count,
+                                  const uint32_t* indices, uint32_t triangle_count, uint32_t width, uint32_t height,
+                                  const float* viewports, float* raster, float* barycentric_derivatives,
+                                  void* stream);
+/* pdr_rasterize_backward_derivatives for a remapped raster: triangles with a vertex at w <= 1e-8 (never
+ * visited by the reference's adjoint) are visited on every pixel they own; others as the reference. */
+PDR_API pdr_status pdr_rasterize_backward_near(const float* clip_positions, uint32_t views, uint32_t vertex_count,
+                                               const uint32_t* indices, uint32_t triangle_count, uint32_t width,
+                                               uint32_t height, const float* viewports, const float* raster,
+                                               const float* grad_raster, const float* grad_barycentric_derivatives,
+                                               float* grad_clip_positions, void* stream);
+
 /* Rasterizer::interpolate_forward (src/rasterizer.cpp:539-601 + shaders/interpolate_forward.hlsl).
  * attribute_view_stride = 0 shares one [V][A] table across views, else floats between views. */
 PDR_API pdr_status pdr_interpolate_forward(const float* attributes, uint64_t attribute_view_stride,

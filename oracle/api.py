@@ -691,3 +691,233 @@ def texture_mip_backward(texture, uv, uv_da, raster, grad, mode=0, max_level=Non
             for xx in (x0, x1):
                 np.add.at(gl[k - 1], (yy[:, None], xx[None, :]), q)
     return gl[0], guv.reshape(shape + (2,))
+
+
+# ---- near-plane clipping (no reference counterpart; README.md:140 and docs/architecture.md:62 say the
+# reference drops every triangle with a vertex at w <= 1e-8 and rasterizes the rest unclipped) ----------
+#
+# clip_near / rasterize_forward_near restate the GPU design in float32, operation by operation, so that the
+# GPU result can be checked bit for bit; near_truth_f64 and rasterize_backward_near (float64) are the
+# independent checks: what a pixel should see, decided geometrically in float64, and the adjoint.
+
+def _near_point(ia, pa, ib, pb):
+    """Intersection of edges (a, b) with z + w = 0, from the lower-indexed vertex, in float32."""
+    sw = (ib < ia)[:, None]
+    a, b = np.where(sw, pb, pa), np.where(sw, pa, pb)
+    da, db = a[:, 2] + a[:, 3], b[:, 2] + b[:, 3]
+    t = (da / (da - db))[:, None]
+    return (a + t * (b - a)).astype(np.float32)
+
+
+def clip_near(clip, idx):
+    """One view's clipped mesh: positions [4 T, 4] (slots 4k .. 4k+3) and indices [2 T, 3] with slot
+    2k = (4k, 4k+1, 4k+2), 2k+1 = (4k, 4k+2, 4k+3). A triangle entirely in front (z + w >= 0) is copied
+    into slots 0-2; with one vertex in front, slots 0-2 hold it and the points on its two edges; with one
+    vertex behind, the quad (edge o->a, a, b, edge b->o); unused slots are zero (w = 0: never binned)."""
+    c = _f(clip).reshape(-1, 4)
+    I = np.asarray(idx, np.int64).reshape(-1, 3)
+    T = I.shape[0]
+    k4 = 4 * np.arange(T, dtype=np.uint32)[:, None]
+    cidx = np.stack([k4 + np.array([0, 1, 2], np.uint32), k4 + np.array([0, 2, 3], np.uint32)], 1).reshape(-1, 3)
+    out = np.zeros((T, 4, 4), np.float32)
+    P = c[I]
+    with np.errstate(all="ignore"):
+        inside = (P[..., 2] + P[..., 3]) >= np.float32(0.0)
+        n_in = inside.sum(1)
+        all_in = np.flatnonzero(n_in == 3)
+        out[all_in, :3] = P[all_in]
+        one = np.flatnonzero(n_in == 1)
+        if one.size:
+            i = np.argmax(inside[one], 1)
+            j, l = (i + 1) % 3, (i + 2) % 3
+            pi, pj, pl = P[one, i], P[one, j], P[one, l]
+            ii, ij, il = I[one, i], I[one, j], I[one, l]
+            out[one, 0] = pi
+            out[one, 1] = _near_point(ii, pi, ij, pj)
+            out[one, 2] = _near_point(il, pl, ii, pi)
+        two = np.flatnonzero(n_in == 2)
+        if two.size:
+            o = np.argmin(inside[two], 1)
+            a, b = (o + 1) % 3, (o + 2) % 3
+            po, pa, pb = P[two, o], P[two, a], P[two, b]
+            io, ia, ib = I[two, o], I[two, a], I[two, b]
+            out[two, 0] = _near_point(io, po, ia, pa)
+            out[two, 1] = pa
+            out[two, 2] = pb
+            out[two, 3] = _near_point(ib, pb, io, po)
+    return out.reshape(-1, 4), cidx
+
+
+def _sample32(pix, w, vp):
+    f = np.float32
+    x, y = (pix % w).astype(np.float32), (pix // w).astype(np.float32)
+    sx = ((x - vp[0] + f(0.5)) * f(2.0) / vp[2] - f(1.0)).astype(np.float32)
+    sy = ((y - vp[1] + f(0.5)) * f(2.0) / vp[3] - f(1.0)).astype(np.float32)
+    return sx, sy
+
+
+def rasterize_forward_near(clip, idx, resolution, cull_mode=0, viewport=None):
+    """Raster and derivatives of one view with near-plane clipping: the clipped mesh through the
+    reference-order rasterizer (ora_rasterize_forward), then each covered pixel remapped to the original
+    triangle k = (slot id - 1) // 2 with rasterize_forward.hlsl's float32 formulas evaluated on it."""
+    c = _f(clip).reshape(-1, 4)
+    I = np.asarray(idx, np.int64).reshape(-1, 3)
+    h, w = int(resolution[0]), int(resolution[1])
+    cp, ci = clip_near(c, I)
+    raster, deriv = rasterize_forward(cp, ci, (h, w), cull_mode, True, viewport)
+    vp = _vp(viewport, w, h)
+    f = np.float32
+    r = raster.reshape(-1, 4)
+    d = deriv.reshape(-1, 4)
+    ids = np.rint(r[:, 3]).astype(np.int64)
+    pix = np.flatnonzero((ids > 0) & (ids <= 2 * I.shape[0]))
+    k = (ids[pix] - 1) // 2
+    tri = I[k]
+    p0, p1, p2 = (c[tri[:, m]] for m in range(3))
+    sx, sy = _sample32(pix, w, vp)
+    with np.errstate(all="ignore"):
+        q = [(p[:, 0] - sx * p[:, 3], p[:, 1] - sy * p[:, 3]) for p in (p0, p1, p2)]
+        cr = lambda u, v: u[0] * v[1] - u[1] * v[0]  # noqa: E731
+        a0, a1, a2 = cr(q[1], q[2]), cr(q[2], q[0]), cr(q[0], q[1])
+        ha = (a0 + a1) + a2
+        binv = f(1.0) / ha
+        iz = (p0[:, 2] * a0 + p1[:, 2] * a1) + p2[:, 2] * a2
+        iw = (p0[:, 3] * a0 + p1[:, 3] * a1) + p2[:, 3] * a2
+        clamp = lambda x, lo, hi: np.fmin(np.fmax(x, f(lo)), f(hi))  # noqa: E731
+        depth = clamp(iz / iw, -1.0, 1.0)
+        b0, b1 = clamp(a0 * binv, 0.0, 1.0), clamp(a1 * binv, 0.0, 1.0)
+        r[pix] = np.stack([b0, b1, depth, (k + 1).astype(np.float32)], 1)
+        d0x = -p1[:, 3] * p2[:, 1] + p2[:, 3] * p1[:, 1]
+        d0y = -p1[:, 0] * p2[:, 3] + p1[:, 3] * p2[:, 0]
+        d1x = -p2[:, 3] * p0[:, 1] + p2[:, 1] * p0[:, 3]
+        d1y = -p2[:, 0] * p0[:, 3] + p2[:, 3] * p0[:, 0]
+        d2x = -p0[:, 3] * p1[:, 1] + p0[:, 1] * p1[:, 3]
+        d2y = -p0[:, 0] * p1[:, 3] + p0[:, 3] * p1[:, 0]
+        dAx, dAy = (d0x + d1x) + d2x, (d0y + d1y) + d2y
+        two = f(2.0)
+        d[pix] = np.stack([(d0x - b0 * dAx) * binv * two / vp[2], (d0y - b0 * dAy) * binv * two / vp[3],
+                           (d1x - b1 * dAx) * binv * two / vp[2], (d1y - b1 * dAy) * binv * two / vp[3]], 1)
+    return r.reshape(h, w, 4), d.reshape(h, w, 4)
+
+
+def near_truth_f64(clip, idx, resolution, cull_mode=0, viewport=None, margin=1e-4, depth_gap=1e-5):
+    """What each pixel sees with near-plane clipping, decided in float64 from the geometry alone: the ray
+    through the pixel centre hits triangle t at the clip-space point sum(l_i p_i) with the homogeneous
+    barycentrics l_i = a_i / A (a_i the 2D homogeneous edge functions, A their sum); t covers the pixel
+    when every l_i >= 0 and the hit lies in front of the near plane (z + w >= 0, w > 0); culling uses the
+    sign of det[x y w] of the vertices (A = det / w_hit, so it is the winding of the part in front of the
+    eye); the nearest depth z / w wins. Pixels within `margin` of
+    an edge or the near plane, or with two candidates closer than `depth_gap` in depth, are undecided.
+    Returns (ids [H, W] int64: 0 empty, t + 1, or -1 undecided; barycentrics [H, W, 2]; depth [H, W])."""
+    c = np.asarray(clip, np.float64).reshape(-1, 4)
+    I = np.asarray(idx, np.int64).reshape(-1, 3)
+    h, w = int(resolution[0]), int(resolution[1])
+    vp = np.asarray(_vp(viewport, w, h), np.float64)
+    pix = np.arange(h * w)
+    sx = ((pix % w) - vp[0] + 0.5) * 2.0 / vp[2] - 1.0
+    sy = ((pix // w) - vp[1] + 0.5) * 2.0 / vp[3] - 1.0
+    best = np.full(h * w, np.inf)
+    second = np.full(h * w, np.inf)
+    best_id = np.zeros(h * w, np.int64)
+    lam = np.zeros((h * w, 2))
+    marginal = np.zeros(h * w, bool)
+    for t in range(I.shape[0]):
+        p = c[I[t]]
+        qx = p[:, 0][:, None] - sx[None] * p[:, 3][:, None]
+        qy = p[:, 1][:, None] - sy[None] * p[:, 3][:, None]
+        a = np.stack([qx[1] * qy[2] - qy[1] * qx[2], qx[2] * qy[0] - qy[2] * qx[0], qx[0] * qy[1] - qy[0] * qx[1]])
+        A = a.sum(0)
+        D = np.linalg.det(p[:, [0, 1, 3]])  # A = D / w of the hit: the winding seen in front of the eye
+        if not np.any(np.abs(A) > 1e-12) or D == 0:
+            continue
+        if (cull_mode == 1 and D <= 0) or (cull_mode == 2 and D >= 0):
+            continue
+        with np.errstate(all="ignore"):
+            l = a / A
+            pz, pw = l.T @ p[:, 2], l.T @ p[:, 3]
+            front = (pz + pw) / np.abs(pw)
+            depth = pz / pw
+        lmin = l.min(0)
+        inside = (lmin >= 0) & (front >= 0) & (pw > 0)
+        near_edge = (np.abs(lmin) < margin) | ((np.abs(front) < margin) & (lmin > -margin))
+        marginal |= near_edge
+        cov = np.flatnonzero(inside & ~near_edge)
+        d = depth[cov]
+        closer = d < best[cov]
+        second[cov] = np.where(closer, best[cov], np.minimum(second[cov], d))
+        upd = cov[closer]
+        best[upd] = d[closer]
+        best_id[upd] = t + 1
+        lam[upd] = l[:2, upd].T
+    ids = best_id.copy()
+    with np.errstate(invalid="ignore"):
+        undecided = marginal | (second - best < depth_gap)
+    ids[undecided] = -1
+    return ids.reshape(h, w), lam.reshape(h, w, 2), best.reshape(h, w)
+
+
+def rasterize_backward_near(clip, idx, raster, grad, viewport=None, dtype=np.float64, abs_terms=False):
+    """d(sum grad[..., :2] * raster[..., :2]) / d clip [V, 4] for a raster remapped to the original triangles
+    (rasterize_backward.hlsl's per-pixel adjoint, with its 1e-6 area offset). A triangle whose vertices
+    all have w > 1e-8 is visited on the pixels of its projected bounds, as the reference visits it; one
+    with a vertex at w <= 1e-8 (which the reference never visits) on every pixel it owns. dtype float32
+    evaluates the per-pixel adjoint with the kernel's float32 operations; abs_terms sums |terms|."""
+    c32 = _f(clip).reshape(-1, 4)
+    I = np.asarray(idx, np.int64).reshape(-1, 3)
+    h, w = raster.shape[:2]
+    vp32 = _vp(viewport, w, h)
+    r = np.asarray(raster, np.float32).reshape(-1, 4)
+    g = np.asarray(grad, np.float32).reshape(-1, 4)
+    ids = np.rint(r[:, 3]).astype(np.int64)
+    pix = np.flatnonzero((ids > 0) & (ids <= I.shape[0]) & ~((g[:, 0] == 0) & (g[:, 1] == 0)))
+    tri = I[ids[pix] - 1]
+    P32 = [c32[tri[:, m]] for m in range(3)]
+    behind = (P32[0][:, 3] <= np.float32(1e-8)) | (P32[1][:, 3] <= np.float32(1e-8)) | (P32[2][:, 3] <= np.float32(1e-8))
+    with np.errstate(all="ignore"):
+        s = [(p[:, 0] / p[:, 3], p[:, 1] / p[:, 3]) for p in P32]
+        f, half = np.float32, np.float32(0.5)
+        mnx, mxx = np.fmin(np.fmin(s[0][0], s[1][0]), s[2][0]), np.fmax(np.fmax(s[0][0], s[1][0]), s[2][0])
+        mny, mxy = np.fmin(np.fmin(s[0][1], s[1][1]), s[2][1]), np.fmax(np.fmax(s[0][1], s[1][1]), s[2][1])
+
+        def bound(v, lim):
+            v = np.where(np.isnan(v), 0.0, np.clip(v.astype(np.float64), -2.0 ** 31, 2.0 ** 31 - 1))
+            return np.clip(v, 0, lim).astype(np.int64)
+
+        x0 = bound(np.floor((mnx * half + half) * vp32[2] + vp32[0]), w)
+        x1 = bound(np.ceil((mxx * half + half) * vp32[2] + vp32[0]), w)
+        y0 = bound(np.floor((mny * half + half) * vp32[3] + vp32[1]), h)
+        y1 = bound(np.ceil((mxy * half + half) * vp32[3] + vp32[1]), h)
+        px, py = pix % w, pix // w
+        visit = behind | ((px >= x0) & (px < x1) & (py >= y0) & (py < y1))
+    pix, tri = pix[visit], tri[visit]
+    if dtype == np.float32:
+        sx, sy = _sample32(pix, w, vp32)
+        p = [c32[tri[:, m]] for m in range(3)]
+    else:
+        vp = vp32.astype(np.float64)
+        sx = ((pix % w) - vp[0] + 0.5) * 2.0 / vp[2] - 1.0
+        sy = ((pix // w) - vp[1] + 0.5) * 2.0 / vp[3] - 1.0
+        p = [c32[tri[:, m]].astype(np.float64) for m in range(3)]
+    gx, gy = g[pix, 0].astype(dtype), g[pix, 1].astype(dtype)
+    with np.errstate(all="ignore"):
+        q = [(pp[:, 0] - sx * pp[:, 3], pp[:, 1] - sy * pp[:, 3]) for pp in p]
+        cr = lambda u, v: u[0] * v[1] - u[1] * v[0]  # noqa: E731
+        a0, a1 = cr(q[1], q[2]), cr(q[2], q[0])
+        area = (a0 + a1) + cr(q[0], q[1])
+        keep = ~(np.abs(area.astype(np.float64)) <= float(np.float32(1e-12)))
+        e6 = dtype(np.float32(1e-6))  # the kernel's 1e-6f
+        eps = np.where(area >= 0, e6, -e6).astype(dtype)
+        inv = dtype(1.0) / (area + eps)
+        b0, b1 = a0 * inv, a1 * inv
+        gb0, gb1 = gx * inv, gy * inv
+        gc = gb0 * b0 + gb1 * b1
+        (q0x, q0y), (q1x, q1y), (q2x, q2y) = q
+        gxs = [gc * (q2y - q1y) - gb1 * q2y, gc * (q0y - q2y) + gb0 * q2y, gc * (q1y - q0y) - gb0 * q1y + gb1 * q0y]
+        gys = [gc * (q1x - q2x) + gb1 * q2x, gc * (q2x - q0x) - gb0 * q2x, gc * (q0x - q1x) + gb0 * q1x - gb1 * q0x]
+    out = np.zeros((c32.shape[0], 4))
+    for m in range(3):
+        vals = [gxs[m], gys[m], -sx * gxs[m] - sy * gys[m]]
+        for col, v in zip((0, 1, 3), vals):
+            v = np.where(keep, v, 0).astype(np.float64)
+            np.add.at(out[:, col], tri[:, m], np.abs(v) if abs_terms else v)
+    return out

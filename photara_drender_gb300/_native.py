@@ -48,6 +48,9 @@ _SIGNATURES = {
     "pdr_rasterize_backward": (_i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     "pdr_rasterize_backward_derivatives": (_i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp,
                                                   _vp]),
+    "pdr_clip_near": (_i32, [_vp, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _vp]),
+    "pdr_remap_near": (_i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp]),
+    "pdr_rasterize_backward_near": (_i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pdr_interpolate_forward": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp]),
     "pdr_interpolate_backward": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp, _vp, _vp]),
     "pdr_interpolate_backward_accumulate": (_i32, [_vp, _u64, _u32, _u32, _vp, _u32, _vp, _u32, _u64, _vp, _vp,

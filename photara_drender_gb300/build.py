@@ -13,7 +13,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphotara_drender_gb300.so")
 CPP_LIB = os.path.join(HERE, "libphotara_drender.so")  # the C++ API of include/photara_drender/*.hpp
 CPP_SOURCES = [os.path.join(HERE, "cpp", "photara_drender.cpp")]
-SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "precond.cu", "batch.cu", "bvh.cu", "padding.cu", "mip.cu", "capi.cu"]
+SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "precond.cu", "batch.cu", "bvh.cu", "padding.cu", "mip.cu", "near.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]

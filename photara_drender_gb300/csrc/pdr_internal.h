@@ -55,7 +55,7 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,
                                    const float* grad_raster, float* grad_clip, cudaStream_t stream,
-                                   const float* grad_derivatives = nullptr);
+                                   const float* grad_derivatives = nullptr, bool near = false);
 
 cudaError_t launch_interpolate_forward(const float* attr, size_t attr_view_stride, uint32_t V, uint32_t A,
                                        const uint32_t* idx, uint32_t T, const float* raster, uint32_t views,

@@ -337,10 +337,13 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
 // One thread per pixel. A pixel contributes to triangle t exactly when the reference's
 // per-triangle loop would visit it: raster id == t+1, inside t's clamped pixel bounds
 // (rasterize_backward.hlsl:78-90) and a non-zero (u, v) gradient. Corner sums use atomics.
+// With near-plane clipping (near != 0) a triangle with a vertex at w <= 1e-8, which the reference
+// never visits, owns the pixels the clipped raster gave it and is visited on all of them (its
+// projected bounds do not exist); every other triangle keeps the reference's rule.
 __global__ void raster_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                                        uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports,
                                        const float4* __restrict__ raster, const float4* __restrict__ grad_raster,
-                                       float* __restrict__ grad_clip) {
+                                       float* __restrict__ grad_clip, uint32_t near) {
     const uint32_t view = blockIdx.y;
     const size_t P = (size_t)W * H;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -355,10 +358,11 @@ __global__ void raster_backward_kernel(const float4* __restrict__ clip_all, uint
     if (vi.x >= V || vi.y >= V || vi.z >= V) return;
     const float4* __restrict__ clip = clip_all + (size_t)view * V;
     const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
-    if (p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f) return;
+    const bool behind = p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f;
+    if (behind && !near) return;
     const float4 vp = viewports[view];
     const uint32_t x = (uint32_t)(p % W), y = (uint32_t)(p / W);
-    {
+    if (!behind) {
         const float s0x = p0.x / p0.w, s0y = p0.y / p0.w;
         const float s1x = p1.x / p1.w, s1y = p1.y / p1.w;
         const float s2x = p2.x / p2.w, s2y = p2.y / p2.w;
@@ -607,7 +611,7 @@ __global__ void raster_deriv_backward_kernel(const float4* __restrict__ clip_all
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,
                                    const float* grad_raster, float* grad_clip, cudaStream_t stream,
-                                   const float* grad_derivatives) {
+                                   const float* grad_derivatives, bool near) {
     cudaError_t err = cudaMemsetAsync(grad_clip, 0, (size_t)views * V * 4 * sizeof(float), stream);
     if (err != cudaSuccess) return err;
     const size_t P = (size_t)W * H;
@@ -616,7 +620,7 @@ cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V
         raster_backward_kernel<<<grid, 256, 0, stream>>>(
         reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,
         reinterpret_cast<const float4*>(viewports), reinterpret_cast<const float4*>(raster),
-        reinterpret_cast<const float4*>(grad_raster), grad_clip);
+        reinterpret_cast<const float4*>(grad_raster), grad_clip, near ? 1u : 0u);
     if (grad_derivatives)
         raster_deriv_backward_kernel<<<grid, 256, 0, stream>>>(
             reinterpret_cast<const float4*>(clip), V, reinterpret_cast<const uint3*>(idx), T, W, H,

@@ -78,6 +78,44 @@ __device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx
     return fminf(fminf(e00, e10), fminf(e01, e11)) - slack > 1e-7f;
 }
 
+// The winner's outputs at sample (sx, sy), rasterize_forward.hlsl's arithmetic: clamped barycentrics,
+// 1 / area and clamped depth; and its pixel derivatives [du/dx, du/dy, dv/dx, dv/dy]. Shared with the
+// near-plane remap, which evaluates them for the original triangle of a clipped one.
+struct WinnerBary {
+    float b0, b1, binv, depth;
+};
+
+__device__ __forceinline__ WinnerBary winner_barycentrics(float4 p0, float4 p1, float4 p2, float sx, float sy) {
+    const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
+    const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
+    const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
+    const float a0 = cross2(q1x, q1y, q2x, q2y);
+    const float a1 = cross2(q2x, q2y, q0x, q0y);
+    const float a2 = cross2(q0x, q0y, q1x, q1y);
+    const float ha = a0 + a1 + a2;
+    WinnerBary r;
+    r.binv = 1.0f / ha;
+    const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
+    const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
+    r.depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
+    r.b0 = clamp_hlsl(a0 * r.binv, 0.0f, 1.0f);
+    r.b1 = clamp_hlsl(a1 * r.binv, 0.0f, 1.0f);
+    return r;
+}
+
+__device__ __forceinline__ float4 winner_derivatives(float4 p0, float4 p1, float4 p2, const WinnerBary& w, float4 vp) {
+    const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
+    const float da0_dy = -p1.x * p2.w + p1.w * p2.x;
+    const float da1_dx = -p2.w * p0.y + p2.y * p0.w;
+    const float da1_dy = -p2.x * p0.w + p2.w * p0.x;
+    const float da2_dx = -p0.w * p1.y + p0.y * p1.w;
+    const float da2_dy = -p0.x * p1.w + p0.w * p1.x;
+    const float dadx = da0_dx + da1_dx + da2_dx;
+    const float dady = da0_dy + da1_dy + da2_dy;
+    return make_float4((da0_dx - w.b0 * dadx) * w.binv * 2.0f / vp.z, (da0_dy - w.b0 * dady) * w.binv * 2.0f / vp.w,
+                       (da1_dx - w.b1 * dadx) * w.binv * 2.0f / vp.z, (da1_dy - w.b1 * dady) * w.binv * 2.0f / vp.w);
+}
+
 // Orders (depth, triangle) pairs as the reference's depth test does: nearest depth first (-0 and
 // +0 equal), then the lowest triangle index.
 __device__ __forceinline__ unsigned long long depth_key(float depth, uint32_t t) {
@@ -241,37 +279,11 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
     // the winner's barycentrics and depth, recomputed with the reference's arithmetic
     const uint32_t best_tri = (uint32_t)key + 1u;
     const uint3 vi = idx[best_tri - 1];
-    float bb0, bb1, binv, best_depth;
-    {
-        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
-        const float q0x = p0.x - sx * p0.w, q0y = p0.y - sy * p0.w;
-        const float q1x = p1.x - sx * p1.w, q1y = p1.y - sy * p1.w;
-        const float q2x = p2.x - sx * p2.w, q2y = p2.y - sy * p2.w;
-        const float a0 = cross2(q1x, q1y, q2x, q2y);
-        const float a1 = cross2(q2x, q2y, q0x, q0y);
-        const float a2 = cross2(q0x, q0y, q1x, q1y);
-        const float ha = a0 + a1 + a2;
-        binv = 1.0f / ha;
-        const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
-        const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
-        best_depth = clamp_hlsl(iz / iw, -1.0f, 1.0f);
-        bb0 = clamp_hlsl(a0 * binv, 0.0f, 1.0f);
-        bb1 = clamp_hlsl(a1 * binv, 0.0f, 1.0f);
-    }
-    v.raster[pix] = make_float4(bb0, bb1, best_depth, (float)best_tri);
-    if (kDeriv) {
-        const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
-        const float da0_dx = -p1.w * p2.y + p2.w * p1.y;
-        const float da0_dy = -p1.x * p2.w + p1.w * p2.x;
-        const float da1_dx = -p2.w * p0.y + p2.y * p0.w;
-        const float da1_dy = -p2.x * p0.w + p2.w * p0.x;
-        const float da2_dx = -p0.w * p1.y + p0.y * p1.w;
-        const float da2_dy = -p0.x * p1.w + p0.w * p1.x;
-        const float dadx = da0_dx + da1_dx + da2_dx;
-        const float dady = da0_dy + da1_dy + da2_dy;
-        v.deriv[pix] = make_float4((da0_dx - bb0 * dadx) * binv * 2.0f / vp.z, (da0_dy - bb0 * dady) * binv * 2.0f / vp.w,
-                                   (da1_dx - bb1 * dadx) * binv * 2.0f / vp.z, (da1_dy - bb1 * dady) * binv * 2.0f / vp.w);
-    }
+    const float4 p0 = clip[vi.x], p1 = clip[vi.y], p2 = clip[vi.z];
+    const WinnerBary wb = winner_barycentrics(p0, p1, p2, sx, sy);
+    const float bb0 = wb.b0, bb1 = wb.b1;
+    v.raster[pix] = make_float4(bb0, bb1, wb.depth, (float)best_tri);
+    if (kDeriv) v.deriv[pix] = winner_derivatives(p0, p1, p2, wb, vp);
     if (kShade) {
         // interpolate_forward.hlsl for the winner (id <= T and indices < V hold here), then
         // texture_forward.hlsl at the interpolated uv: the same arithmetic as the separate kernels.

@@ -23,6 +23,7 @@ from . import _native
 CULL_MODES = {"none": 0, "back": 1, "front": 2}
 ADDRESS_MODES = {"clamp": 0, "wrap": 1, "mirror": 2}
 TILE = 16
+NEAR_MAX_TRIANGLES = 8388608  # PDR_NEAR_MAX_TRIANGLES: ids of the clipped mesh (2 T) stay exact in fp32
 
 
 def parse_cull_mode(value: str) -> int:
@@ -226,8 +227,11 @@ class Rasterizer:
 
     # -- rasterize ----------------------------------------------------------------------------
     def forward(self, positions, indices, resolution, cull_mode: str = "none",
-                output_barycentric_derivatives: bool = True, viewport=None):
-        """Rasterizer::forward (src/rasterizer.cpp:373-442). resolution is (height, width)."""
+                output_barycentric_derivatives: bool = True, viewport=None, *, clip_near_plane: bool = False):
+        """Rasterizer::forward (src/rasterizer.cpp:373-442). resolution is (height, width).
+        clip_near_plane clips triangles against the near plane z = -w first (the reference has no
+        clipping: it drops triangles with a vertex at w <= 1e-8, README.md:140); ids, barycentrics,
+        depth and derivatives stay those of the original triangles."""
         with self.context.lock:
             ctx = self.context
             cull = parse_cull_mode(cull_mode)
@@ -240,22 +244,39 @@ class Rasterizer:
             if h <= 0 or w <= 0:
                 raise ValueError("Rasterization width and height must be positive")
             vps, _ = _viewports(viewport, views, w, h, ctx.device)
-            offsets, lst, capacity, _ = self._bin(clip, idx, w, h, vps)
             raster = torch.empty((views, h, w, 4), dtype=torch.float32, device=ctx.device)
             deriv = torch.empty((views, h, w, 4), dtype=torch.float32, device=ctx.device) \
                 if output_barycentric_derivatives else None
-            _native.call("pdr_rasterize_forward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h, _ptr(vps), cull,
-                         _ptr(offsets), _ptr(lst), capacity, _ptr(raster), _ptr(deriv), ctx.stream())
+            if clip_near_plane:
+                T = idx.shape[0]
+                if T > NEAR_MAX_TRIANGLES:
+                    raise OverflowError("near-plane clipping supports at most 8388608 triangles")
+                cpos = torch.empty((views, 4 * T, 4), dtype=torch.float32, device=ctx.device)
+                cidx = torch.empty((2 * T, 3), dtype=torch.int32, device=ctx.device)
+                _native.call("pdr_clip_near", _ptr(clip), views, V, _ptr(idx), T, _ptr(cpos), _ptr(cidx), None,
+                             ctx.stream())
+                offsets, lst, capacity, _ = self._bin(cpos, cidx, w, h, vps)
+                _native.call("pdr_rasterize_forward", _ptr(cpos), views, 4 * T, _ptr(cidx), 2 * T, w, h, _ptr(vps),
+                             cull, _ptr(offsets), _ptr(lst), capacity, _ptr(raster), _ptr(deriv), ctx.stream())
+                _native.call("pdr_remap_near", _ptr(clip), views, V, _ptr(idx), T, w, h, _ptr(vps), _ptr(raster),
+                             _ptr(deriv), ctx.stream())
+            else:
+                offsets, lst, capacity, _ = self._bin(clip, idx, w, h, vps)
+                _native.call("pdr_rasterize_forward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h, _ptr(vps),
+                             cull, _ptr(offsets), _ptr(lst), capacity, _ptr(raster), _ptr(deriv), ctx.stream())
             if deriv is None:
                 deriv = torch.empty((views, 0, 0, 4), dtype=torch.float32, device=ctx.device)
             if not batched:
                 raster, deriv = raster[0], deriv[0]
             return io.out(raster), io.out(deriv)
 
-    def backward(self, positions, indices, raster, grad_raster, viewport=None, *, grad_barycentric_derivatives=None):
+    def backward(self, positions, indices, raster, grad_raster, viewport=None, *, grad_barycentric_derivatives=None,
+                 clip_near_plane: bool = False):
         """Rasterizer::backward (src/rasterizer.cpp:444-537); returns d loss / d clip positions.
         grad_barycentric_derivatives ([H, W, 4], like the forward's derivative output) adds the gradient
-        through the pixel derivatives, which the reference rejects (src/rasterizer.cpp:459-462)."""
+        through the pixel derivatives, which the reference rejects (src/rasterizer.cpp:459-462).
+        clip_near_plane is the adjoint of forward(..., clip_near_plane=True): triangles with a vertex at
+        w <= 1e-8 pass gradient on every pixel they own."""
         with self.context.lock:
             ctx = self.context
             io = _Io(ctx, positions, indices, raster, grad_raster)
@@ -274,14 +295,19 @@ class Rasterizer:
             h, w = r.shape[1], r.shape[2]
             vps, _ = _viewports(viewport, views, w, h, ctx.device)
             out = torch.empty((views, V, 4), dtype=torch.float32, device=ctx.device)
-            if grad_barycentric_derivatives is None:
-                _native.call("pdr_rasterize_backward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h,
-                             _ptr(vps), _ptr(r), _ptr(g), _ptr(out), ctx.stream())
-            else:
+            gd = None
+            if grad_barycentric_derivatives is not None:
                 gd = io.f32(grad_barycentric_derivatives, "grad_barycentric_derivatives")
                 gd = gd.unsqueeze(0) if gd.ndim == 3 else gd
                 if gd.shape != r.shape:
                     raise ValueError("grad_barycentric_derivatives must have shape [height, width, 4]")
+            if clip_near_plane:
+                _native.call("pdr_rasterize_backward_near", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h,
+                             _ptr(vps), _ptr(r), _ptr(g), _ptr(gd), _ptr(out), ctx.stream())
+            elif gd is None:
+                _native.call("pdr_rasterize_backward", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w, h,
+                             _ptr(vps), _ptr(r), _ptr(g), _ptr(out), ctx.stream())
+            else:
                 _native.call("pdr_rasterize_backward_derivatives", _ptr(clip), views, V, _ptr(idx), idx.shape[0], w,
                              h, _ptr(vps), _ptr(r), _ptr(g), _ptr(gd), _ptr(out), ctx.stream())
             return io.out(out if batched else out[0])

@@ -26,14 +26,16 @@ def _rasterizer_for(device_index: int, enable_validation: bool) -> Rasterizer:
 class _RasterizeFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, positions, indices, resolution, rasterizer, cull_mode, output_barycentric_derivatives, viewport,
-                recompute, differentiable_derivatives=False):
+                recompute, differentiable_derivatives=False, clip_near_plane=False):
         if positions.dtype != torch.float32 or positions.ndim not in (2, 3) or positions.shape[-1] != 4:
             raise ValueError("positions must be a float32 tensor with shape [vertex_count, 4]")
         if indices.ndim != 2 or indices.shape[1] != 3:
             raise ValueError("indices must have shape [triangle_count, 3]")
         raster, derivatives = rasterizer.forward(positions.detach(), indices.detach(), resolution, cull_mode,
-                                                 output_barycentric_derivatives, viewport)
+                                                 output_barycentric_derivatives, viewport,
+                                                 clip_near_plane=clip_near_plane)
         ctx.rasterizer = rasterizer
+        ctx.clip_near_plane = clip_near_plane
         ctx.viewport = viewport
         ctx.resolution = resolution
         ctx.cull_mode = cull_mode
@@ -51,18 +53,20 @@ class _RasterizeFunction(torch.autograd.Function):
     def backward(ctx, grad_raster, grad_derivatives):
         use_deriv = ctx.differentiable_derivatives and grad_derivatives is not None
         if grad_raster is None and not use_deriv:
-            return (None,) * 9
+            return (None,) * 10
         if ctx.recompute:
             positions, indices = ctx.saved_tensors
-            raster, _ = ctx.rasterizer.forward(positions, indices, ctx.resolution, ctx.cull_mode, False, ctx.viewport)
+            raster, _ = ctx.rasterizer.forward(positions, indices, ctx.resolution, ctx.cull_mode, False, ctx.viewport,
+                                               clip_near_plane=ctx.clip_near_plane)
         else:
             positions, indices, raster = ctx.saved_tensors
         if grad_raster is None:
             grad_raster = torch.zeros_like(raster)
         grad_positions = ctx.rasterizer.backward(
             positions, indices, raster, grad_raster.contiguous(), ctx.viewport,
-            grad_barycentric_derivatives=grad_derivatives.contiguous() if use_deriv else None)
-        return grad_positions, None, None, None, None, None, None, None, None
+            grad_barycentric_derivatives=grad_derivatives.contiguous() if use_deriv else None,
+            clip_near_plane=ctx.clip_near_plane)
+        return grad_positions, None, None, None, None, None, None, None, None, None
 
 
 class _InterpolateFunction(torch.autograd.Function):
@@ -120,13 +124,16 @@ def rasterize(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequen
               rasterizer: Optional[Rasterizer] = None, device_index: int = 0, enable_validation: bool = False,
               cull_mode: str = "none", output_barycentric_derivatives: bool = True,
               viewport: Optional[Sequence[float]] = None, recompute_in_backward: bool = False,
-              differentiable_derivatives: bool = False) -> Tuple[torch.Tensor, torch.Tensor]:
+              differentiable_derivatives: bool = False,
+              clip_near_plane: bool = False) -> Tuple[torch.Tensor, torch.Tensor]:
     """Rasterize clip-space vertices and connect the output to autograd (torch.py:181-216).
 
     Resolution uses ``(height, width)`` order. ``recompute_in_backward`` keeps only positions and
     indices for the backward pass and rasterizes again there, instead of holding the raster.
     ``differentiable_derivatives`` makes the barycentric derivative output differentiable (its gradient
-    reaches the positions); by default it is a constant, as in the reference."""
+    reaches the positions); by default it is a constant, as in the reference. ``clip_near_plane`` clips
+    triangles against the near plane before rasterizing (the reference drops triangles with a vertex at
+    w <= 1e-8 instead); outputs and gradients refer to the original triangles."""
     if len(resolution) != 2 or int(resolution[0]) <= 0 or int(resolution[1]) <= 0:
         raise ValueError("resolution must be (height, width) with positive values")
     active = rasterizer or _rasterizer_for(device_index, enable_validation)
@@ -138,7 +145,7 @@ def rasterize(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequen
             normalized_viewport = [None if v is None else tuple(float(x) for x in v) for v in viewport]
     return _RasterizeFunction.apply(positions, indices, (int(resolution[0]), int(resolution[1])), active, cull_mode,
                                     output_barycentric_derivatives, normalized_viewport, recompute_in_backward,
-                                    differentiable_derivatives)
+                                    differentiable_derivatives, clip_near_plane)
 
 
 def interpolate(vertex_attributes: torch.Tensor, raster: torch.Tensor, indices: torch.Tensor, *,
