@@ -2,10 +2,12 @@
 // optional shading epilogue; shared by the per-mesh launch (raster.cu) and the uneven multi-mesh
 // batch (batch.cu). The kernel that calls raster_tile must run TW * TH threads.
 //
-// Per tile: the tile's triangles are staged in shared memory (structure of arrays) CHUNK at a time.
-// Each warp owns an 8x4 pixel region and, per group of 32 staged triangles:
-//   1. cull: every lane takes one triangle and decides whether any pixel of the region can pass its
-//      edge tests (rigorous bound, edge_rejects_region);
+// Per tile: the tile's triangles are staged in shared memory (structure of arrays) CHUNK at a time,
+// each with the rectangle of tile pixels whose samples can pass its edge tests (pixel_rect, a rigorous
+// bound). Each warp owns an 8x4 pixel region and, per group of 32 staged triangles:
+//   1. cull: every lane takes one triangle and keeps it when its rectangle meets the region (a triangle
+//      the bound does not cover is kept unless the rigorous region test below, edge_rejects_region,
+//      proves that no pixel of the region passes its edge tests);
 //   2. coverage: for each surviving triangle, every lane runs the edge tests for its pixel, and the
 //      passing (triangle, pixel) pairs are appended to a per-warp queue;
 //   3. depth: whenever 32 pairs are queued, each lane takes one pair, computes its depth with the
@@ -59,8 +61,54 @@ template <int CHUNK>
 struct TileStage {
     float s0x[CHUNK], s0y[CHUNK], s1x[CHUNK], s1y[CHUNK], s2x[CHUNK], s2y[CHUNK], sign[CHUNK];
     uint32_t t[CHUNK];
+    uint32_t rect[CHUNK];  // candidate rectangle (x0 | x1 << 8 | y0 << 16 | y1 << 24, tile-local), or below
     float4 p0[CHUNK], p1[CHUNK], p2[CHUNK];
 };
+
+constexpr uint32_t kRectNone = 0xFFFFFFFEu;   // no pixel of the tile can pass: nothing to do
+constexpr uint32_t kRectLarge = 0xFFFFFFFFu;  // the bound does not apply: region cull
+
+// The pixels of tile [x_org, x_org + TW) x [y_org, y_org + TH) (clipped to the image) whose samples can pass
+// all three of the reference's edge tests fl(e) * sign >= -1e-7, as a rectangle, or kRectLarge when the
+// bound below does not apply, or kRectNone when it is empty.
+// Bound: let L bound |a - s| over vertices a and the tile's samples s. The fp32 edge value differs from the
+// exact one by at most 4u(|AB| + |CD|) <= 8u L^2 (u = 2^-24), so a sample passing the fp32 test satisfies
+// the exact test e * sign >= -tau, tau = 1e-7 + 2e-6 L^2; such samples lie in the triangle with every edge
+// moved out by tau / |edge|, whose vertices move by at most tau (|e_a| + |e_b|) / |cross| <= tau P / |area|
+// (P the perimeter, area = the cross product the reference computes). D = 2 tau P / |area| bounds that
+// with room for the rounding of P and of area (at most 0.6% when |area| >= 1e-4 ext^2, required), so
+// every passing sample lies in the vertex bounding box grown by D. Pixel indices come from inverting
+// sample_ndc with 0.05 pixel (plus 1e-6 of the viewport size) of slack for its rounding.
+__device__ __forceinline__ uint32_t pixel_rect(float s0x, float s0y, float s1x, float s1y, float s2x, float s2y,
+                                               float area, float4 vp, uint32_t x_org, uint32_t y_org, uint32_t x_end,
+                                               uint32_t y_end, float tsx_lo, float tsx_hi, float tsy_lo,
+                                               float tsy_hi) {
+    const float mnx = fminf(s0x, fminf(s1x, s2x)), mxx = fmaxf(s0x, fmaxf(s1x, s2x));
+    const float mny = fminf(s0y, fminf(s1y, s2y)), mxy = fmaxf(s0y, fmaxf(s1y, s2y));
+    const float pxw = 2.0f / vp.z, pyw = 2.0f / vp.w;  // one pixel in NDC
+    const float ext = fmaxf(mxx - mnx, mxy - mny);
+    // |a - s| over vertices and tile samples (tile sample ranges [tsx_lo, tsx_hi] x [tsy_lo, tsy_hi]), 1% up
+    const float L = 1.01f * fmaxf(fmaxf(fabsf(mxx - tsx_lo), fabsf(tsx_hi - mnx)),
+                                  fmaxf(fabsf(mxy - tsy_lo), fabsf(tsy_hi - mny)));
+    const float perim = fabsf(s1x - s0x) + fabsf(s1y - s0y) + fabsf(s2x - s1x) + fabsf(s2y - s1y) +
+                        fabsf(s0x - s2x) + fabsf(s0y - s2y);
+    const float tau = 1e-7f + 2e-6f * L * L;
+    const float D = 2.0f * tau * perim / fabsf(area);
+    // NaN-safe: every comparison with a NaN fails and sends the triangle to the warp path
+    if (!(D <= fminf(pxw, pyw)) || !(fabsf(area) >= 1e-4f * ext * ext)) return kRectLarge;
+    const float slx = 0.05f + 1e-6f * (vp.z + fabsf(vp.x)), sly = 0.05f + 1e-6f * (vp.w + fabsf(vp.y));
+    // p = (s + 1) * size / 2 + origin - 0.5 inverts sample_ndc
+    const float fx0 = ceilf(((mnx - D) + 1.0f) * 0.5f * vp.z + vp.x - 0.5f - slx);
+    const float fx1 = floorf(((mxx + D) + 1.0f) * 0.5f * vp.z + vp.x - 0.5f + slx);
+    const float fy0 = ceilf(((mny - D) + 1.0f) * 0.5f * vp.w + vp.y - 0.5f - sly);
+    const float fy1 = floorf(((mxy + D) + 1.0f) * 0.5f * vp.w + vp.y - 0.5f + sly);
+    const float cx0 = fmaxf(fx0, (float)x_org), cx1 = fminf(fx1, (float)(x_end - 1u));
+    const float cy0 = fmaxf(fy0, (float)y_org), cy1 = fminf(fy1, (float)(y_end - 1u));
+    if (!(cx0 <= cx1) || !(cy0 <= cy1)) return kRectNone;
+    const uint32_t x0 = (uint32_t)cx0 - x_org, x1 = (uint32_t)cx1 - x_org;
+    const uint32_t y0 = (uint32_t)cy0 - y_org, y1 = (uint32_t)cy1 - y_org;
+    return x0 | (x1 << 8) | (y0 << 16) | (y1 << 24);
+}
 
 // true when fl(cross(a - s, b - s)) * sign < -1e-7 holds for every sample s of the region box
 __device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx, float by, float sign, float sx_lo,
@@ -139,6 +187,7 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
     // the nearest depth, ties to the lowest id, exactly the reference's sequential test.
     __shared__ unsigned long long best_key[kThreads];
     __shared__ uint32_t queue[kWarps][64];  // per warp: (triangle slot << 5) | pixel lane
+    __shared__ float tile_sx[TW], tile_sy[TH];  // sample positions of the tile's columns and rows
 
     const float4* __restrict__ clip = v.clip;
     const uint3* __restrict__ idx = v.idx;
@@ -155,12 +204,18 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
     uint32_t* q = queue[warp];
     best_key[threadIdx.x] = ~0ull;
     const bool in_image = px < v.W && py < v.H;
+    const uint32_t reg_x = (warp % kRegionsX) * 8u, reg_y = (warp / kRegionsX) * 4u;  // region in the tile
+    const uint32_t x_org = tx * TW, y_org = ty * TH;
+    const uint32_t x_end = min(x_org + (uint32_t)TW, v.W), y_end = min(y_org + (uint32_t)TH, v.H);
+    if (threadIdx.x < (uint32_t)TW) tile_sx[threadIdx.x] = sample_ndc(x_org + threadIdx.x, vp.x, vp.z);
+    if (threadIdx.x < (uint32_t)TH) tile_sy[threadIdx.x] = sample_ndc(y_org + threadIdx.x, vp.y, vp.w);
     for (uint32_t chunk = b; chunk < e; chunk += CHUNK) {
         __syncthreads();
         const uint32_t i = chunk + threadIdx.x;
         if (threadIdx.x < (uint32_t)CHUNK && i < e) {
             const uint32_t t = list[i];
             float sgn = 0.0f;
+            uint32_t rect = kRectNone;
             float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
             float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f, s2x = 0.f, s2y = 0.f;
             const uint3 vi = idx[t];
@@ -168,6 +223,10 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                 p0 = clip[vi.x];
                 p1 = clip[vi.y];
                 p2 = clip[vi.z];
+            }
+            tri.t[threadIdx.x] = t;
+            tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
+            if (vi.x < v.V && vi.y < v.V && vi.z < v.V) {
                 if (!(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f)) {
                     s0x = p0.x / p0.w; s0y = p0.y / p0.w;
                     s1x = p1.x / p1.w; s1y = p1.y / p1.w;
@@ -175,15 +234,19 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                     const float area = cross2(s1x - s0x, s1y - s0y, s2x - s0x, s2y - s0y);
                     const bool skip = fabsf(area) <= 1e-12f || (v.cull == 1 && area <= 0.0f) ||
                                       (v.cull == 2 && area >= 0.0f);
-                    if (!skip) sgn = area > 0.0f ? 1.0f : -1.0f;
+                    if (!skip) {
+                        sgn = area > 0.0f ? 1.0f : -1.0f;
+                        rect = pixel_rect(s0x, s0y, s1x, s1y, s2x, s2y, area, vp, x_org, y_org, x_end, y_end,
+                                          tile_sx[0], tile_sx[x_end - x_org - 1u], tile_sy[0],
+                                          tile_sy[y_end - y_org - 1u]);
+                    }
                 }
             }
             tri.s0x[threadIdx.x] = s0x; tri.s0y[threadIdx.x] = s0y;
             tri.s1x[threadIdx.x] = s1x; tri.s1y[threadIdx.x] = s1y;
             tri.s2x[threadIdx.x] = s2x; tri.s2y[threadIdx.x] = s2y;
             tri.sign[threadIdx.x] = sgn;
-            tri.t[threadIdx.x] = t;
-            tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
+            tri.rect[threadIdx.x] = rect;
         }
         __syncthreads();
         const uint32_t n = min(e - chunk, (uint32_t)CHUNK);
@@ -216,8 +279,13 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
             const uint32_t j = g + lane;
             bool maybe = false;
             if (j < n) {
-                const float sgn = tri.sign[j];
-                if (sgn != 0.0f) {
+                const uint32_t rc = tri.rect[j];
+                if (rc < kRectNone) {
+                    // the triangle's candidate rectangle meets the region
+                    maybe = (rc & 0xFFu) <= reg_x + 7u && ((rc >> 8) & 0xFFu) >= reg_x &&
+                            ((rc >> 16) & 0xFFu) <= reg_y + 3u && (rc >> 24) >= reg_y;
+                } else if (rc == kRectLarge) {
+                    const float sgn = tri.sign[j];
                     const float ax0 = tri.s0x[j], ay0 = tri.s0y[j], ax1 = tri.s1x[j], ay1 = tri.s1y[j];
                     const float ax2 = tri.s2x[j], ay2 = tri.s2y[j];
                     maybe = !(edge_rejects_region(ax1, ay1, ax2, ay2, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
