@@ -635,7 +635,7 @@ STAGES = ["bin_tiles", "rasterize_forward+shade", "render_backward"]
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the two fused kernels on this
 # 64-view workload, from a single-pass ncu capture of the full-size run (the capture cannot run inside
 # the timed region; it is re-taken whenever these kernels change).
-KERNEL_TRAFFIC = {"rasterize_forward+shade": 2132001061 + 4508806693, "render_backward": 6810716197 + 1586401207}
+KERNEL_TRAFFIC = {"rasterize_forward+shade": 2160528713 + 4589287790, "render_backward": 6810716197 + 1586401207}
 
 
 def stage_bytes(w, T, V, entries):

@@ -99,6 +99,44 @@ def test_large_tiles_sorted(rast):
         assert same_bits(raster, api.rasterize_forward(pos, idx, res)[0])
 
 
+def edge_case_triangles(seed=11):
+    """Triangles that stress the forward's per-triangle candidate rectangle: microscopic ones (whose
+    1e-7 edge tolerance reaches pixels beyond their bounding box), slivers, triangles with a far
+    vertex, triangles with vertices on pixel centres and tile borders, and near-degenerate ones."""
+    rng = np.random.default_rng(seed)
+    tris = []
+    for size in (1e-7, 1e-5, 1e-3, 3e-2):  # NDC
+        c = rng.uniform(-0.95, 0.95, size=(150, 1, 2))
+        tris.append(c + rng.normal(scale=size, size=(150, 3, 2)))
+    a = rng.uniform(-0.9, 0.9, size=(150, 2))
+    d = rng.normal(size=(150, 2))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    n = np.stack([-d[:, 1], d[:, 0]], 1)
+    length = rng.uniform(0.05, 0.5, size=(150, 1))
+    for width in (1e-6, 1e-4):  # slivers
+        tris.append(np.stack([a, a + d * length, a + d * length * 0.5 + n * width], 1))
+    far = rng.uniform(-0.9, 0.9, size=(150, 3, 2))
+    far[:, 0] = rng.uniform(-1e3, 1e3, size=(150, 2))
+    tris.append(far)
+    grid = (np.arange(-8, 9) / 8.0)  # pixel centres and tile borders of a 64x64 image lie on this lattice
+    tris.append(rng.choice(grid, size=(150, 3, 2)))
+    xy = np.concatenate(tris).astype(np.float32)
+    T = xy.shape[0]
+    w = rng.uniform(0.5, 2.0, size=(T, 3, 1)).astype(np.float32)
+    z = rng.uniform(-0.9, 0.9, size=(T, 3, 1)).astype(np.float32)
+    pos = np.concatenate([xy * w, z * w, w], 2).reshape(-1, 4).astype(np.float32)
+    return pos, np.arange(3 * T, dtype=np.uint32).reshape(T, 3)
+
+
+@pytest.mark.parametrize("cull", ["none", "back"])
+def test_candidate_rectangle_edge_cases(rast, cull):
+    pos, idx = edge_case_triangles()
+    for res, vp in [((64, 64), None), ((61, 70), (-3.0, 2.0, 75.0, 58.0)), ((40, 48), (1000.5, -700.25, 8192.0, 4096.0))]:
+        raster, deriv = rast.forward(pos, idx, res, cull_mode=cull, viewport=vp)
+        o_r, o_d = api.rasterize_forward(pos, idx, res, cull_mode={"none": 0, "back": 1}[cull], viewport=vp)
+        assert same_bits(raster, o_r) and same_bits(deriv, o_d), (res, vp)
+
+
 def test_backward_chain_vs_oracle(rast):
     rng = np.random.default_rng(2)
     pos3, idx, clip, uvv = sphere_scene(views=2)
