@@ -827,6 +827,20 @@ def run_gpu(args, world, rank, local):
         except Exception as e:  # the CPU leg never hides a GPU result
             cpu = {"value": None, "unit": "Mpix/s", "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"failed: {e}"}
+    # ---- parity of view 0 at full size: the GPU raster against the oracle, with the tie counts ----------
+    parity = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        try:
+            from oracle import api
+
+            clip0 = clip[0].cpu().numpy()
+            o_r, _, counts = api.rasterize_tie_counts(clip0, idx, (H, W))
+            g_r = pipe.raster[0].cpu().numpy()
+            parity = {"view": 0, "raster_bit_exact": bool(np.array_equal(o_r.view(np.uint32), g_r.view(np.uint32))),
+                      **counts, "note": "depth_ties: pixels the lowest-id rule decided; edge_ties: pixels whose "
+                                        "winner passed an edge test inside the 1e-7 tolerance"}
+        except Exception as e:
+            parity = {"view": 0, "failed": str(e)}
 
     if rank == 0:
         line = {
@@ -853,6 +867,7 @@ def run_gpu(args, world, rank, local):
                            "pinned host memory every step (double-buffered on a copy stream), gradients read back "
                            "on a third stream"},
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clocks.summary(),
         }
         if world == 1:

@@ -104,6 +104,23 @@ def rasterize_forward(pos, idx, resolution, cull_mode=0, output_derivatives=True
     return raster, deriv
 
 
+def rasterize_tie_counts(pos, idx, resolution, cull_mode=0, viewport=None):
+    """How the reference's rasterizer decided each covered pixel: returns (raster, ties [H, W] u8, counts)
+    with counts = {"covered", "depth_ties", "edge_ties"}: pixels where another covering triangle had
+    the winner's depth (the lowest-id rule decided) and pixels whose winner passed an edge test only on
+    the edge or inside the 1e-7 tolerance."""
+    pos, idx = _f(pos), _u(idx)
+    h, w = resolution
+    vp = _vp(viewport, w, h)
+    raster = np.zeros((h, w, 4), dtype=np.float32)
+    ties = np.zeros((h, w), dtype=np.uint8)
+    _check(lib().ora_rasterize_forward_ties(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, cull_mode,
+                                            _p(vp), _p(raster), _p(ties, _u8p)))
+    counts = {"covered": int(np.count_nonzero(raster[..., 3])), "depth_ties": int(np.count_nonzero(ties & 1)),
+              "edge_ties": int(np.count_nonzero(ties & 2))}
+    return raster, ties, counts
+
+
 def rasterize_forward_f64(pos, idx, raster, viewport=None):
     pos, idx, raster = _f(pos), _u(idx), _f(raster)
     h, w = raster.shape[:2]

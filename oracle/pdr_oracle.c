@@ -158,9 +158,12 @@ static int validate_mesh(const float* pos, uint32_t V, const uint32_t* idx, uint
     return ORA_OK;
 }
 
-int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
-                          uint32_t W, uint32_t H, uint32_t cull_mode, int out_deriv,
-                          const float vp[4], float* raster, float* deriv) {
+/* ties (optional, one byte per pixel): ORA_TIE_DEPTH when another covering triangle had the winner's
+ * depth, so the lowest-id rule decided the pixel; ORA_TIE_EDGE when the winner passed one of its edge
+ * tests only on the edge or inside the 1e-7 tolerance (e * sign <= 0). */
+static int raster_forward_impl(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                               uint32_t W, uint32_t H, uint32_t cull_mode, int out_deriv,
+                               const float vp[4], float* raster, float* deriv, uint8_t* ties) {
     int rc = validate_mesh(pos, V, idx, T);
     if (rc) return rc;
     if (W == 0 || H == 0) return ORA_INVALID;
@@ -182,6 +185,7 @@ int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uin
             const float sy = sample_ndc((uint32_t)py, vp[1], vp[3]);
             float best_depth = 3.402823466e+38f;
             uint32_t best_tri = 0;
+            int depth_tie = 0, edge_tie = 0;
             float bb0 = 0.0f, bb1 = 0.0f;
             float bd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             const uint64_t tile = ((uint64_t)py / TILE) * tcx + px / TILE;
@@ -220,7 +224,13 @@ int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uin
                 const float iw = p0[3] * a0 + p1[3] * a1 + p2[3] * a2;
                 if (fabsf(iw) <= 1e-12f) continue;
                 const float depth = clampf_hlsl(iz / iw, -1.0f, 1.0f);
-                if (depth > best_depth || (depth == best_depth && best_tri != 0 && t + 1 >= best_tri)) continue;
+                const int same_depth = depth == best_depth && best_tri != 0;
+                if (depth > best_depth || (same_depth && t + 1 >= best_tri)) {
+                    depth_tie |= same_depth;
+                    continue;
+                }
+                depth_tie = same_depth;
+                edge_tie = e0 * sign <= 0.0f || e1 * sign <= 0.0f || e2 * sign <= 0.0f;
                 best_depth = depth;
                 best_tri = t + 1;
                 bb0 = b0;
@@ -240,6 +250,7 @@ int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uin
                     bd[3] = (da1_dy - b1 * dady) * inv * 2.0f / vp[3];
                 }
             }
+            if (ties) ties[pixel] = (uint8_t)(best_tri != 0 ? (depth_tie ? ORA_TIE_DEPTH : 0) | (edge_tie ? ORA_TIE_EDGE : 0) : 0);
             float* r = raster + pixel * 4;
             if (best_tri == 0) {
                 r[0] = r[1] = r[2] = r[3] = 0.0f;
@@ -261,6 +272,18 @@ int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uin
     free(list);
     free(offsets);
     return ORA_OK;
+}
+
+int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                          uint32_t W, uint32_t H, uint32_t cull_mode, int out_deriv,
+                          const float vp[4], float* raster, float* deriv) {
+    return raster_forward_impl(pos, V, idx, T, W, H, cull_mode, out_deriv, vp, raster, deriv, NULL);
+}
+
+int ora_rasterize_forward_ties(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                               uint32_t W, uint32_t H, uint32_t cull_mode, const float vp[4], float* raster,
+                               uint8_t* ties) {
+    return raster_forward_impl(pos, V, idx, T, W, H, cull_mode, 0, vp, raster, NULL, ties);
 }
 
 /* FP64 twin: same formulas in double for the triangle the fp32 pass selected. */

@@ -39,6 +39,15 @@ int ora_rasterize_forward(const float* pos, uint32_t V, const uint32_t* idx, uin
                           int output_derivatives, const float viewport[4],
                           float* raster, float* derivatives);
 
+/* ora_rasterize_forward (no derivatives) that also flags, per pixel, how the winner was decided:
+ * ORA_TIE_DEPTH when another covering triangle had the same depth (the lowest-id rule decided),
+ * ORA_TIE_EDGE when the winner's sample lies on one of its edges or inside the 1e-7 tolerance. */
+#define ORA_TIE_DEPTH 1
+#define ORA_TIE_EDGE 2
+int ora_rasterize_forward_ties(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
+                               uint32_t width, uint32_t height, uint32_t cull_mode, const float viewport[4],
+                               float* raster, uint8_t* ties);
+
 /* FP64 twin of the barycentric/derivative arithmetic for the fp32 winners in raster. */
 int ora_rasterize_forward_f64(const float* pos, uint32_t V, const uint32_t* idx, uint32_t T,
                               uint32_t width, uint32_t height, const float viewport[4],

@@ -12,6 +12,7 @@ import torch
 from oracle import api
 from photara_drender_gb300 import synthetic as S
 from tests.gpu_util import grad_check, same_bits
+from tests.raster_scenes import tie_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -126,6 +127,20 @@ def edge_case_triangles(seed=11):
     z = rng.uniform(-0.9, 0.9, size=(T, 3, 1)).astype(np.float32)
     pos = np.concatenate([xy * w, z * w, w], 2).reshape(-1, 4).astype(np.float32)
     return pos, np.arange(3 * T, dtype=np.uint32).reshape(T, 3)
+
+
+def test_tie_rules_counted(rast):
+    """Edge ties (samples on an edge, inside the 1e-7 tolerance) and depth ties (the lowest-id rule) are
+    counted by the oracle and decided identically on the GPU."""
+    pos, idx, res = tie_scene()
+    _, _, counts = api.rasterize_tie_counts(pos, idx, res)
+    assert counts["depth_ties"] > 0 and counts["edge_ties"] > 0, counts
+    raster, _ = rast.forward(pos, idx, res)
+    assert same_bits(raster, api.rasterize_forward(pos, idx, res)[0])
+    apos, aidx = adversarial_scene()
+    _, _, acounts = api.rasterize_tie_counts(apos, aidx, (40, 36))
+    assert acounts["depth_ties"] > 0
+    print(f"tie counts: grid {counts}, adversarial {acounts}")
 
 
 @pytest.mark.parametrize("cull", ["none", "back"])

@@ -6,6 +6,7 @@ import pytest
 
 from oracle import api, ref_api
 from photara_drender_gb300 import synthetic as S
+from tests.raster_scenes import tie_scene
 
 pytestmark = pytest.mark.skipif(not ref_api.available(), reason="reference sources not available")
 
@@ -48,6 +49,19 @@ def test_raster_adversarial(case, cull):
         g = np.random.default_rng(1).normal(size=r1.shape).astype(np.float32)
         assert same_bits(api.rasterize_backward(pos, idx, r1, g, viewport=vp),
                          ref_api.rasterize_backward(pos, idx, r1, g, viewport=vp))
+
+
+def test_tie_decisions_match_reference():
+    """Pixels decided by the edge tolerance or by the lowest-id depth rule (counted by the oracle) come
+    out the same in the reference's own shader code: a coplanar pixel-centre grid drawn twice."""
+    pos, idx, res = tie_scene()
+    r1, ties, counts = api.rasterize_tie_counts(pos, idx, res)
+    r2, _ = ref_api.rasterize_forward(pos, idx, res)
+    assert same_bits(r1, r2)
+    assert counts["depth_ties"] > 0 and counts["edge_ties"] > 0
+    # the lowest-id rule: every depth-tied pixel of the duplicated grid shows the first copy
+    ids = np.rint(r1[..., 3]).astype(np.int64)
+    assert (ids[(ties & 1) > 0] <= idx.shape[0] // 2).all()
 
 
 @pytest.mark.parametrize("view", range(3))
