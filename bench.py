@@ -855,7 +855,7 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": pipe.kernels_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": KERNEL_TRAFFIC.get(dom_name) if views == 64 else None,
+                         "traffic": KERNEL_TRAFFIC.get(dom_name) if views == 64 and w["atlas"] == 4096 else None,
                          "algorithmic_bytes": sbytes[dom_name], "ms": float(stage_ms[dom])},
             "stages_ms": {n: float(t) for n, t in zip(STAGES, stage_ms)},
             "pipeline": "fused" if pipe.fused else "separate kernels",
@@ -894,6 +894,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
     ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
     ap.add_argument("--views", type=int, default=None, help="override the view count (small profiling cases)")
+    ap.add_argument("--atlas", type=int, default=None, help="override the atlas size (texture-gradient profiling)")
     ap.add_argument("--skip-c1", action="store_true", help="omit the small-mesh (C1) leg")
     ap.add_argument("--skip-bake", action="store_true", help="omit the bake leg")
     ap.add_argument("--skip-refine", action="store_true", help="omit the refine leg")
@@ -903,6 +904,9 @@ def main():
     if args.views:
         WORKLOAD["views"] = args.views
         WORKLOAD["name"] = WORKLOAD["name"].replace("64x", f"{args.views}x")
+    if args.atlas:
+        WORKLOAD["name"] = WORKLOAD["name"].replace(f"atlas{WORKLOAD['atlas']}", f"atlas{args.atlas}")
+        WORKLOAD["atlas"] = args.atlas
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))

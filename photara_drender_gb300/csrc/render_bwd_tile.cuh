@@ -3,9 +3,9 @@
 // multi-mesh batch (batch.cu). The kernel that calls render_backward_tile runs 256 threads.
 //
 // One thread per pixel runs, in the reference's order and arithmetic, texture_grad_texture
-// (double-exact weights, vector atomics), texture_grad_uv, interpolate_grad_attributes /
-// interpolate_grad_raster for both attribute sets, and rasterize_backward for the summed raster
-// gradient. Per-vertex gradients are summed over each run of adjacent pixels of a warp that hit the
+// (double-exact weights, vector atomics, warp-aggregated for magnified textures), texture_grad_uv,
+// interpolate_grad_attributes / interpolate_grad_raster for both attribute sets, and
+// rasterize_backward for the summed raster gradient. Per-vertex gradients are summed over each run of adjacent pixels of a warp that hit the
 // same triangle (warp shuffles); the run's last lane then adds them to global memory with vector
 // reductions (clip x/y/0/w as one v4, uv as one v2). A per-tile shared-memory table that merged the
 // runs' vertices before one flush was measured slower: its hash probes and shared float atomics cost
@@ -95,7 +95,9 @@ struct BackwardView {
     uint32_t* status;
 };
 
-template <int kA>
+// kTexAgg: texture-gradient taps warp-aggregated (1), plain (0), or decided from the texture and image
+// sizes (-1: aggregated when the texture has fewer texels than the view has pixels).
+template <int kA, int kTexAgg = -1>
 __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint32_t tile_x, uint32_t tile_y) {
     const float4* __restrict__ clip_view = v.clip;
     const uint32_t V = v.V, T = v.T, W = v.W, H = v.H;
@@ -115,6 +117,7 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
     uint32_t* __restrict__ status = v.status;
 
     constexpr uint32_t kNV = 2 + kA + 3;  // per vertex: uv attributes, attributes, clip x/y/w
+    const bool magnified = kTexAgg >= 0 ? kTexAgg == 1 : (uint64_t)tw * th < (uint64_t)W * H;
     float* g_clip = g_clip_view;
     const uint32_t lane = threadIdx.x & 31u;
 
@@ -151,10 +154,10 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
                     const int32_t ys0 = address_coordinate(by, th, mode), ys1 = address_coordinate(by + 1, th, mode);
                     const float w0 = (1.0f - fx) * (1.0f - fy), w1 = fx * (1.0f - fy), w2 = (1.0f - fx) * fy,
                                 w3 = fx * fy;
-                    red_v4(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs0) * 4, make_float4(w0 * gs.x, w0 * gs.y, w0 * gs.z, w0 * gs.w));
-                    red_v4(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs1) * 4, make_float4(w1 * gs.x, w1 * gs.y, w1 * gs.z, w1 * gs.w));
-                    red_v4(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs0) * 4, make_float4(w2 * gs.x, w2 * gs.y, w2 * gs.z, w2 * gs.w));
-                    red_v4(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs1) * 4, make_float4(w3 * gs.x, w3 * gs.y, w3 * gs.z, w3 * gs.w));
+                    red_add_v4_texel(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs0) * 4, make_float4(w0 * gs.x, w0 * gs.y, w0 * gs.z, w0 * gs.w), magnified);
+                    red_add_v4_texel(g_tex + ((size_t)(uint32_t)ys0 * tw + (uint32_t)xs1) * 4, make_float4(w1 * gs.x, w1 * gs.y, w1 * gs.z, w1 * gs.w), magnified);
+                    red_add_v4_texel(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs0) * 4, make_float4(w2 * gs.x, w2 * gs.y, w2 * gs.z, w2 * gs.w), magnified);
+                    red_add_v4_texel(g_tex + ((size_t)(uint32_t)ys1 * tw + (uint32_t)xs1) * 4, make_float4(w3 * gs.x, w3 * gs.y, w3 * gs.z, w3 * gs.w), magnified);
                 }
             }
             // texture_grad_uv (fp32)

@@ -165,11 +165,6 @@ __global__ void texture_forward_kernel(const float* __restrict__ tex_all, size_t
     }
 }
 
-__device__ __forceinline__ void red_add_v4(float* addr, float4 v) {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-                 : "memory");
-}
-
 // grad_texture: pixels with raster.w != 0 scatter weight * grad to their four texels, the
 // weights computed from the double-precision texel position of src/rasterizer.cpp:207-229
 // (reproduced exactly with integer arithmetic). grad_uv follows texture_grad_uv.hlsl in fp32.
@@ -206,7 +201,8 @@ __global__ void texture_backward_kernel(const float* __restrict__ tex_all, size_
                 const float4 gg = reinterpret_cast<const float4*>(grad)[pix];
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
-                    red_add_v4(gt + (size_t)o[k] * 4, make_float4(w[k] * gg.x, w[k] * gg.y, w[k] * gg.z, w[k] * gg.w));
+                    red_add_v4_texel(gt + (size_t)o[k] * 4, make_float4(w[k] * gg.x, w[k] * gg.y, w[k] * gg.z, w[k] * gg.w),
+                                     (size_t)tw * th < P);
             } else {
                 for (int k = 0; k < 4; ++k)
                     for (uint32_t c = 0; c < nc; ++c) atomicAdd(gt + (size_t)o[k] * nc + c, w[k] * g[c]);

@@ -190,6 +190,25 @@ def test_backward_chain_vs_oracle(rast):
                    api.rasterize_backward(clip[k], idx, o_r, g, f64=True, abs_terms=True), name="grad_positions")
 
 
+@pytest.mark.parametrize("tex_hw,res", [((4, 4), (96, 80)), ((2, 3), (64, 64)), ((160, 128), (40, 36))])
+def test_texture_gradient_magnified_and_minified(rast, tex_hw, res):
+    """grad_texture when many pixels of a warp share texels (warp-aggregated reductions) and when they
+    do not (plain reductions), in every address mode, against the float64 oracle."""
+    rng = np.random.default_rng(4)
+    pos3, idx, clip, uvv = sphere_scene(views=1)
+    o_r, _ = api.rasterize_forward(clip[0], idx, res)
+    uv = api.interpolate_forward(uvv, idx, o_r) * 1.7 - 0.35
+    tex = rng.uniform(size=tex_hw + (4,)).astype(np.float32)
+    gs = rng.normal(size=res + (4,)).astype(np.float32)
+    for mode in ("clamp", "wrap", "mirror"):
+        gt, gu = rast.texture_backward(tex, uv, o_r, gs, mode)
+        o_gt, o_gu = api.texture_backward(tex, uv, o_r, gs, mode)
+        o64_gt, _ = api.texture_backward(tex, uv, o_r, gs, mode, f64=True)
+        abs_gt, _ = api.texture_backward(tex, uv, o_r, gs, mode, f64=True, abs_terms=True)
+        assert same_bits(gu, o_gu), f"grad_uv {mode}"
+        grad_check(gt, o_gt, o64_gt, abs_gt, name=f"grad_texture {mode} {tex_hw}")
+
+
 def test_texture_channels_not_four(rast):
     rng = np.random.default_rng(9)
     pos3, idx, clip, uvv = sphere_scene(views=1)
