@@ -827,8 +827,22 @@ def run_gpu(args, world, rank, local):
         except Exception as e:  # the CPU leg never hides a GPU result
             cpu = {"value": None, "unit": "Mpix/s", "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"failed: {e}"}
-    # ---- parity of view 0 at full size: the GPU raster against the oracle, with the tie counts ----------
+    # ---- parity at full size ---------------------------------------------------------------------------
+    # (1) size-independent sums of the last backward: bilinear weights and barycentric weights each sum to
+    # one, so the texture gradient summed over texels equals the sample gradient summed over covered
+    # pixels, and the attribute gradient summed over vertices equals the attribute gradient summed over
+    # covered pixels (errors relative to the sum of |terms|, float64 on the device);
+    # (2) view 0's raster against the oracle at full size, with the tie counts.
     parity = None
+    if rank == 0:
+        cov = (pipe.raster[..., 3] != 0).unsqueeze(-1).double()
+        ref_t, abs_t = (g_samp.double() * cov).sum((0, 1, 2)), (g_samp.double().abs() * cov).sum((0, 1, 2))
+        ids = pipe.raster[..., 3]
+        covv = ((ids >= 0.5) & (ids < T + 0.5)).unsqueeze(-1).double()
+        ref_a, abs_a = (g_attr.double() * covv).sum((0, 1, 2)), (g_attr.double().abs() * covv).sum((0, 1, 2))
+        parity = {"grad_texture_sum_err": float(((pipe.grad_tex.double().sum((0, 1)) - ref_t).abs() / abs_t).max()),
+                  "grad_attribute_sum_err": float(((pipe.grad_attr.double().sum(0) - ref_a).abs() / abs_a).max())}
+        del cov, covv
     if rank == 0 and world == 1 and not args.skip_cpu:
         try:
             from oracle import api
@@ -836,11 +850,14 @@ def run_gpu(args, world, rank, local):
             clip0 = clip[0].cpu().numpy()
             o_r, _, counts = api.rasterize_tie_counts(clip0, idx, (H, W))
             g_r = pipe.raster[0].cpu().numpy()
-            parity = {"view": 0, "raster_bit_exact": bool(np.array_equal(o_r.view(np.uint32), g_r.view(np.uint32))),
-                      **counts, "note": "depth_ties: pixels the lowest-id rule decided; edge_ties: pixels whose "
-                                        "winner passed an edge test inside the 1e-7 tolerance"}
+            parity.update({"view": 0, "raster_bit_exact": bool(np.array_equal(o_r.view(np.uint32),
+                                                                                 g_r.view(np.uint32))),
+                           **counts, "note": "depth_ties: pixels the lowest-id rule decided; edge_ties: pixels whose "
+                                             "winner passed an edge test inside the 1e-7 tolerance; *_sum_err: "
+                                             "|sum of the GPU gradient - sum of the upstream gradient over covered "
+                                             "pixels| / sum of |terms|, per channel, worst channel"})
         except Exception as e:
-            parity = {"view": 0, "failed": str(e)}
+            parity.update({"view": 0, "failed": str(e)})
 
     if rank == 0:
         line = {
