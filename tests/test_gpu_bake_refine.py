@@ -179,3 +179,43 @@ def test_refine_step_kernels(baker):
     api.adam_update(tex, g, m, v, 0.01, 0.9, 0.999, 1e-8, 0.1, 0.001, 0.0, 1.0)
     assert same_bits(tt.cpu().numpy(), tex) and same_bits(tm.cpu().numpy(), m) and same_bits(tv.cpu().numpy(), v)
     assert not tg.any()
+
+
+@pytest.mark.parametrize("masked", [False, True])
+def test_total_variation_kernel(masked):
+    """pdr_refine_total_variation (the chart-aware TV of atlas.py:84-115 added into the refiner's gradient)
+    against ora_tv_gradient, itself pinned to the reference's autograd (tests/test_atlas_losses.py), on
+    the golden texture and a larger random atlas: per texel a sum of at most four pair terms, so within
+    1e-6 of the element plus 1e-7 of the largest element."""
+    import ctypes as C
+    import os
+
+    import torch
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    golden = np.load(os.path.join(os.path.dirname(__file__), "golden", "atlas_losses.npz"))
+    rng = np.random.default_rng(6)
+    cases = [(golden["tex"].astype(np.float32), golden["valid"], golden["chart"])]
+    big = rng.uniform(size=(301, 517, 3)).astype(np.float32)
+    cases.append((big, rng.uniform(size=big.shape[:2]) < 0.9,
+                  (np.arange(517)[None, :] // 64 + 9 * (np.arange(301)[:, None] // 50)).astype(np.int32)))
+    dev = torch.device("cuda", 0)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for tex, valid, chart in cases:
+        if not masked:
+            valid, chart = np.ones(tex.shape[:2], bool), None
+        H, W = tex.shape[:2]
+        ok_h = valid[:, 1:] & valid[:, :-1] & (True if chart is None else chart[:, 1:] == chart[:, :-1])
+        ok_v = valid[1:, :] & valid[:-1, :] & (True if chart is None else chart[1:, :] == chart[:-1, :])
+        scale = np.float32(0.37 / (max(int(ok_h.sum() + ok_v.sum()), 1) * 3.0))
+        want, _ = api.tv_gradient(tex, valid=valid.astype(np.uint8), chart=chart, eps=1e-4, weight=0.37)
+        t_tex = torch.tensor(tex, device=dev)
+        t_valid = torch.tensor(valid.astype(np.uint8), device=dev)
+        t_chart = None if chart is None else torch.tensor(chart, device=dev)
+        grad = torch.zeros_like(t_tex)
+        _native.call("pdr_refine_total_variation", _ptr(t_tex), W, H, _ptr(t_valid), _ptr(t_chart), 1e-4,
+                     float(scale), _ptr(grad), stream)
+        got = grad.cpu().numpy()
+        assert np.all(np.abs(got - want) <= 1e-6 * np.abs(want) + 1e-7 * np.abs(want).max()), (H, W, masked)
