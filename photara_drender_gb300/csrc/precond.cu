@@ -770,9 +770,8 @@ cudaError_t launch_adam_scaled(float* tex, float* grad, float* m1, float* m2, ui
                                const uint32_t* fallback, float lr, float b1, float b2, float eps, float bc1, float bc2,
                                float cmin, float cmax, cudaStream_t stream) {
     const uint64_t n = N * 3;
-    uint64_t blocks = (n / 4 + 255) / 256;
-    const uint64_t cap = (uint64_t)num_sms() * 8;
-    if (blocks > cap) blocks = cap;
+    uint64_t blocks = (n / 4 + 255) / 256;  // one float4 per thread, as launch_adam
+    if (blocks > 0x7FFFFFFFu) blocks = 0x7FFFFFFFu;
     if (blocks == 0) blocks = 1;
     adam_scaled_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tex, grad, m1, m2, n, mult, fallback, lr, b1, b2, eps,
                                                              bc1, bc2, cmin, cmax);
