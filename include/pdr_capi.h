@@ -211,7 +211,10 @@ PDR_API pdr_status pdr_project_views(const float* atlas_positions, const float* 
                                      float* confidence, uint32_t* source_view, float* valid_mask, float* coverage_mask,
                                      uint32_t* face_ids, void* stream);
 
-/* ---- refine: src/texture_refiner.cpp + atlas_* shaders ---------------------------------------- */
+/* ---- refine: src/texture_refiner.cpp + atlas_* shaders ---------------------------------------- *
+ * Layouts: texture and Adam moments [height][width][3]; the gradient is [height][width][4] (RGB and
+ * one unused float per texel, 16-byte aligned), so a bilinear tap adds its three channels with one
+ * vector reduction. The gradient is scratch: zero before the first accumulation, zero after Adam. */
 
 /* Cached per-view refinement inputs (texture_refiner.cpp:79-85), device pointers; 32 bytes. */
 typedef struct {
@@ -248,6 +251,7 @@ PDR_API pdr_status pdr_refine_seam(const float* texture, uint32_t width, uint32_
 PDR_API pdr_status pdr_refine_total_variation(const float* texture, uint32_t width, uint32_t height,
                                               const uint8_t* valid, const int32_t* chart_ids, float epsilon,
                                               float scale, float* gradient, void* stream);
+/* count = texels * 3 values of texture and moments; gradient [texels][4]. */
 PDR_API pdr_status pdr_refine_adam(float* texture, float* gradient, float* moment1, float* moment2, uint64_t count,
                                    float learning_rate, float beta1, float beta2, float epsilon,
                                    float bias_correction1, float bias_correction2, float clamp_min, float clamp_max,

@@ -485,7 +485,7 @@ class TextureBaker:
         steps, seam_polish_steps = int(o.steps), int(o.seam_polish_steps)
         t1 = st.t1
         tex = init.clone().contiguous()
-        grad = torch.empty_like(tex)
+        grad = torch.empty((tex.shape[0], tex.shape[1], 4), dtype=torch.float32, device=tex.device)  # RGB + pad
         m1 = torch.empty_like(tex)
         m2 = torch.empty_like(tex)
         seam_steps = 0 if npairs == 0 else int(seam_polish_steps)

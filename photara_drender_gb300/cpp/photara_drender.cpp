@@ -810,7 +810,7 @@ TextureRefineOutput TextureRefiner::refine(std::span<const float> initial_textur
     check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     const auto t1 = std::chrono::steady_clock::now();
     auto d_tex = upload(initial_texture, s);
-    DeviceArray<float> g(n), m1(n), m2(n);
+    DeviceArray<float> g(n / 3 * 4), m1(n), m2(n);  // the gradient is [texels][4]
     const std::uint32_t pairs = static_cast<std::uint32_t>(seam_uv_pairs.size() / 4);
     auto d_pairs = upload(seam_uv_pairs, s);
     const std::uint32_t seam_steps = pairs == 0 ? 0u : o.seam_polish_steps;

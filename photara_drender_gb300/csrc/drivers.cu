@@ -49,10 +49,10 @@ pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* vi
         if (err == cudaSuccess && e != cudaSuccess) err = e;
     };
     chk(cudaMemsetAsync(loss, 0, (size_t)(o->steps + seam_steps) * sizeof(float), stream));
-    chk(cudaMemsetAsync(grad, 0, n * sizeof(float), stream));
+    const uint64_t texels = (uint64_t)o->width * o->height;
+    chk(cudaMemsetAsync(grad, 0, texels * 4 * sizeof(float), stream));  // [texels][4]
     chk(cudaMemsetAsync(m1, 0, n * sizeof(float), stream));
     chk(cudaMemsetAsync(m2, 0, n * sizeof(float), stream));
-    const uint64_t texels = (uint64_t)o->width * o->height;
     if (pc) chk(cudaMemsetAsync(pc->fallback, 0, sizeof(uint32_t), stream));
     for (uint32_t step = 0; step < o->steps && err == cudaSuccess; ++step) {
         if (pc && step % pc->refresh_interval == 0) {
@@ -85,7 +85,7 @@ pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* vi
     }
     if (seam_steps) {
         // texture_refiner.cpp:371-415: reset gradient and moments, then seam + Adam steps
-        chk(cudaMemsetAsync(grad, 0, n * sizeof(float), stream));
+        chk(cudaMemsetAsync(grad, 0, texels * 4 * sizeof(float), stream));
         chk(cudaMemsetAsync(m1, 0, n * sizeof(float), stream));
         chk(cudaMemsetAsync(m2, 0, n * sizeof(float), stream));
         const float norm = 1.0F / static_cast<float>(npairs * 3u);
@@ -221,6 +221,7 @@ pdr_status pdr_refine_photometric(const float* tex, uint32_t W, uint32_t H, cons
                                   float* loss, void* stream) {
     if (!tex || !views || !grad || !loss || nviews == 0 || batch == 0 || W == 0 || H == 0)
         return fail(PDR_INVALID_ARGUMENT, "texture refinement options are invalid");
+    if (!aligned(grad, 16)) return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers must be 16-byte aligned");
     return cuda_status(launch_photometric(tex, W, H, views, nviews, max_pixels, step, batch, eps, norm, grad, loss,
                                           (cudaStream_t)stream),
                        "refine_photometric");
@@ -230,6 +231,7 @@ pdr_status pdr_refine_seam(const float* tex, uint32_t W, uint32_t H, const float
                            float norm, float* grad, float* loss, uint32_t loss_index, void* stream) {
     if (!tex || !grad || !loss || W == 0 || H == 0 || (npairs && (!pairs || !aligned(pairs, 16))))
         return fail(PDR_INVALID_ARGUMENT, "seam_uv_pairs must have shape [pair_count, 2, 2]");
+    if (!aligned(grad, 16)) return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers must be 16-byte aligned");
     if (npairs == 0) return PDR_OK;
     return cuda_status(launch_seam(tex, W, H, pairs, npairs, eps, norm, grad, loss, loss_index, (cudaStream_t)stream),
                        "refine_seam");
@@ -238,6 +240,7 @@ pdr_status pdr_refine_seam(const float* tex, uint32_t W, uint32_t H, const float
 pdr_status pdr_refine_total_variation(const float* tex, uint32_t W, uint32_t H, const uint8_t* valid, const int32_t* chart,
                                       float eps, float scale, float* grad, void* stream) {
     if (!tex || !valid || !grad || W == 0 || H == 0) return fail(PDR_INVALID_ARGUMENT, "valid_mask must have shape [texture_height, texture_width]");
+    if (!aligned(grad, 16)) return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers must be 16-byte aligned");
     return cuda_status(launch_tv(tex, W, H, valid, chart, eps, scale, grad, (cudaStream_t)stream), "refine_total_variation");
 }
 
@@ -246,6 +249,7 @@ pdr_status pdr_refine_adam(float* tex, float* grad, float* m1, float* m2, uint64
     if (!tex || !grad || !m1 || !m2) return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers are required");
     if (!aligned(tex, 16) || !aligned(grad, 16) || !aligned(m1, 16) || !aligned(m2, 16))
         return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers must be 16-byte aligned");
+    if (n % 3) return fail(PDR_INVALID_ARGUMENT, "texture refinement values must be RGB texels (a multiple of 3)");
     if (n == 0) return PDR_OK;
     return cuda_status(launch_adam(tex, grad, m1, m2, n, lr, b1, b2, eps, bc1, bc2, cmin, cmax, (cudaStream_t)stream),
                        "refine_adam");

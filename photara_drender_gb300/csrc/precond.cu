@@ -642,30 +642,22 @@ __device__ __forceinline__ float step_multiplier(const float* __restrict__ mult,
 }
 
 __global__ void adam_scaled_kernel(float* __restrict__ tex, float* __restrict__ grad, float* __restrict__ m1,
-                                   float* __restrict__ m2, uint64_t n, const float* __restrict__ mult,
+                                   float* __restrict__ m2, uint64_t texels, const float* __restrict__ mult,
                                    const uint32_t* __restrict__ fallback, float lr, float b1, float b2, float eps,
                                    float bc1, float bc2, float cmin, float cmax) {
+    // one texel per thread, as adam_kernel: texture and moments [texels][3], gradient and multipliers
+    // [texels][4]
     const bool plain = *fallback != 0;
-    const uint64_t n4 = n / 4;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-        float4 x = reinterpret_cast<float4*>(tex)[i];
-        float4 g = reinterpret_cast<float4*>(grad)[i];
-        float4 m = reinterpret_cast<float4*>(m1)[i];
-        float4 v = reinterpret_cast<float4*>(m2)[i];
-        const uint64_t k = i * 4;
-        adam_scaled_one(x.x, g.x, m.x, v.x, step_multiplier(mult, k, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
-        adam_scaled_one(x.y, g.y, m.y, v.y, step_multiplier(mult, k + 1, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
-        adam_scaled_one(x.z, g.z, m.z, v.z, step_multiplier(mult, k + 2, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
-        adam_scaled_one(x.w, g.w, m.w, v.w, step_multiplier(mult, k + 3, plain), lr, b1, b2, eps, bc1, bc2, cmin, cmax);
-        reinterpret_cast<float4*>(tex)[i] = x;
-        reinterpret_cast<float4*>(grad)[i] = g;
-        reinterpret_cast<float4*>(m1)[i] = m;
-        reinterpret_cast<float4*>(m2)[i] = v;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < texels; t += stride) {
+        const float4 d = reinterpret_cast<const float4*>(grad)[t];
+        float g[3] = {d.x, d.y, d.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            adam_scaled_one(tex[t * 3 + c], g[c], m1[t * 3 + c], m2[t * 3 + c], step_multiplier(mult, t * 3 + c, plain),
+                            lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+        reinterpret_cast<float4*>(grad)[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    for (uint64_t k = n4 * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
-        adam_scaled_one(tex[k], grad[k], m1[k], m2[k], step_multiplier(mult, k, plain), lr, b1, b2, eps, bc1, bc2, cmin,
-                        cmax);
 }
 
 // Plain-Adam fallback: after each refresh window, if the mean batch loss of the last window rose by more
@@ -769,11 +761,10 @@ cudaError_t launch_precond_features(const float* tex, const float* m1, const flo
 cudaError_t launch_adam_scaled(float* tex, float* grad, float* m1, float* m2, uint64_t N, const float* mult,
                                const uint32_t* fallback, float lr, float b1, float b2, float eps, float bc1, float bc2,
                                float cmin, float cmax, cudaStream_t stream) {
-    const uint64_t n = N * 3;
-    uint64_t blocks = (n / 4 + 255) / 256;  // one float4 per thread, as launch_adam
+    uint64_t blocks = (N + 255) / 256;  // one texel per thread, as launch_adam
     if (blocks > 0x7FFFFFFFu) blocks = 0x7FFFFFFFu;
     if (blocks == 0) blocks = 1;
-    adam_scaled_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tex, grad, m1, m2, n, mult, fallback, lr, b1, b2, eps,
+    adam_scaled_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tex, grad, m1, m2, N, mult, fallback, lr, b1, b2, eps,
                                                              bc1, bc2, cmin, cmax);
     return cudaGetLastError();
 }

@@ -177,7 +177,7 @@ def plain_trajectory_samples(state, stats: TexelStats, valid: torch.Tensor, inte
     N = W * H
     L = _native.lib()
     tex = state.init.clone().contiguous()
-    grad = torch.zeros_like(tex)
+    grad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)  # the refiner's RGB + pad gradient
     m1 = torch.zeros_like(tex)
     m2 = torch.zeros_like(tex)
     steps = int(o.steps)
@@ -254,7 +254,7 @@ def photometric_loss(state, texture: torch.Tensor) -> float:
     dev = state.init.device
     W, H = int(o.width), int(o.height)
     n = len(state.weights)
-    grad = torch.zeros_like(texture)
+    grad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
     loss = torch.zeros(n, dtype=torch.float32, device=dev)
     s = _stream(dev)
     L = _native.lib()

@@ -160,23 +160,24 @@ def test_refine_step_kernels(baker):
     table[0].uv, table[0].target, table[0].mask, table[0].pixel_count = (t_uv.data_ptr(), t_tgt.data_ptr(),
                                                                          t_mask.data_ptr(), P)
     t_table = torch.frombuffer(bytearray(bytes(table)), dtype=torch.uint8).to(dev)
-    grad = torch.zeros_like(t_tex)
+    grad = torch.zeros((30, 20, 4), dtype=torch.float32, device=dev)  # the refiner's RGB + pad layout
     loss = torch.zeros(4, dtype=torch.float32, device=dev)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     _native.call("pdr_refine_photometric", _ptr(t_tex), 20, 30, _ptr(t_table), 1, P, 2, 1, 1e-3, 0.01, _ptr(grad),
                  _ptr(loss), stream)
     g32, l32 = api.photometric_gradient(tex, uv, tgt, mask, 1e-3, 0.01)
     # per-texel sums of a handful of atomically added terms: within 1e-5 of the reference-order sums
-    g = grad.cpu().numpy()
+    assert not grad[..., 3].any()
+    g = grad[..., :3].cpu().numpy()
     assert np.all(np.abs(g - g32) <= 1e-5 * np.maximum(np.abs(g32), 1e-3 * np.abs(g32).max()))
     assert abs(float(loss[2]) - l32) <= 1e-5 * abs(l32)
     m = (rng.normal(size=tex.shape) * 0.01).astype(np.float32)
     v = (rng.uniform(size=tex.shape) * 0.001).astype(np.float32)
-    g = g32.copy()
+    g = np.concatenate([g32, np.full(g32.shape[:2] + (1,), 7.0, np.float32)], -1)  # the pad is ignored
     tt, tg, tm, tv = (torch.tensor(x, device=dev) for x in (tex, g, m, v))
     _native.call("pdr_refine_adam", _ptr(tt), _ptr(tg), _ptr(tm), _ptr(tv), tex.size, 0.01, 0.9, 0.999, 1e-8, 0.1,
                  0.001, 0.0, 1.0, stream)
-    api.adam_update(tex, g, m, v, 0.01, 0.9, 0.999, 1e-8, 0.1, 0.001, 0.0, 1.0)
+    api.adam_update(tex, g32.copy(), m, v, 0.01, 0.9, 0.999, 1e-8, 0.1, 0.001, 0.0, 1.0)
     assert same_bits(tt.cpu().numpy(), tex) and same_bits(tm.cpu().numpy(), m) and same_bits(tv.cpu().numpy(), v)
     assert not tg.any()
 
@@ -214,8 +215,9 @@ def test_total_variation_kernel(masked):
         t_tex = torch.tensor(tex, device=dev)
         t_valid = torch.tensor(valid.astype(np.uint8), device=dev)
         t_chart = None if chart is None else torch.tensor(chart, device=dev)
-        grad = torch.zeros_like(t_tex)
+        grad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
         _native.call("pdr_refine_total_variation", _ptr(t_tex), W, H, _ptr(t_valid), _ptr(t_chart), 1e-4,
                      float(scale), _ptr(grad), stream)
-        got = grad.cpu().numpy()
+        assert not grad[..., 3].any()
+        got = grad[..., :3].cpu().numpy()
         assert np.all(np.abs(got - want) <= 1e-6 * np.abs(want) + 1e-7 * np.abs(want).max()), (H, W, masked)

@@ -253,7 +253,8 @@ def test_scaled_adam_matches_restatement(dev, fallback):
     x, g = rng.uniform(0, 1, (N, 3)).astype(np.float32), rng.normal(0, 1e-3, (N, 3)).astype(np.float32)
     m, v = rng.normal(0, 1e-3, (N, 3)).astype(np.float32), rng.uniform(0, 1e-6, (N, 3)).astype(np.float32)
     mult = rng.uniform(-4, 4, (N, 4)).astype(np.float32)
-    t = [torch.tensor(a, device=dev) for a in (x, g, m, v, mult)]
+    g4 = np.concatenate([g, np.full((N, 1), 5.0, np.float32)], 1)  # the refiner's RGB + pad gradient
+    t = [torch.tensor(a, device=dev) for a in (x, g4, m, v, mult)]
     flag = torch.tensor([fallback], dtype=torch.int32, device=dev)
     lr, b1, b2, eps, bc1, bc2 = 1e-2, 0.9, 0.999, 1e-8, 0.271, 0.00299
     s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
