@@ -913,6 +913,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
     ap.add_argument("--views", type=int, default=None, help="override the view count (small profiling cases)")
     ap.add_argument("--atlas", type=int, default=None, help="override the atlas size (texture-gradient profiling)")
+    ap.add_argument("--bake-views", type=int, default=None, help="override the bake leg's view count (profiling)")
     ap.add_argument("--skip-c1", action="store_true", help="omit the small-mesh (C1) leg")
     ap.add_argument("--skip-bake", action="store_true", help="omit the bake leg")
     ap.add_argument("--skip-refine", action="store_true", help="omit the refine leg")
@@ -922,6 +923,9 @@ def main():
     if args.views:
         WORKLOAD["views"] = args.views
         WORKLOAD["name"] = WORKLOAD["name"].replace("64x", f"{args.views}x")
+    if args.bake_views:
+        BAKE["name"] = BAKE["name"].replace(f"{BAKE['views']}x", f"{args.bake_views}x")
+        BAKE["views"] = args.bake_views
     if args.atlas:
         WORKLOAD["name"] = WORKLOAD["name"].replace(f"atlas{WORKLOAD['atlas']}", f"atlas{args.atlas}")
         WORKLOAD["atlas"] = args.atlas

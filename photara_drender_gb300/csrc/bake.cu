@@ -75,6 +75,9 @@ __device__ __forceinline__ float shadow_visibility(const pdr_projection_view& v,
     return count > 0.0f ? visible / count : 0.0f;
 }
 
+constexpr uint32_t kViewChunk = 32;
+static_assert(sizeof(pdr_projection_view) % sizeof(uint4) == 0, "view records are copied as 16-byte words");
+
 __global__ void project_views_kernel(const float* __restrict__ apos, const float* __restrict__ anrm,
                                      const float4* __restrict__ araster, uint32_t N,
                                      const pdr_projection_view* __restrict__ views, uint32_t nviews,
@@ -83,18 +86,37 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
                                      uint32_t* __restrict__ source_view, float* __restrict__ valid_mask,
                                      float* __restrict__ coverage_mask, uint32_t* __restrict__ face_ids,
                                      const uint32_t* __restrict__ vis_bits, uint32_t vis_words) {
+    // The view records are staged in shared memory kViewChunk at a time: every texel reads every field of
+    // every view, and shared-memory loads are shorter than L1 hits on the global table.
+    __shared__ __align__(16) pdr_projection_view sv[kViewChunk];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const float rw = araster[i].w;
+    const float rw = i < N ? araster[i].w : 0.0f;
+    const bool active = raster_id(rw) != 0;
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, accw = 0.0f, best = 0.0f;
     uint32_t src = 0xffffffffu;
-    if (raster_id(rw) != 0) {
-        const float px = apos[(size_t)i * 3], py = apos[(size_t)i * 3 + 1], pz = apos[(size_t)i * 3 + 2];
+    float px = 0.0f, py = 0.0f, pz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (active) {
+        px = apos[(size_t)i * 3];
+        py = apos[(size_t)i * 3 + 1];
+        pz = apos[(size_t)i * 3 + 2];
         const float nx0 = anrm[(size_t)i * 3], ny0 = anrm[(size_t)i * 3 + 1], nz0 = anrm[(size_t)i * 3 + 2];
         const float nl = sqrtf(nx0 * nx0 + ny0 * ny0 + nz0 * nz0);
-        const float nx = nx0 / nl, ny = ny0 / nl, nz = nz0 / nl;
-        for (uint32_t k = 0; k < nviews; ++k) {
-            const pdr_projection_view& v = views[k];
+        nx = nx0 / nl;
+        ny = ny0 / nl;
+        nz = nz0 / nl;
+    }
+    const bool any_active = __syncthreads_or(active) != 0;
+    for (uint32_t k0 = 0; any_active && k0 < nviews; k0 += kViewChunk) {
+        const uint32_t cnt = min(kViewChunk, nviews - k0);
+        __syncthreads();
+        constexpr uint32_t kWords = sizeof(pdr_projection_view) / sizeof(uint4);
+        for (uint32_t q = threadIdx.x; q < cnt * kWords; q += blockDim.x)
+            reinterpret_cast<uint4*>(sv)[q] = __ldg(reinterpret_cast<const uint4*>(views + k0) + q);
+        __syncthreads();
+        if (!active) continue;
+        for (uint32_t kk = 0; kk < cnt; ++kk) {
+            const uint32_t k = k0 + kk;
+            const pdr_projection_view& v = sv[kk];
             ProjectedTexel pt;
             if (!project_texel(v, px, py, pz, nx, ny, nz, pt)) continue;
             const float ppx = pt.ppx, ppy = pt.ppy, ndz = pt.ndz, vl = pt.vl, cosv = pt.cosv;
@@ -152,6 +174,7 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
             }
         }
     }
+    if (i >= N) return;
     // texture_baker.cpp:192-204 and 347-358
     const float valid = accw > 0.0f ? 1.0f : 0.0f;
     const float div = blend_mode != 0 && accw > 0.0f ? accw : 1.0f;

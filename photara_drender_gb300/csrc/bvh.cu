@@ -546,6 +546,8 @@ pdr_status pdr_project_views_bits(const float* apos, const float* anrm, const fl
         return set_error(PDR_INVALID_ARGUMENT, "projection buffers are required");
     if (N == 0 || nviews == 0 || pcf_radius > 4 || blend_mode > 2 || visibility_mode < 1 || visibility_mode > 2)
         return set_error(PDR_INVALID_ARGUMENT, "ray-visibility projection needs visibility mode 1 or 2");
+    if (((uintptr_t)araster | (uintptr_t)color | (uintptr_t)views) & 15u)
+        return set_error(PDR_INVALID_ARGUMENT, "projection buffers must be 16-byte aligned");
     return set_cuda_error(launch_project_views(apos, anrm, araster, N, views, nviews, blend_mode, pcf_radius,
                                                visibility_mode, color, confidence, source_view, valid_mask,
                                                coverage_mask, face_ids, (cudaStream_t)stream, visibility,
