@@ -49,6 +49,20 @@ int num_sms() {
     return sms;
 }
 
+pdr_status check_raster_args(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
+                                    uint32_t W, uint32_t H, const float* viewports) {
+    if (!clip || !idx || !viewports) return fail(PDR_INVALID_ARGUMENT, "clip_positions, indices and viewports are required");
+    if (views == 0 || V == 0) return fail(PDR_INVALID_ARGUMENT, "clip_positions must have shape [vertex_count, 4]");
+    if (T == 0) return fail(PDR_INVALID_ARGUMENT, "triangle_indices must have shape [triangle_count, 3]");
+    if (W == 0 || H == 0) return fail(PDR_INVALID_ARGUMENT, "Rasterization width and height must be positive");
+    if (W > 65535u * kTile || H > 65535u * kTile) return fail(PDR_OVERFLOW, "Rasterization output size overflow");
+    const uint64_t tiles = (uint64_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+    if (tiles * views >= 0x7fffffffull || (uint64_t)T * views >= 0x7fffffffull)
+        return fail(PDR_OVERFLOW, "Rasterization output size overflow");
+    if (!aligned(clip, 16) || !aligned(viewports, 16)) return fail(PDR_INVALID_ARGUMENT, "clip_positions and viewports must be 16-byte aligned");
+    return PDR_OK;
+}
+
 }  // namespace pdr
 
 using namespace pdr;
@@ -98,20 +112,6 @@ pdr_status pdr_validate_indices(const uint32_t* indices, uint64_t n, uint32_t ve
 size_t pdr_bin_tiles_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
                                      uint64_t capacity) {
     return bins_workspace_bytes(views, triangle_count, width, height, capacity);
-}
-
-static pdr_status check_raster_args(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
-                                    uint32_t W, uint32_t H, const float* viewports) {
-    if (!clip || !idx || !viewports) return fail(PDR_INVALID_ARGUMENT, "clip_positions, indices and viewports are required");
-    if (views == 0 || V == 0) return fail(PDR_INVALID_ARGUMENT, "clip_positions must have shape [vertex_count, 4]");
-    if (T == 0) return fail(PDR_INVALID_ARGUMENT, "triangle_indices must have shape [triangle_count, 3]");
-    if (W == 0 || H == 0) return fail(PDR_INVALID_ARGUMENT, "Rasterization width and height must be positive");
-    if (W > 65535u * kTile || H > 65535u * kTile) return fail(PDR_OVERFLOW, "Rasterization output size overflow");
-    const uint64_t tiles = (uint64_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
-    if (tiles * views >= 0x7fffffffull || (uint64_t)T * views >= 0x7fffffffull)
-        return fail(PDR_OVERFLOW, "Rasterization output size overflow");
-    if (!aligned(clip, 16) || !aligned(viewports, 16)) return fail(PDR_INVALID_ARGUMENT, "clip_positions and viewports must be 16-byte aligned");
-    return PDR_OK;
 }
 
 pdr_status pdr_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T, uint32_t W,

@@ -163,9 +163,10 @@ pdr_status pdr_clip_near(const float* clip_positions, uint32_t views, uint32_t v
 pdr_status pdr_remap_near(const float* clip_positions, uint32_t views, uint32_t vertex_count, const uint32_t* indices,
                           uint32_t triangle_count, uint32_t width, uint32_t height, const float* viewports,
                           float* raster, float* barycentric_derivatives, void* stream) {
-    if (!near_args_ok(clip_positions, views, vertex_count, indices, triangle_count) || !viewports || !raster ||
-        width == 0 || height == 0)
-        return set_error(PDR_INVALID_ARGUMENT, "near remap needs positions, indices, viewports and the raster");
+    const pdr_status st = check_raster_args(clip_positions, views, vertex_count, indices, triangle_count, width,
+                                            height, viewports);
+    if (st) return st;
+    if (!raster) return set_error(PDR_INVALID_ARGUMENT, "near remap needs positions, indices, viewports and the raster");
     if (triangle_count > PDR_NEAR_MAX_TRIANGLES)
         return set_error(PDR_OVERFLOW, "near-plane clipping supports at most 8388608 triangles");
     if (((uintptr_t)clip_positions | (uintptr_t)raster | (uintptr_t)barycentric_derivatives) & 15u)
@@ -184,8 +185,10 @@ pdr_status pdr_rasterize_backward_near(const float* clip_positions, uint32_t vie
                                        uint32_t height, const float* viewports, const float* raster,
                                        const float* grad_raster, const float* grad_barycentric_derivatives,
                                        float* grad_clip_positions, void* stream) {
-    if (!near_args_ok(clip_positions, views, vertex_count, indices, triangle_count) || !viewports || !raster ||
-        !grad_clip_positions || width == 0 || height == 0)
+    const pdr_status st = check_raster_args(clip_positions, views, vertex_count, indices, triangle_count, width,
+                                            height, viewports);
+    if (st) return st;
+    if (!raster || !grad_clip_positions)
         return set_error(PDR_INVALID_ARGUMENT, "raster, grad_raster and grad_clip_positions are required");
     if (((uintptr_t)clip_positions | (uintptr_t)raster | (uintptr_t)grad_raster |
          (uintptr_t)grad_barycentric_derivatives) & 15u)

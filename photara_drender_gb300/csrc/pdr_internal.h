@@ -84,6 +84,9 @@ namespace pdr {
 
 pdr_status set_error(pdr_status code, const char* msg);
 pdr_status set_cuda_error(cudaError_t err, const char* what);
+// The shape, size and alignment checks every raster entry point makes (the reference's messages).
+pdr_status check_raster_args(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
+                             uint32_t W, uint32_t H, const float* viewports);
 
 cudaError_t launch_project_views(const float* apos, const float* anrm, const float* araster, uint32_t N,
                                  const pdr_projection_view* views, uint32_t nviews, uint32_t blend_mode,
