@@ -1,0 +1,114 @@
+"""The raster forward's per-triangle candidate rectangle (photara_drender_gb300/csrc/raster_tile.cuh
+pixel_rect) must contain every pixel of the tile whose sample passes the reference's edge tests
+(rasterize_forward.hlsl: fl(cross(a - s, b - s)) * sign >= -1e-7 for the three edges), or else decline
+(the kernel then falls back to the exact per-region test). Restated here in NumPy float32, operation by
+operation, and checked against brute-force edge tests over whole tiles on triangles of every scale:
+microscopic ones (whose tolerance reaches beyond their bounding box), slivers, large ones crossing the
+tile, vertices on the sample lattice, and odd viewports."""
+import numpy as np
+
+f = np.float32
+TILE = 16
+
+
+def sample_ndc(p, v0, size):
+    return ((p.astype(np.float32) - f(v0) + f(0.5)) * f(2.0) / f(size) - f(1.0)).astype(np.float32)
+
+
+def pixel_rect(s, area, vp, x_org, y_org, x_end, y_end):
+    """NumPy float32 restatement of pixel_rect for arrays of triangles s [n, 3, 2]; returns (large, none,
+    x0, x1, y0, y1) with absolute pixel bounds."""
+    vp = [f(v) for v in vp]
+    sx, sy = s[..., 0], s[..., 1]
+    mnx, mxx = np.fmin(sx[:, 0], np.fmin(sx[:, 1], sx[:, 2])), np.fmax(sx[:, 0], np.fmax(sx[:, 1], sx[:, 2]))
+    mny, mxy = np.fmin(sy[:, 0], np.fmin(sy[:, 1], sy[:, 2])), np.fmax(sy[:, 0], np.fmax(sy[:, 1], sy[:, 2]))
+    pxw, pyw = f(2.0) / vp[2], f(2.0) / vp[3]
+    ext = np.fmax(mxx - mnx, mxy - mny)
+    tsx_lo = sample_ndc(np.array([x_org]), vp[0], vp[2])[0]
+    tsx_hi = sample_ndc(np.array([x_end - 1]), vp[0], vp[2])[0]
+    tsy_lo = sample_ndc(np.array([y_org]), vp[1], vp[3])[0]
+    tsy_hi = sample_ndc(np.array([y_end - 1]), vp[1], vp[3])[0]
+    L = f(1.01) * np.fmax(np.fmax(np.abs(mxx - tsx_lo), np.abs(tsx_hi - mnx)),
+                          np.fmax(np.abs(mxy - tsy_lo), np.abs(tsy_hi - mny)))
+    perim = (np.abs(sx[:, 1] - sx[:, 0]) + np.abs(sy[:, 1] - sy[:, 0]) + np.abs(sx[:, 2] - sx[:, 1]) +
+             np.abs(sy[:, 2] - sy[:, 1]) + np.abs(sx[:, 0] - sx[:, 2]) + np.abs(sy[:, 0] - sy[:, 2]))
+    tau = f(1e-7) + f(2e-6) * L * L
+    D = f(2.0) * tau * perim / np.abs(area)
+    large = ~(D <= np.fmin(pxw, pyw)) | ~(np.abs(area) >= f(1e-4) * ext * ext)
+    slx = f(0.05) + f(1e-6) * (vp[2] + abs(vp[0]))
+    sly = f(0.05) + f(1e-6) * (vp[3] + abs(vp[1]))
+    fx0 = np.ceil(((mnx - D) + f(1.0)) * f(0.5) * vp[2] + vp[0] - f(0.5) - slx)
+    fx1 = np.floor(((mxx + D) + f(1.0)) * f(0.5) * vp[2] + vp[0] - f(0.5) + slx)
+    fy0 = np.ceil(((mny - D) + f(1.0)) * f(0.5) * vp[3] + vp[1] - f(0.5) - sly)
+    fy1 = np.floor(((mxy + D) + f(1.0)) * f(0.5) * vp[3] + vp[1] - f(0.5) + sly)
+    cx0, cx1 = np.fmax(fx0, f(x_org)), np.fmin(fx1, f(x_end - 1))
+    cy0, cy1 = np.fmax(fy0, f(y_org)), np.fmin(fy1, f(y_end - 1))
+    none = ~(cx0 <= cx1) | ~(cy0 <= cy1)
+    return large, none, cx0, cx1, cy0, cy1
+
+
+def covered(s, sign, px, py, vp):
+    """The reference's edge tests of every triangle at every pixel (px, py): [n, pixels] bool."""
+    sx = sample_ndc(px, vp[0], vp[2])[None, :]
+    sy = sample_ndc(py, vp[1], vp[3])[None, :]
+    cr = lambda ax, ay, bx, by: ax * by - ay * bx  # noqa: E731
+    a = [(s[:, k, 0:1], s[:, k, 1:2]) for k in range(3)]
+    e0 = cr(a[1][0] - sx, a[1][1] - sy, a[2][0] - sx, a[2][1] - sy)
+    e1 = cr(a[2][0] - sx, a[2][1] - sy, a[0][0] - sx, a[0][1] - sy)
+    e2 = cr(a[0][0] - sx, a[0][1] - sy, a[1][0] - sx, a[1][1] - sy)
+    c, sg = f(-1e-7), sign[:, None]
+    return ~((e0 * sg < c) | (e1 * sg < c) | (e2 * sg < c))
+
+
+def triangles(rng, n):
+    """Projected vertices [n, 3, 2] float32 of mixed scales around the tile at NDC (-0.1 .. 0.1)."""
+    out = []
+    for scale in (1e-6, 1e-5, 1e-4, 1e-3, 1e-2, 0.05, 0.3, 3.0):
+        c = rng.uniform(-0.12, 0.12, size=(n, 1, 2))
+        out.append(c + rng.normal(scale=scale, size=(n, 3, 2)))
+    a = rng.uniform(-0.12, 0.12, size=(n, 2))
+    d = rng.normal(size=(n, 2))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    nrm = np.stack([-d[:, 1], d[:, 0]], 1)
+    for width in (1e-7, 1e-5, 1e-3):
+        ln = rng.uniform(0.01, 0.4, size=(n, 1))
+        out.append(np.stack([a, a + d * ln, a + d * ln * 0.5 + nrm * width], 1))
+    return np.concatenate(out).astype(np.float32)
+
+
+def check(rng, vp, tiles):
+    W, H = int(vp[2]), int(vp[3])
+    s = triangles(rng, 600)
+    # snap some vertices onto the sample lattice (edges through pixel centres)
+    lat = rng.uniform(size=s.shape[:2]) < 0.2
+    k = np.round((s[..., 0] + 1) * 0.5 * vp[2] + vp[0] - 0.5)
+    s[..., 0] = np.where(lat, sample_ndc(k, vp[0], vp[2]), s[..., 0])
+    area = ((s[:, 1, 0] - s[:, 0, 0]) * (s[:, 2, 1] - s[:, 0, 1]) -
+            (s[:, 1, 1] - s[:, 0, 1]) * (s[:, 2, 0] - s[:, 0, 0])).astype(np.float32)
+    keep = ~(np.abs(area) <= f(1e-12))  # the reference skips these before the edge tests
+    s, area = s[keep], area[keep]
+    sign = np.where(area > 0, f(1.0), f(-1.0))
+    declined = total = 0
+    for tx, ty in tiles:
+        x_org, y_org = tx * TILE, ty * TILE
+        x_end, y_end = min(x_org + TILE, W), min(y_org + TILE, H)
+        px, py = np.meshgrid(np.arange(x_org, x_end), np.arange(y_org, y_end))
+        px, py = px.reshape(-1), py.reshape(-1)
+        cov = covered(s, sign, px, py, vp)
+        large, none, x0, x1, y0, y1 = pixel_rect(s, area, vp, x_org, y_org, x_end, y_end)
+        inside = ((px[None] >= x0[:, None]) & (px[None] <= x1[:, None]) & (py[None] >= y0[:, None]) &
+                  (py[None] <= y1[:, None]) & ~none[:, None])
+        missed = cov & ~inside & ~large[:, None]
+        assert not missed.any(), f"tile {(tx, ty)}: {int(missed.sum())} covered pixels outside the rectangle"
+        declined += int(large.sum())
+        total += len(large)
+    return declined, total
+
+
+def test_rectangle_contains_every_covered_pixel():
+    rng = np.random.default_rng(12)
+    for vp, tiles in [((0.0, 0.0, 64.0, 64.0), [(1, 1), (2, 1), (1, 2), (2, 2)]),
+                      ((-3.0, 2.5, 75.0, 58.0), [(0, 0), (1, 1), (2, 1), (3, 2)]),
+                      ((0.0, 0.0, 1024.0, 1024.0), [(31, 31), (32, 32), (30, 33)])]:
+        declined, total = check(rng, vp, tiles)
+        assert 0 < declined < total  # both the rectangle and the fallback are exercised
