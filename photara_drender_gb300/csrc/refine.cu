@@ -192,7 +192,7 @@ __global__ void tv_kernel(const float* __restrict__ tex, uint32_t tw, uint32_t t
     *gp = cur;
 }
 
-// atlas_adam_update.hlsl:20-43, four values per thread.
+// atlas_adam_update.hlsl:20-43 for one value (the update, then the gradient cleared).
 __device__ __forceinline__ void adam_one(float& x, float& g, float& m, float& v, float lr, float b1, float b2, float eps,
                                          float bc1, float bc2, float cmin, float cmax) {
     const float m1 = b1 * m + (1.0f - b1) * g;
