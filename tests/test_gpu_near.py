@@ -106,3 +106,26 @@ def test_torch_rasterize_near_autograd(r):
     with pytest.raises(OverflowError):
         big = np.zeros((8388609, 3), np.uint32)
         r.forward(clip, big, res, clip_near_plane=True)
+
+
+def test_near_derivatives_and_their_gradient(r):
+    """With clipping, the derivative output and its gradient are those of the original triangle at the
+    pixel, triangles behind the eye included: against the float64 derivative formula and its adjoint
+    (oracle/api.py, checked by central differences in tests/test_oracle_derivative_grad.py)."""
+    clip, idx, res = ground()
+    raster, deriv = r.forward(clip, idx, res, clip_near_plane=True)
+    ref = api.barycentric_derivatives_f64(clip, idx, raster)
+    covered = raster[..., 3] > 0
+    behind = (clip[idx.astype(np.int64)][..., 3] <= 1e-8).any(1)
+    ids = np.rint(raster[..., 3]).astype(np.int64)
+    assert behind[ids[covered] - 1].any()
+    err = np.abs(deriv.astype(np.float64) - ref)[covered]
+    assert err.max() <= 1e-4 * np.abs(ref).max(), err.max()
+    gd = np.random.default_rng(9).normal(size=res + (4,)).astype(np.float32)
+    got = r.backward(clip, idx, raster, np.zeros_like(raster), grad_barycentric_derivatives=gd, clip_near_plane=True)
+    f64 = api.barycentric_derivatives_backward_f64(clip, idx, raster, gd)
+    f32 = api.barycentric_derivatives_backward_f64(clip, idx, raster, gd, dtype=np.float32)
+    fabs = api.barycentric_derivatives_backward_f64(clip, idx, raster, gd, abs_terms=True)
+    bound = 4.0 * np.abs(f32 - f64) + 2e-6 * fabs + 1e-7 * np.abs(f64).max()
+    assert np.all(np.abs(got.astype(np.float64) - f64) <= bound)
+    assert np.abs(got[clip[:, 3] <= 1e-8]).max() > 0
