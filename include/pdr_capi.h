@@ -70,7 +70,8 @@ PDR_API pdr_status pdr_validate_indices(const uint32_t* indices, uint64_t n, uin
  * (view, 16x16 tile) with triangle ids ascending in every tile, bit-identical to the reference's
  * lists. tile_offsets has views*tiles+1 entries; tile_triangles holds `capacity` entries; the
  * entry count lands in status[PDR_STATUS_TILE_ENTRIES] and status[PDR_STATUS_TILE_OVERFLOW] is
- * set when it exceeds capacity (the caller then grows the list and calls again). */
+ * set when it exceeds capacity (the caller then grows the list and calls again). A capacity above
+ * UINT32_MAX is refused with PDR_OVERFLOW (the offsets are u32). */
 PDR_API size_t pdr_bin_tiles_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width,
                                              uint32_t height, uint64_t capacity);
 PDR_API pdr_status pdr_bin_tiles(const float* clip_positions, uint32_t views, uint32_t vertex_count,
@@ -348,8 +349,11 @@ PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream
  * is a 16 MiB array compiled into the library and held on every GPU that loads it until the process
  * exits. Bins needing more scratch than that (pdr_bin_tiles_workspace_bytes() > 16 MiB) are rejected
  * with PDR_INVALID_ARGUMENT. The first call on a device looks the array's device address up
- * (cudaGetSymbolAddress); make it before any stream capture. Every call shares the array: calls that
- * overlap on the GPU race and must be serialised by the caller. */
+ * (cudaGetSymbolAddress); make it before any stream capture. The address is kept for the life of the
+ * process, so the entry point must not be used across a device reset. Every call shares the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. Argument checks are those
+ * of pdr_bin_tiles (16-byte aligned clip positions and viewports; capacity at most UINT32_MAX, else
+ * PDR_OVERFLOW). */
 PDR_API pdr_status pdr_bin_tiles_no_alloc(const float* clip_positions, uint32_t views, uint32_t vertex_count,
                                           const uint32_t* indices, uint32_t triangle_count, uint32_t width,
                                           uint32_t height, const float* viewports, uint32_t* tile_offsets,

@@ -2,10 +2,14 @@
 
 * ``build_oracle()`` compiles ``oracle/pdr_oracle.c`` (the C restatement of the reference's
   shaders and host routines) into ``oracle/_build/libpdr_oracle.so``.
-* ``build_ref()`` compiles the reference's own sources, read where they lie under
-  ``/root/reference``, into ``oracle/_ref/libpdr_ref.so``: the HLSL compute shaders (after
+* ``build_ref()`` compiles the reference's own sources, read where they lie (``REFERENCE``
+  below), into ``oracle/_ref/libpdr_ref.so``: the HLSL compute shaders (after
   stripping the ``[numthreads]`` attribute line and ``: SV_*`` semantics, which C++ has no
-  syntax for) through ``oracle/ref_shim.hpp``, and ``src/texture_padding.cpp`` as-is.
+  syntax for) through ``oracle/ref_shim.hpp``, ``src/texture_padding.cpp`` as-is, and the
+  self-contained host routines of ``src/rasterizer.cpp`` (tile binning and the two CSR builders,
+  cut out by name through ``oracle/ref_host.cpp``; the rest of that file needs the absent Vulkan
+  wrapper). The reference directory is ``$PDR_REFERENCE_DIR`` (default: the mount point of the
+  read-only reference checkout).
   Nothing from the reference is copied into the repository; the stripped shader text is
   written only under ``oracle/_ref/gen`` (git-ignored).
 
@@ -19,7 +23,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# where the reference's sources lie; override with PDR_REFERENCE_DIR
+REFERENCE = os.environ.get("PDR_REFERENCE_DIR", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "_build", "libpdr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpdr_ref.so")
 SHADERS = [
@@ -55,15 +60,49 @@ def _strip_hlsl(text: str) -> str:
     return re.sub(r"\s*:\s*SV_[A-Za-z]+", "", text)
 
 
+# Definitions of src/rasterizer.cpp compiled for the checker, in source order: the binning and table
+# builders of the raster path plus the constants, structs and helpers they use.
+HOST_DEFINITIONS = [
+    r"constexpr std::uint32_t RASTER_TILE_SIZE\b", r"std::uint32_t divide_round_up\(", r"struct TileBins\b",
+    r"TileBins build_tile_bins\(", r"struct VertexAdjacency\b", r"VertexAdjacency build_vertex_adjacency\(",
+    r"std::int32_t address_coordinate\(", r"struct TextureSampleAdjacency\b",
+    r"TextureSampleAdjacency build_texture_sample_adjacency\(",
+]
+
+
+def _definition(text: str, pattern: str) -> str:
+    """The definition starting at `pattern`: up to its first ';' when that comes before any '{',
+    else through the matching closing brace (and a trailing ';' for a struct)."""
+    m = re.search(r"^" + pattern, text, flags=re.M)
+    if m is None:
+        raise RuntimeError(f"definition {pattern!r} not found in the reference source")
+    i = m.start()
+    semi, brace = text.find(";", i), text.find("{", i)
+    if brace < 0 or (0 <= semi < brace):
+        return text[i:semi + 1]
+    depth, j = 0, brace
+    while True:
+        c = text[j]
+        depth += c == "{"
+        depth -= c == "}"
+        j += 1
+        if depth == 0:
+            break
+    if text[j:j + 1] == ";":
+        j += 1
+    return text[i:j]
+
+
 def build_ref(force: bool = False) -> str | None:
     """Returns the library path, or None when the reference sources are absent."""
     shader_dir = os.path.join(REFERENCE, "shaders")
     if not os.path.isdir(shader_dir):
         return REF_SO if os.path.exists(REF_SO) else None
     sources = [os.path.join(shader_dir, s + ".hlsl") for s in SHADERS]
-    own = [os.path.join(HERE, f) for f in ("ref_shim.hpp", "ref_shaders.cpp", "ref_padding.cpp")]
+    own = [os.path.join(HERE, f) for f in ("ref_shim.hpp", "ref_shaders.cpp", "ref_padding.cpp", "ref_host.cpp")]
     padding = os.path.join(REFERENCE, "src", "texture_padding.cpp")
-    if not force and _newer(REF_SO, sources + own + [padding, __file__]):
+    rasterizer = os.path.join(REFERENCE, "src", "rasterizer.cpp")
+    if not force and _newer(REF_SO, sources + own + [padding, rasterizer, __file__]):
         return REF_SO
     gen = os.path.join(HERE, "_ref", "gen")
     os.makedirs(gen, exist_ok=True)
@@ -72,11 +111,16 @@ def build_ref(force: bool = False) -> str | None:
             text = _strip_hlsl(f.read())
         with open(os.path.join(gen, name + ".hlsl.inc"), "w", encoding="utf-8") as f:
             f.write(text)
+    with open(rasterizer, encoding="utf-8") as f:
+        host = f.read()
+    with open(os.path.join(gen, "rasterizer_host.inc"), "w", encoding="utf-8") as f:
+        f.write("\n\n".join(_definition(host, p) for p in HOST_DEFINITIONS) + "\n")
     tmp = REF_SO + f".tmp{os.getpid()}"
     subprocess.run(
         ["g++", "-std=c++20", *FP_FLAGS, "-Wno-attributes", "-I", HERE, "-I", gen,
          "-I", os.path.join(REFERENCE, "include"),
-         os.path.join(HERE, "ref_shaders.cpp"), os.path.join(HERE, "ref_padding.cpp"), padding,
+         os.path.join(HERE, "ref_shaders.cpp"), os.path.join(HERE, "ref_padding.cpp"),
+         os.path.join(HERE, "ref_host.cpp"), padding,
          "-o", tmp, "-lpthread"],
         check=True,
     )

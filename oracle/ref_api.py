@@ -1,11 +1,10 @@
 """NumPy face of ``libpdr_ref.so``: the reference's own HLSL shaders (and its CPU
 ``texture_padding.cpp``) compiled for the CPU. TEST INFRASTRUCTURE ONLY.
 
-The reference's host-side table builders cannot be compiled here (``src/rasterizer.cpp`` needs
-the absent Vulkan wrapper), so this module restates the two small ones it needs in NumPy:
-the vertex->corner table (src/rasterizer.cpp:145-162) and the texel->sample table with
-double-precision weights (src/rasterizer.cpp:187-258). Tile bins come from the oracle's
-restatement of build_tile_bins (src/rasterizer.cpp:61-138).
+The reference's host-side routines of the path come from its own source as well: tile binning
+(src/rasterizer.cpp:61-138 build_tile_bins), the vertex->corner table (:145-162) and the
+texel->sample table with double-precision weights (:187-258), cut out of ``src/rasterizer.cpp``
+by ``oracle/build.py`` (the rest of that file needs the absent Vulkan wrapper).
 """
 from __future__ import annotations
 
@@ -28,6 +27,8 @@ def _L():
     if L is None:
         raise RuntimeError("reference sources are not available on this machine")
     L.ref_suggest_softmax_scale.restype = C.c_float
+    L.ref_build_tile_bins.restype = C.c_int64
+    L.ref_build_texture_sample_adjacency.restype = C.c_int64
     return L
 
 
@@ -35,11 +36,29 @@ def _p(a, t=_f32p):
     return a.ctypes.data_as(t) if a is not None else None
 
 
+def bin_tiles(pos, idx, resolution, viewport=None):
+    """src/rasterizer.cpp:61-138 build_tile_bins: (offsets [tiles+1], ascending triangle ids)."""
+    pos, idx = api._f(pos), api._u(idx)
+    h, w = resolution
+    vp = api._vp(viewport, w, h)
+    tiles = ((w + 15) // 16) * ((h + 15) // 16)
+    offsets = np.zeros(tiles + 1, np.uint32)
+    L = _L()
+    n = L.ref_build_tile_bins(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp),
+                              _p(offsets, _u32p), None, C.c_uint64(0))
+    if n < 0:
+        raise OverflowError("Tile triangle list exceeds backend limits")
+    lst = np.zeros(max(n, 1), np.uint32)
+    L.ref_build_tile_bins(_p(pos), pos.shape[0], _p(idx, _u32p), idx.shape[0], w, h, _p(vp), _p(offsets, _u32p),
+                          _p(lst, _u32p), C.c_uint64(n))
+    return offsets, lst[:n]
+
+
 def rasterize_forward(pos, idx, resolution, cull_mode=0, output_derivatives=True, viewport=None):
     pos, idx = api._f(pos), api._u(idx)
     h, w = resolution
     vp = api._vp(viewport, w, h)
-    offsets, lst = api.bin_tiles(pos, idx, resolution, vp)
+    offsets, lst = bin_tiles(pos, idx, resolution, vp)
     lst = np.ascontiguousarray(lst if lst.size else np.zeros(1, np.uint32))
     raster = np.zeros((h, w, 4), np.float32)
     deriv = np.zeros((h, w, 4), np.float32)
@@ -50,13 +69,12 @@ def rasterize_forward(pos, idx, resolution, cull_mode=0, output_derivatives=True
 
 
 def vertex_corner_table(idx, V):
-    """src/rasterizer.cpp:145-162: CSR of corners per vertex, corners ascending."""
-    flat = np.asarray(idx, dtype=np.uint32).reshape(-1)
+    """src/rasterizer.cpp:145-162 build_vertex_adjacency: CSR of corners per vertex."""
+    idx = api._u(idx)
     offsets = np.zeros(V + 1, np.uint32)
-    np.add.at(offsets, flat.astype(np.int64) + 1, 1)
-    offsets = np.cumsum(offsets).astype(np.uint32)
-    corners = np.argsort(flat, kind="stable").astype(np.uint32)
-    return offsets, corners
+    corners = np.zeros(max(idx.size, 1), np.uint32)
+    _L().ref_build_vertex_adjacency(_p(idx, _u32p), idx.shape[0], V, _p(offsets, _u32p), _p(corners, _u32p))
+    return offsets, corners[:idx.size]
 
 
 def rasterize_backward(pos, idx, raster, grad_raster, viewport=None):
@@ -103,47 +121,25 @@ def texture_forward(tex, uv, raster, address_mode="clamp"):
     return out
 
 
-def _address(c, size, mode):
-    c = c.astype(np.int64)
-    if mode == 0:
-        return np.clip(c, 0, size - 1)
-    if mode == 1:
-        return np.mod(c, size)
-    period = 2 * size
-    m = np.mod(c, period)
-    return np.where(m < size, m, period - 1 - m)
-
-
 def texture_sample_table(uv, raster, tw, th, mode):
-    """src/rasterizer.cpp:187-258 restated: texel CSR of sample entries and float weights from
-    double-precision texel positions."""
-    uv = np.asarray(uv, np.float32).reshape(-1, 2)
-    r3 = np.asarray(raster, np.float32).reshape(-1, 4)[:, 3]
-    P = uv.shape[0]
-    covered = r3 != 0.0
-    tx = uv[:, 0].astype(np.float64) * tw - 0.5
-    ty = uv[:, 1].astype(np.float64) * th - 0.5
-    bx, by = np.floor(tx), np.floor(ty)
-    fx = (tx - bx).astype(np.float32)
-    fy = (ty - by).astype(np.float32)
-    one = np.float32(1.0)
-    weights = np.stack([(one - fx) * (one - fy), fx * (one - fy), (one - fx) * fy, fx * fy], axis=1)
-    weights[~covered] = 0.0
-    bx = np.where(covered, bx, 0).astype(np.int64)
-    by = np.where(covered, by, 0).astype(np.int64)
-    xs = [_address(bx, tw, mode), _address(bx + 1, tw, mode)]
-    ys = [_address(by, th, mode), _address(by + 1, th, mode)]
-    texels = np.stack([ys[0] * tw + xs[0], ys[0] * tw + xs[1], ys[1] * tw + xs[0], ys[1] * tw + xs[1]], axis=1)
-    entries = np.arange(P * 4, dtype=np.int64)
-    valid = np.repeat(covered, 4)
-    tex_of_entry = texels.reshape(-1)[valid]
-    ent = entries[valid]
-    order = np.argsort(tex_of_entry, kind="stable")
-    offsets = np.zeros(tw * th + 1, np.int64)
-    np.add.at(offsets, tex_of_entry + 1, 1)
-    offsets = np.cumsum(offsets)
-    return (offsets.astype(np.uint32), np.ascontiguousarray(ent[order].astype(np.uint32)),
-            np.ascontiguousarray(weights.reshape(-1).astype(np.float32)))
+    """src/rasterizer.cpp:187-258 build_texture_sample_adjacency: texel CSR of sample entries and
+    float weights from double-precision texel positions."""
+    uv, raster = api._f(uv), api._f(raster)
+    h, w = raster.shape[:2]
+    P = h * w
+    offsets = np.zeros(tw * th + 1, np.uint32)
+    weights = np.zeros(P * 4, np.float32)
+    L = _L()
+    n = L.ref_build_texture_sample_adjacency(_p(uv), _p(raster), w, h, tw, th, mode, _p(offsets, _u32p), None,
+                                             C.c_uint64(0), _p(weights))
+    if n == -1:
+        raise ValueError("uv contains a non-finite value in a covered pixel")
+    if n == -2:
+        raise IndexError("uv is too large for portable texture addressing")
+    entries = np.zeros(max(n, 1), np.uint32)
+    L.ref_build_texture_sample_adjacency(_p(uv), _p(raster), w, h, tw, th, mode, _p(offsets, _u32p),
+                                         _p(entries, _u32p), C.c_uint64(n), _p(weights))
+    return offsets, entries[:n], weights
 
 
 def texture_backward(tex, uv, raster, grad, address_mode="clamp", compute_uv_gradient=True):

@@ -120,6 +120,8 @@ pdr_status pdr_bin_tiles(const float* clip, uint32_t views, uint32_t V, const ui
     pdr_status st = check_raster_args(clip, views, V, idx, T, W, H, viewports);
     if (st) return st;
     if (!offsets || !status || (capacity && !list)) return fail(PDR_INVALID_ARGUMENT, "tile_offsets, tile_triangles and status are required");
+    // tile offsets are u32: a larger capacity means nothing and would wrap the workspace size
+    if (capacity > 0xffffffffull) return fail(PDR_OVERFLOW, "tile list capacity exceeds the u32 tile offsets");
     if (workspace_bytes < bins_workspace_bytes(views, T, W, H, capacity) || !workspace)
         return fail(PDR_INVALID_ARGUMENT, "workspace is smaller than pdr_bin_tiles_workspace_bytes()");
     return cuda_status(launch_bin_tiles(clip, views, V, idx, T, W, H, viewports, offsets, list, capacity, workspace,

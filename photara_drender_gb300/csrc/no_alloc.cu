@@ -9,6 +9,9 @@
 // The array lives in device memory of every GPU that loads this library, for the life of the
 // process. Its address is looked up once per device (cudaGetSymbolAddress, with that device
 // current) on the first call made on that device; make that first call before any stream capture.
+// The looked-up address is kept for the life of the process: do not use this entry point across a
+// device reset (cudaDeviceReset, or a primary context released and created again), after which the
+// array may sit at another address.
 // All calls share the one array, so calls that overlap on the GPU (different streams, or different
 // host threads without ordering) race with each other: serialise them.
 #include <cuda_runtime.h>
@@ -61,19 +64,22 @@ pdr_status pdr_bin_tiles_no_alloc(const float* clip_positions, uint32_t views, u
                                   const uint32_t* indices, uint32_t triangle_count, uint32_t width, uint32_t height,
                                   const float* viewports, uint32_t* tile_offsets, uint32_t* tile_triangles,
                                   uint64_t capacity, uint32_t* status, void* stream) {
-    if (!clip_positions || !indices || !viewports || !tile_offsets || !status || (capacity && !tile_triangles))
-        return set_error(PDR_INVALID_ARGUMENT, "clip_positions, indices, viewports, tile bins and status are required");
-    if (views == 0 || vertex_count == 0 || triangle_count == 0 || width == 0 || height == 0)
-        return set_error(PDR_INVALID_ARGUMENT, "binning dimensions must be positive");
-    if (width > 65535u * kTile || height > 65535u * kTile)
-        return set_error(PDR_OVERFLOW, "Rasterization output size overflow");
+    // the same shape, size and alignment checks as pdr_bin_tiles: the count kernel reads clip
+    // positions and viewports as float4, so a misaligned pointer is refused here, before any launch
+    pdr_status st = check_raster_args(clip_positions, views, vertex_count, indices, triangle_count, width, height,
+                                      viewports);
+    if (st != PDR_OK) return st;
+    if (!tile_offsets || !status || (capacity && !tile_triangles))
+        return set_error(PDR_INVALID_ARGUMENT, "tile_offsets, tile_triangles and status are required");
+    // tile offsets are u32: a larger capacity means nothing and would wrap the size computation below
+    if (capacity > 0xffffffffull) return set_error(PDR_OVERFLOW, "tile list capacity exceeds the u32 tile offsets");
     const size_t need = bins_workspace_bytes(views, triangle_count, width, height, capacity);
     if (need > kStaticScratchBytes)
         return set_error(PDR_INVALID_ARGUMENT,
                          "pdr_bin_tiles_no_alloc: this binning needs more scratch than the library's fixed "
                          "PDR_BIN_TILES_NO_ALLOC_SCRATCH_BYTES array; use pdr_bin_tiles with a caller workspace");
     void* scratch = nullptr;
-    pdr_status st = scratch_address(&scratch);
+    st = scratch_address(&scratch);
     if (st != PDR_OK) return st;
     // launch_bin_tiles clears the per-tile counters itself (cudaMemsetAsync); every other scratch
     // word is written before it is read, so leftovers of the previous call do not matter.

@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("PDR_REFERENCE_DIR", "/root/reference")  # the reference checkout
 
 
 def load_reference_atlas():

@@ -12,7 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))  # the repository root
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("PDR_REFERENCE_DIR", "/root/reference")  # the reference checkout
 
 from photara_drender_gb300 import synthetic as S  # noqa: E402
 

@@ -65,3 +65,32 @@ def test_cpp_api_library_builds_and_links():
                     exe, "-L", os.path.dirname(lib), "-lphotara_drender", f"-Wl,-rpath,{os.path.dirname(lib)}"],
                    check=True)
     assert os.path.exists(exe)
+
+
+def test_binning_argument_checks_without_gpu():
+    """Both binning entry points refuse, before any launch, clip positions or viewports that are not
+    16-byte aligned (the count kernel reads them as float4) and a tile-list capacity beyond the u32
+    offsets. The pointers are never dereferenced: the checks answer on a machine without a GPU."""
+    import ctypes as C
+
+    from photara_drender_gb300 import _native
+
+    L = _native.lib()
+    fn = L.pdr_bin_tiles_no_alloc
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
+    base = 1 << 20  # a 16-byte aligned stand-in address
+    clip, idx, vps, off, lst, status = (C.c_void_p(base + k * 4096) for k in range(6))
+    odd = C.c_void_p(base + 4)
+    with pytest.raises(ValueError, match="16-byte aligned"):
+        _native.check(fn(odd, 1, 3, idx, 1, 32, 32, vps, off, lst, 64, status, None))
+    with pytest.raises(ValueError, match="16-byte aligned"):
+        _native.check(fn(clip, 1, 3, idx, 1, 32, 32, odd, off, lst, 64, status, None))
+    with pytest.raises(OverflowError, match="capacity"):
+        _native.check(fn(clip, 1, 3, idx, 1, 32, 32, vps, off, lst, 1 << 62, status, None))
+    ws = C.c_void_p(base + 8 * 4096)
+    with pytest.raises(ValueError, match="16-byte aligned"):
+        _native.check(L.pdr_bin_tiles(odd, 1, 3, idx, 1, 32, 32, vps, off, lst, 64, ws, 1 << 30, status, None))
+    with pytest.raises(OverflowError, match="capacity"):
+        _native.check(L.pdr_bin_tiles(clip, 1, 3, idx, 1, 32, 32, vps, off, lst, 1 << 62, ws, 1 << 30, status, None))
