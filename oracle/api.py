@@ -51,6 +51,9 @@ def _declare(L):
     L.ora_photometric_gradient.restype = C.c_float
     L.ora_seam_gradient.restype = C.c_float
     L.ora_tv_gradient.restype = C.c_double
+    L.ora_photometric_gradient_f64.restype = C.c_double
+    L.ora_seam_gradient_f64.restype = C.c_double
+    L.ora_tv_gradient_f64.restype = C.c_double
 
 
 def _p(a, t=_f32p):
@@ -294,7 +297,9 @@ def refine_options(width, height, steps=1000, batch_size=4, learning_rate=5e-3, 
 
 
 def refine(initial_texture, positions, uv, indices, images, world_to_clip, *, visibility_masks=None, viewports=None,
-           seam_uv_pairs=None, **kw):
+           seam_uv_pairs=None, reverse_order=False, **kw):
+    """TextureRefiner::refine (texture_refiner.cpp:256-415). reverse_order visits pixels and seam pairs
+    in reverse: another order the reference's atomic additions may take on a GPU."""
     init = _f(initial_texture)
     h, w, _ = init.shape
     o = refine_options(w, h, **kw)
@@ -306,8 +311,12 @@ def refine(initial_texture, positions, uv, indices, images, world_to_clip, *, vi
     loss = np.zeros(o.steps, dtype=np.float32)
     seam_steps = 0 if npairs == 0 else o.seam_polish_steps
     seam = np.zeros(seam_steps, dtype=np.float32)
-    _check(lib().ora_refine(_p(init), _p(pos), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views, len(images),
-                            _p(pairs), npairs, C.byref(o), _p(out), _p(loss), _p(seam)))
+    lib().ora_set_reverse_order(int(bool(reverse_order)))
+    try:
+        _check(lib().ora_refine(_p(init), _p(pos), _p(uvv), pos.shape[0], _p(idx, _u32p), idx.shape[0], views,
+                                len(images), _p(pairs), npairs, C.byref(o), _p(out), _p(loss), _p(seam)))
+    finally:
+        lib().ora_set_reverse_order(0)
     del keep
     return out, loss, seam
 
@@ -326,19 +335,32 @@ def refine_view_cache(positions, uv, indices, image, world_to_clip, visibility_m
     return uv_out, tgt, msk, vw.value
 
 
-def photometric_gradient(tex3, uv, target, mask, eps, normalization, grad=None):
+def photometric_gradient(tex3, uv, target, mask, eps, normalization, grad=None, f64=False, abs_terms=False):
+    """atlas_photometric_gradient.hlsl for one view: (gradient added into `grad`, loss). With f64 the
+    FP64 twin (gradient float64; abs_terms accumulates |term|)."""
     tex3, uv, target, mask = _f(tex3), _f(uv), _f(target), _f(mask)
     th, tw, _ = tex3.shape
-    g = np.zeros_like(tex3) if grad is None else grad
     P = int(np.prod(mask.shape))
+    if f64:
+        g = np.zeros(tex3.shape, np.float64) if grad is None else grad
+        loss = lib().ora_photometric_gradient_f64(_p(tex3), tw, th, _p(uv), _p(target), _p(mask), P, C.c_float(eps),
+                                                  C.c_float(normalization), g.ctypes.data_as(_f64p), int(abs_terms))
+        return g, loss
+    g = np.zeros_like(tex3) if grad is None else grad
     loss = lib().ora_photometric_gradient(_p(tex3), tw, th, _p(uv), _p(target), _p(mask), P, C.c_float(eps),
                                           C.c_float(normalization), _p(g))
     return g, loss
 
 
-def seam_gradient(tex3, pairs, eps, normalization, grad=None):
+def seam_gradient(tex3, pairs, eps, normalization, grad=None, f64=False, abs_terms=False):
+    """atlas_seam_gradient.hlsl: (gradient added into `grad`, loss); f64 / abs_terms as above."""
     tex3, pairs = _f(tex3), _f(pairs)
     th, tw, _ = tex3.shape
+    if f64:
+        g = np.zeros(tex3.shape, np.float64) if grad is None else grad
+        loss = lib().ora_seam_gradient_f64(_p(tex3), tw, th, _p(pairs), pairs.shape[0], C.c_float(eps),
+                                           C.c_float(normalization), g.ctypes.data_as(_f64p), int(abs_terms))
+        return g, loss
     g = np.zeros_like(tex3) if grad is None else grad
     loss = lib().ora_seam_gradient(_p(tex3), tw, th, _p(pairs), pairs.shape[0], C.c_float(eps),
                                    C.c_float(normalization), _p(g))
@@ -351,11 +373,16 @@ def adam_update(tex, grad, m, v, lr, b1, b2, eps, bc1, bc2, cmin, cmax):
                           C.c_float(cmax))
 
 
-def tv_gradient(tex, valid=None, chart=None, eps=1e-4, weight=1.0, grad=None):
+def tv_gradient(tex, valid=None, chart=None, eps=1e-4, weight=1.0, grad=None, f64=False, abs_terms=False):
     tex = _f(tex)
     th, tw, Cc = tex.shape
     valid = np.ones((th, tw), np.uint8) if valid is None else np.ascontiguousarray(valid, dtype=np.uint8)
     chart = None if chart is None else np.ascontiguousarray(chart, dtype=np.int32)
+    if f64:
+        g = np.zeros(tex.shape, np.float64) if grad is None else grad
+        loss = lib().ora_tv_gradient_f64(_p(tex), tw, th, Cc, _p(valid, _u8p), _p(chart, _i32p), C.c_float(eps),
+                                         C.c_float(weight), g.ctypes.data_as(_f64p), int(abs_terms))
+        return g, loss
     g = np.zeros_like(tex) if grad is None else grad
     loss = lib().ora_tv_gradient(_p(tex), tw, th, Cc, _p(valid, _u8p), _p(chart, _i32p), C.c_float(eps),
                                  C.c_float(weight), _p(g))

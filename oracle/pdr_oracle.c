@@ -947,6 +947,12 @@ static void clamp_layout(float u, float v, uint32_t tw, uint32_t th, uint32_t tx
     w[3] = fx * fy;
 }
 
+/* Order in which the two refiner gradients visit pixels / seam pairs. The reference adds with
+ * atomics, so on a GPU any order is one the reference may take; reversing it gives a second valid
+ * accumulation order, and the two results bound the reference's own order noise. */
+static int g_reverse_order = 0;
+void ora_set_reverse_order(int reverse) { g_reverse_order = reverse != 0; }
+
 /* atlas_photometric_gradient.hlsl:45-108: per-pixel math in pixel order; the loss is
  * reduced per 64-pixel group with the shader's tree, then groups in order. */
 float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const float* uv,
@@ -956,7 +962,7 @@ float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const
     float group[64];
     for (uint32_t g0 = 0; g0 < P; g0 += 64) {
         for (uint32_t gi = 0; gi < 64; ++gi) {
-            const uint32_t p = g0 + gi;
+            const uint32_t p = g_reverse_order ? (g0 + gi < P ? P - 1 - (g0 + gi) : P) : g0 + gi;
             float local = 0.0f;
             if (p < P) {
                 const float m = mask[p];
@@ -990,7 +996,7 @@ float ora_seam_gradient(const float* tex, uint32_t tw, uint32_t th, const float*
     float group[64];
     for (uint32_t g0 = 0; g0 < npairs; g0 += 64) {
         for (uint32_t gi = 0; gi < 64; ++gi) {
-            const uint32_t i = g0 + gi;
+            const uint32_t i = g_reverse_order ? (g0 + gi < npairs ? npairs - 1 - (g0 + gi) : npairs) : g0 + gi;
             float local = 0.0f;
             if (i < npairs) {
                 uint32_t t0[4], t1[4];
@@ -1018,6 +1024,78 @@ float ora_seam_gradient(const float* tex, uint32_t tw, uint32_t th, const float*
         for (uint32_t stride = 32; stride > 0; stride >>= 1)
             for (uint32_t gi = 0; gi < stride; ++gi) group[gi] += group[gi + stride];
         if (group[0] != 0.0f) loss += group[0];
+    }
+    return loss;
+}
+
+/* FP64 twins of the two refiner gradients: the same taps (texel positions and weights from the
+ * fp32 uv, computed exactly in double), every product and sum in double. With abs_terms the gradient
+ * accumulates |term| (the sum of absolute terms that bounds summation-order error). Return the loss. */
+static void clamp_layout_f64(float u, float v, uint32_t tw, uint32_t th, uint32_t tx[4], double w[4]) {
+    const double px = (double)u * tw - 0.5, py = (double)v * th - 0.5;
+    const double flx = floor(px), fly = floor(py);
+    const int32_t bx = d2i_sat(flx), by = d2i_sat(fly);
+    const double fx = px - flx, fy = py - fly;
+    const uint32_t x0 = (uint32_t)clampi(bx, 0, (int32_t)tw - 1), x1 = (uint32_t)clampi(add1(bx), 0, (int32_t)tw - 1);
+    const uint32_t y0 = (uint32_t)clampi(by, 0, (int32_t)th - 1), y1 = (uint32_t)clampi(add1(by), 0, (int32_t)th - 1);
+    tx[0] = y0 * tw + x0;
+    tx[1] = y0 * tw + x1;
+    tx[2] = y1 * tw + x0;
+    tx[3] = y1 * tw + x1;
+    w[0] = (1.0 - fx) * (1.0 - fy);
+    w[1] = fx * (1.0 - fy);
+    w[2] = (1.0 - fx) * fy;
+    w[3] = fx * fy;
+}
+
+double ora_photometric_gradient_f64(const float* tex, uint32_t tw, uint32_t th, const float* uv,
+                                    const float* target, const float* mask, uint32_t P, float eps,
+                                    float norm, double* grad, int abs_terms) {
+    double loss = 0.0;
+    const double e = eps, n = norm;
+    for (uint32_t p = 0; p < P; ++p) {
+        const double m = mask[p];
+        if (!(m > 0.0)) continue;
+        uint32_t tx[4];
+        double w[4];
+        clamp_layout_f64(uv[(uint64_t)p * 2], uv[(uint64_t)p * 2 + 1], tw, th, tx, w);
+        for (uint32_t c = 0; c < 3; ++c) {
+            double rendered = 0.0;
+            for (int k = 0; k < 4; ++k) rendered += (double)tex[(uint64_t)tx[k] * 3 + c] * w[k];
+            const double d = rendered - target[(uint64_t)p * 3 + c];
+            const double robust = sqrt(d * d + e * e);
+            const double og = d / robust * m * n;
+            loss += robust * m * n;
+            for (int k = 0; k < 4; ++k) grad[(uint64_t)tx[k] * 3 + c] += abs_terms ? fabs(og * w[k]) : og * w[k];
+        }
+    }
+    return loss;
+}
+
+double ora_seam_gradient_f64(const float* tex, uint32_t tw, uint32_t th, const float* pairs, uint32_t npairs,
+                             float eps, float norm, double* grad, int abs_terms) {
+    double loss = 0.0;
+    const double e = eps, n = norm;
+    for (uint32_t i = 0; i < npairs; ++i) {
+        uint32_t t0[4], t1[4];
+        double w0[4], w1[4];
+        clamp_layout_f64(pairs[(uint64_t)i * 4], pairs[(uint64_t)i * 4 + 1], tw, th, t0, w0);
+        clamp_layout_f64(pairs[(uint64_t)i * 4 + 2], pairs[(uint64_t)i * 4 + 3], tw, th, t1, w1);
+        for (uint32_t c = 0; c < 3; ++c) {
+            double c0 = 0.0, c1 = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                c0 += (double)tex[(uint64_t)t0[k] * 3 + c] * w0[k];
+                c1 += (double)tex[(uint64_t)t1[k] * 3 + c] * w1[k];
+            }
+            const double d = c0 - c1;
+            const double robust = sqrt(d * d + e * e);
+            const double g = d / robust * n;
+            loss += robust * n;
+            for (int k = 0; k < 4; ++k) {
+                grad[(uint64_t)t0[k] * 3 + c] += abs_terms ? fabs(g * w0[k]) : g * w0[k];
+                grad[(uint64_t)t1[k] * 3 + c] += abs_terms ? fabs(g * w1[k]) : -g * w1[k];
+            }
+        }
     }
     return loss;
 }
@@ -1180,6 +1258,40 @@ double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C, c
             }
         }
     return loss * (double)weight / denom;
+}
+
+/* FP64 twin of ora_tv_gradient (abs_terms as above); returns the weighted loss. */
+double ora_tv_gradient_f64(const float* tex, uint32_t tw, uint32_t th, uint32_t C, const uint8_t* valid,
+                           const int32_t* chart, float eps, float weight, double* grad, int abs_terms) {
+    uint64_t pairs = 0;
+    for (uint32_t y = 0; y < th; ++y)
+        for (uint32_t x = 0; x < tw; ++x) {
+            const uint64_t i = (uint64_t)y * tw + x;
+            if (x + 1 < tw && valid[i] && valid[i + 1] && (!chart || chart[i] == chart[i + 1])) pairs++;
+            if (y + 1 < th && valid[i] && valid[i + tw] && (!chart || chart[i] == chart[i + tw])) pairs++;
+        }
+    const double scale = (double)weight / ((double)(pairs > 0 ? pairs : 1) * C);
+    const double e = eps;
+    double loss = 0.0;
+    for (uint32_t y = 0; y < th; ++y)
+        for (uint32_t x = 0; x < tw; ++x) {
+            const uint64_t i = (uint64_t)y * tw + x;
+            for (int dir = 0; dir < 2; ++dir) {
+                uint64_t j;
+                if (dir == 0) { if (x + 1 >= tw) continue; j = i + 1; }
+                else { if (y + 1 >= th) continue; j = i + tw; }
+                if (!(valid[i] && valid[j] && (!chart || chart[i] == chart[j]))) continue;
+                for (uint32_t c = 0; c < C; ++c) {
+                    const double d = (double)tex[j * C + c] - (double)tex[i * C + c];
+                    const double r = sqrt(d * d + e * e);
+                    loss += r * scale;
+                    const double gg = d / r * scale;
+                    grad[j * C + c] += abs_terms ? fabs(gg) : gg;
+                    grad[i * C + c] += abs_terms ? fabs(gg) : -gg;
+                }
+            }
+        }
+    return loss;
 }
 
 /* ---- ray-query visibility ------------------------------------------------------------------ */

@@ -145,6 +145,15 @@ float ora_photometric_gradient(const float* tex3, uint32_t tw, uint32_t th, cons
 /* atlas_seam_gradient.hlsl */
 float ora_seam_gradient(const float* tex3, uint32_t tw, uint32_t th, const float* pairs,
                         uint32_t npairs, float eps, float normalization, float* grad);
+/* FP64 twins of the two gradients above (abs_terms: accumulate |term|); return the loss. */
+double ora_photometric_gradient_f64(const float* tex3, uint32_t tw, uint32_t th, const float* uv,
+                                    const float* target3, const float* mask, uint32_t P, float eps,
+                                    float normalization, double* grad, int abs_terms);
+double ora_seam_gradient_f64(const float* tex3, uint32_t tw, uint32_t th, const float* pairs,
+                             uint32_t npairs, float eps, float normalization, double* grad, int abs_terms);
+/* Visit pixels and seam pairs in reverse order in the two functions above (and in ora_refine): a
+ * second accumulation order of the reference's atomics, for stating order noise. Process-wide. */
+void ora_set_reverse_order(int reverse);
 /* atlas_adam_update.hlsl */
 void ora_adam_update(float* tex, float* grad, float* m, float* v, uint64_t n, float lr, float b1,
                      float b2, float eps, float bc1, float bc2, float cmin, float cmax);
@@ -174,6 +183,11 @@ int ora_refine_view_cache(const float* pos3, const float* uv2, uint32_t V, const
 double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C,
                        const uint8_t* valid, const int32_t* chart, float eps, float weight,
                        float* grad);
+
+/* FP64 twin of ora_tv_gradient (abs_terms: accumulate |term|); returns the weighted loss. */
+double ora_tv_gradient_f64(const float* tex, uint32_t tw, uint32_t th, uint32_t C,
+                           const uint8_t* valid, const int32_t* chart, float eps, float weight,
+                           double* grad, int abs_terms);
 
 /* src/texture_padding.cpp:37-95: the 8SSEDT nearest-source offsets (sources: mask >= threshold). */
 int ora_nearest_field_offsets(const float* source_mask, uint32_t width, uint32_t height, float threshold,

@@ -36,3 +36,38 @@ def grad_check(gpu, ora32, ora64, abs64=None, rtol=1e-5, noise=2e-6, name=""):
     rel = float((err / np.where(denom > 0, denom, 1)).max())
     rel_abs = float((err / np.where(a64 > 0, a64, np.inf)).max()) if abs64 is not None else 0.0
     return rel, rel_abs
+
+
+def oracle_render_chain(api, clip, idx, uva, attrs, tex, g_attr, g_samp, res, mode="clamp", viewport=None,
+                        acc=None):
+    """One view through the oracle in the reference's order: rasterize -> interpolate(attributes),
+    interpolate(uv) -> texture, then texture_grad_texture / texture_grad_uv, both interpolate adjoints and
+    rasterize_backward for the summed raster gradient, each in fp32 (reference order), FP64 and FP64 of
+    |terms|. Returns the forward outputs and the per-view clip gradients; the texture, attribute and uv
+    attribute gradients are added into `acc` (a dict, summed over the views passed)."""
+    r, d = api.rasterize_forward(clip, idx, res, viewport=viewport)
+    a = api.interpolate_forward(attrs, idx, r)
+    uv = api.interpolate_forward(uva, idx, r)
+    s = api.texture_forward(tex, uv, r, mode)
+    gt, gu = api.texture_backward(tex, uv, r, g_samp, mode)
+    gt64 = api.texture_backward(tex, uv, r, g_samp, mode, f64=True)[0]
+    gtab = api.texture_backward(tex, uv, r, g_samp, mode, f64=True, abs_terms=True)[0]
+    guv, gr1 = api.interpolate_backward(uva, idx, r, gu)
+    ga, gr2 = api.interpolate_backward(attrs, idx, r, g_attr)
+    sums = {
+        "grad_tex": (gt, gt64, gtab),
+        "grad_uv_attr": (guv, api.interpolate_backward(uva, idx, r, gu, f64=True)[0],
+                         api.interpolate_backward(uva, idx, r, gu, f64=True, abs_terms=True)[0]),
+        "grad_attr": (ga, api.interpolate_backward(attrs, idx, r, g_attr, f64=True)[0],
+                      api.interpolate_backward(attrs, idx, r, g_attr, f64=True, abs_terms=True)[0]),
+    }
+    if acc is not None:
+        for k, trio in sums.items():
+            prev = acc.get(k)
+            acc[k] = tuple(t.astype(np.float64) + (0.0 if prev is None else p) for t, p in
+                           zip(trio, prev if prev is not None else (None,) * 3))
+    grs = (gr1 + gr2).astype(np.float32)
+    clip_grads = (api.rasterize_backward(clip, idx, r, grs, viewport=viewport),
+                  api.rasterize_backward(clip, idx, r, grs, viewport=viewport, f64=True),
+                  api.rasterize_backward(clip, idx, r, grs, viewport=viewport, f64=True, abs_terms=True))
+    return {"raster": r, "deriv": d, "attr_out": a, "uv": uv, "sampled": s}, clip_grads

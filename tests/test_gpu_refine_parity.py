@@ -1,0 +1,268 @@
+"""GPU parity of the atlas refiner's gradients and of the refine loop over many steps.
+
+* The seam kernel on its own (atlas_seam_gradient.hlsl:50-100) against the oracle's FP64 twin
+  (tests/gpu_util.grad_check), on chart seams of a displaced sphere plus random pairs.
+* The photometric, seam and total-variation kernels against central finite differences of the FP64
+  objective at sampled texels, on a small atlas.
+* One full gradient step at the 4096x4096 atlas of the refinement benchmark: four 2048x1536 views
+  (photometric), the chart-aware TV and the seam gradient added into one gradient buffer, against the
+  FP64 sum of the three.
+* 200 refine steps plus a 30-step seam polish on a mid-size scene: the reference adds its gradients
+  with atomics, so its result depends on the accumulation order. The oracle run in pixel order and in
+  reverse order gives that order noise; the GPU run must stay within a small multiple of it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import api
+from photara_drender_gb300 import synthetic as S
+from tests.gpu_util import grad_check
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda", 0)
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream(DEV).cuda_stream)
+
+
+def _t(a):
+    return torch.tensor(np.ascontiguousarray(a), device=DEV)
+
+
+def gpu_seam(tex, pairs, eps, norm):
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    th, tw, _ = tex.shape
+    t_tex, t_pairs = _t(tex), _t(pairs.reshape(-1, 4))
+    grad = torch.zeros((th, tw, 4), dtype=torch.float32, device=DEV)
+    loss = torch.zeros(2, dtype=torch.float32, device=DEV)
+    _native.call("pdr_refine_seam", _ptr(t_tex), tw, th, _ptr(t_pairs), pairs.shape[0], C.c_float(eps),
+                 C.c_float(norm), _ptr(grad), _ptr(loss), 1, _stream())
+    torch.cuda.synchronize()
+    assert not grad[..., 3].any()
+    return grad[..., :3].cpu().numpy(), float(loss[1])
+
+
+def view_table(views):
+    """Device table of pdr_refine_view records for [(uv, target, mask)] device tensors."""
+    from photara_drender_gb300.baking import RefineViewC
+
+    table = (RefineViewC * len(views))()
+    for k, (uv, tgt, mask) in enumerate(views):
+        table[k].uv, table[k].target, table[k].mask = uv.data_ptr(), tgt.data_ptr(), mask.data_ptr()
+        table[k].pixel_count = mask.numel()
+    return torch.frombuffer(bytearray(bytes(table)), dtype=torch.uint8).to(DEV)
+
+
+def gpu_photometric(tex, views, eps, norm, grad=None, loss=None):
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    th, tw, _ = tex.shape
+    t_views = [tuple(_t(a) for a in v) for v in views]
+    table = view_table(t_views)
+    if grad is None:
+        grad = torch.zeros((th, tw, 4), dtype=torch.float32, device=DEV)
+    if loss is None:
+        loss = torch.zeros(1, dtype=torch.float32, device=DEV)
+    t_tex = _t(tex)
+    _native.call("pdr_refine_photometric", _ptr(t_tex), tw, th, _ptr(table), len(views),
+                 max(v[2].size for v in views), 0, len(views), C.c_float(eps), C.c_float(norm), _ptr(grad), _ptr(loss),
+                 _stream())
+    torch.cuda.synchronize()
+    return grad, loss
+
+
+def gpu_tv(tex, valid, chart, eps, weight, grad=None):
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    th, tw, _ = tex.shape
+    ok_h = valid[:, 1:] & valid[:, :-1] & (chart[:, 1:] == chart[:, :-1])
+    ok_v = valid[1:, :] & valid[:-1, :] & (chart[1:, :] == chart[:-1, :])
+    scale = np.float32(weight / (max(int(ok_h.sum() + ok_v.sum()), 1) * 3.0))
+    if grad is None:
+        grad = torch.zeros((th, tw, 4), dtype=torch.float32, device=DEV)
+    t_tex, t_valid, t_chart = _t(tex), _t(valid.astype(np.uint8)), _t(chart.astype(np.int32))
+    _native.call("pdr_refine_total_variation", _ptr(t_tex), tw, th, _ptr(t_valid), _ptr(t_chart), C.c_float(eps),
+                 C.c_float(float(scale)), _ptr(grad), _stream())
+    torch.cuda.synchronize()
+    return grad
+
+
+def seam_pairs(tw, seed):
+    rng = np.random.default_rng(seed)
+    pos3, _, uv, idx, chart, remap = S.displaced_sphere(20_000, seed=seed, atlas_size=tw)
+    pairs = S.seam_uv_pairs(uv, idx, remap, chart, samples_per_edge=4).astype(np.float32)
+    extra = rng.uniform(-0.02, 1.02, size=(5000, 2, 2)).astype(np.float32)
+    return np.concatenate([pairs, extra])
+
+
+@pytest.mark.parametrize("size", [(64, 48), (512, 512)])
+def test_seam_kernel_against_oracle(size):
+    th, tw = size
+    rng = np.random.default_rng(th)
+    tex = rng.uniform(size=(th, tw, 3)).astype(np.float32)
+    pairs = seam_pairs(tw, th)
+    for eps in (1e-4, 1e-2):
+        norm = 1.0 / (pairs.shape[0] * 3)
+        g, loss = gpu_seam(tex, pairs, eps, norm)
+        g32, l32 = api.seam_gradient(tex, pairs, eps, norm)
+        g64, l64 = api.seam_gradient(tex, pairs, eps, norm, f64=True)
+        gab, _ = api.seam_gradient(tex, pairs, eps, norm, f64=True, abs_terms=True)
+        rel, rel_abs = grad_check(g, g32, g64, gab, name=f"seam {size} eps {eps}")
+        assert abs(loss - l64) <= 1e-5 * abs(l64), (loss, l32, l64)
+        print(f"\nseam {size} eps {eps}: {pairs.shape[0]} pairs, worst {rel:.2e} / {rel_abs:.2e}, "
+              f"loss {loss:.7g} vs f64 {l64:.7g}")
+
+
+def fd_scene(seed=0, th=40, tw=48, P=6000):
+    rng = np.random.default_rng(seed)
+    tex = rng.uniform(0.05, 0.95, size=(th, tw, 3)).astype(np.float32)
+    uv = rng.uniform(-0.05, 1.05, size=(P, 2)).astype(np.float32)
+    tgt = (rng.uniform(size=(P, 3)) * 0.8 + 0.1).astype(np.float32)
+    mask = ((rng.uniform(size=P) > 0.25) * rng.uniform(0.2, 1.0, size=P)).astype(np.float32)
+    valid = rng.uniform(size=(th, tw)) < 0.85
+    chart = ((np.arange(tw)[None, :] // 13) + 5 * (np.arange(th)[:, None] // 11)).astype(np.int32)
+    return tex, uv, tgt, mask, valid, chart
+
+
+@pytest.mark.parametrize("kind", ["photometric", "seam", "tv"])
+def test_refine_gradients_against_finite_differences(kind):
+    """GPU gradient at 60 sampled texel channels against central differences of the FP64 objective
+    (the perturbed texture values are fp32, the difference quotient uses the exact perturbation)."""
+    tex, uv, tgt, mask, valid, chart = fd_scene()
+    th, tw, _ = tex.shape
+    if kind == "photometric":
+        eps, norm = 1e-3, 1e-3
+        g = gpu_photometric(tex, [(uv, tgt, mask)], eps, norm)[0][..., :3].cpu().numpy()
+        f = lambda t: api.photometric_gradient(t, uv, tgt, mask, eps, norm, f64=True)[1]  # noqa: E731
+    elif kind == "seam":
+        pairs = seam_pairs(tw, 5)
+        eps, norm = 1e-4, 1.0 / (pairs.shape[0] * 3)
+        g = gpu_seam(tex, pairs, eps, norm)[0]
+        f = lambda t: api.seam_gradient(t, pairs, eps, norm, f64=True)[1]  # noqa: E731
+    else:
+        g = gpu_tv(tex, valid, chart, 1e-4, 0.5)[..., :3].cpu().numpy()
+        f = lambda t: api.tv_gradient(t, valid=valid.astype(np.uint8), chart=chart, eps=1e-4, weight=0.5,  # noqa: E731
+                                      f64=True)[1]
+    rng = np.random.default_rng(7)
+    nz = np.argwhere(np.abs(g) > 0)
+    picks = nz[rng.choice(len(nz), size=60, replace=False)]
+    scale = np.abs(g).max()
+    worst = 0.0
+    for y, x, c in picks:
+        tp, tm = tex.copy(), tex.copy()
+        tp[y, x, c] = np.float32(tex[y, x, c] + 2e-6)
+        tm[y, x, c] = np.float32(tex[y, x, c] - 2e-6)
+        fd = (f(tp) - f(tm)) / (float(tp[y, x, c]) - float(tm[y, x, c]))
+        worst = max(worst, abs(fd - g[y, x, c]) / max(abs(fd), 1e-3 * scale))
+    print(f"\n{kind}: GPU gradient vs central differences, worst relative error {worst:.2e}")
+    # fp32 per-tap arithmetic (as the reference's) and atomic order, against exact derivatives
+    assert worst < 1e-3, worst
+
+
+def test_full_step_at_refine_atlas_size():
+    """Photometric (4 views of 2048x1536), TV and seam gradients of one step into one 4096x4096
+    gradient buffer, against the FP64 sum of the three."""
+    th = tw = 4096
+    rng = np.random.default_rng(21)
+    tex = rng.uniform(0.02, 0.98, size=(th, tw, 3)).astype(np.float32)
+    H, W = 1536, 2048
+    yy, xx = np.meshgrid(np.arange(H, dtype=np.float32), np.arange(W, dtype=np.float32), indexing="ij")
+    views = []
+    for k in range(4):
+        # a smooth warp of the pixel grid onto a region of the atlas (about 2.5 texels per pixel), an
+        # elliptical foreground mask and noisy targets
+        ox, oy = rng.uniform(0.05, 0.3, size=2)
+        a = 0.62 * (xx / W) + 0.04 * np.sin(yy / H * 6.0 + k)
+        b = 0.62 * (yy / H) + 0.04 * np.cos(xx / W * 5.0 - k)
+        uv = np.stack([ox + a, oy + b], -1).astype(np.float32).reshape(-1, 2)
+        ell = ((xx - W / 2) / (0.45 * W)) ** 2 + ((yy - H / 2) / (0.42 * H)) ** 2 < 1.0
+        mask = (ell & (rng.uniform(size=(H, W)) > 0.02)).astype(np.float32).reshape(-1)
+        tgt = rng.uniform(size=(H * W, 3)).astype(np.float32)
+        views.append((uv, tgt, mask))
+    valid = rng.uniform(size=(th, tw)) < 0.97
+    chart = ((np.arange(tw)[None, :] // 1365) + 3 * (np.arange(th)[:, None] // 2048)).astype(np.int32)
+    pairs = seam_pairs(tw, 9)
+    vw = sum(float(v[2].sum()) for v in views)
+    norm = np.float32(1.0 / (vw * 3.0))
+    eps, tv_w, tv_eps, seam_eps = 1e-3, 1e-4, 1e-4, 1e-4
+    seam_norm = 1.0 / (pairs.shape[0] * 3)
+    grad, loss = gpu_photometric(tex, views, eps, float(norm))
+    gpu_tv(tex, valid, chart, tv_eps, tv_w, grad=grad)
+    seam_loss = torch.zeros(1, dtype=torch.float32, device=DEV)
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    t_tex, t_pairs = _t(tex), _t(pairs.reshape(-1, 4))
+    _native.call("pdr_refine_seam", _ptr(t_tex), tw, th, _ptr(t_pairs), pairs.shape[0], C.c_float(seam_eps),
+                 C.c_float(seam_norm), _ptr(grad), _ptr(seam_loss), 0, _stream())
+    torch.cuda.synchronize()
+    g = grad[..., :3].cpu().numpy()
+    # oracle: fp32 in reference order into one buffer, FP64 and FP64 |terms| sums
+    o32 = np.zeros_like(tex)
+    o64 = np.zeros(tex.shape, np.float64)
+    oab = np.zeros(tex.shape, np.float64)
+    l64 = 0.0
+    for uv, tgt, mask in views:
+        api.photometric_gradient(tex, uv, tgt, mask, eps, float(norm), grad=o32)
+        l64 += api.photometric_gradient(tex, uv, tgt, mask, eps, float(norm), grad=o64, f64=True)[1]
+        api.photometric_gradient(tex, uv, tgt, mask, eps, float(norm), grad=oab, f64=True, abs_terms=True)
+    kw = dict(valid=valid.astype(np.uint8), chart=chart, eps=tv_eps, weight=tv_w)
+    api.tv_gradient(tex, grad=o32, **kw)
+    api.tv_gradient(tex, grad=o64, f64=True, **kw)
+    api.tv_gradient(tex, grad=oab, f64=True, abs_terms=True, **kw)
+    api.seam_gradient(tex, pairs, seam_eps, seam_norm, grad=o32)
+    s64 = api.seam_gradient(tex, pairs, seam_eps, seam_norm, grad=o64, f64=True)[1]
+    api.seam_gradient(tex, pairs, seam_eps, seam_norm, grad=oab, f64=True, abs_terms=True)
+    rel, rel_abs = grad_check(g, o32, o64, oab, name="full step")
+    assert abs(float(loss[0]) - l64) <= 1e-5 * l64 and abs(float(seam_loss[0]) - s64) <= 1e-5 * s64
+    touched = int((np.abs(o64) > 0).any(-1).sum())
+    print(f"\nfull step 4096^2: {touched} texels with a gradient, worst {rel:.2e} / {rel_abs:.2e}; "
+          f"loss {float(loss[0]):.7g} vs f64 {l64:.7g}")
+
+
+def test_refine_drift_over_200_steps():
+    from photara_drender_gb300.baking import TextureBaker
+
+    rng = np.random.default_rng(3)
+    pos3, _, uv, idx, chart, remap = S.displaced_sphere(20_000, seed=3, atlas_size=256)
+    mats, _ = S.orbit_cameras(4)
+    truth = rng.uniform(size=(256, 256, 3)).astype(np.float32)
+    images, masks = [], []
+    for k in range(4):
+        r, _ = api.rasterize_forward(api.transform_positions(pos3, mats[k]), idx, (120, 160), output_derivatives=False)
+        img = api.texture_forward(truth, api.interpolate_forward(uv, idx, r), r)
+        images.append(img + rng.normal(scale=0.01, size=img.shape).astype(np.float32))
+        masks.append((rng.uniform(size=(120, 160)) > 0.1).astype(np.float32))
+    pairs = S.seam_uv_pairs(uv, idx, remap, chart, samples_per_edge=2)
+    init = np.full((256, 256, 3), 0.5, np.float32)
+    kw = dict(steps=200, batch_size=2, learning_rate=1e-2, minimum_learning_rate=2.5e-4, seam_polish_steps=30)
+    color, loss, seam, _, _ = TextureBaker(0).refine_texture(init, pos3, uv, idx, images, mats, visibility_masks=masks,
+                                                             seam_uv_pairs=pairs, **kw)
+    o_color, o_loss, o_seam = api.refine(init, pos3, uv, idx, images, mats, visibility_masks=masks,
+                                         seam_uv_pairs=pairs, **kw)
+    r_color, r_loss, r_seam = api.refine(init, pos3, uv, idx, images, mats, visibility_masks=masks,
+                                         seam_uv_pairs=pairs, reverse_order=True, **kw)
+    d_gpu, d_rev = np.abs(color - o_color), np.abs(r_color - o_color)
+    l_gpu = np.abs(loss - o_loss) / np.abs(o_loss)
+    l_rev = np.abs(r_loss - o_loss) / np.abs(o_loss)
+    s_gpu = np.abs(seam - o_seam) / np.abs(o_seam)
+    s_rev = np.abs(r_seam - o_seam) / np.abs(o_seam)
+    q = lambda a: (float(a.max()), float(np.quantile(a, 0.999)), float(np.mean(a)))  # noqa: E731
+    print(f"\n200-step refine, atlas values: GPU vs oracle max/p99.9/mean {q(d_gpu)}; reversed-order oracle vs "
+          f"oracle {q(d_rev)}")
+    print(f"loss history relative: GPU {l_gpu.max():.2e}, reversed {l_rev.max():.2e}; seam history: GPU "
+          f"{s_gpu.max():.2e}, reversed {s_rev.max():.2e}")
+    assert d_rev.max() > 0
+    assert d_gpu.max() <= 8.0 * d_rev.max() + 1e-6
+    assert np.quantile(d_gpu, 0.999) <= 8.0 * np.quantile(d_rev, 0.999) + 1e-6
+    assert l_gpu.max() <= 8.0 * l_rev.max() + 1e-6 and s_gpu.max() <= 8.0 * s_rev.max() + 1e-6
+    assert loss[-1] < 0.5 * loss[0]
