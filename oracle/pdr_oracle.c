@@ -18,6 +18,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <omp.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -340,6 +341,7 @@ int ora_rasterize_forward_f64(const float* pos, uint32_t V, const uint32_t* idx,
 /* ACC(x) is the identity, or |x| in the FP64 twins' abs_terms mode (sum of absolute terms,
  * the scale against which summation-order error is stated). */
 #define RB_BODY(REAL, CROSS, EPS_AREA, SAMPLE)                                                       \
+    _Pragma("omp parallel for schedule(dynamic, 256)")                                               \
     for (uint32_t t = 0; t < T; ++t) {                                                               \
         REAL g[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};                                  \
         const uint32_t vi[3] = {idx[t * 3 + 0], idx[t * 3 + 1], idx[t * 3 + 2]};                     \
@@ -419,6 +421,7 @@ int ora_rasterize_backward(const float* pos, uint32_t V, const uint32_t* idx, ui
 #undef ACC
     uint32_t *off, *corners;
     vertex_csr(idx, T, V, &off, &corners);
+#pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; ++v) {
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         for (uint32_t a = off[v]; a < off[v + 1]; ++a)
@@ -443,6 +446,7 @@ int ora_rasterize_backward_f64(const float* pos, uint32_t V, const uint32_t* idx
 #undef ACC
     uint32_t *off, *corners;
     vertex_csr(idx, T, V, &off, &corners);
+#pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; ++v) {
         double acc[4] = {0, 0, 0, 0};
         for (uint32_t a = off[v]; a < off[v + 1]; ++a)
@@ -485,27 +489,17 @@ int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uin
  * pixels in ascending order; adding zero-weight terms leaves a finite sum unchanged, so the
  * per-pixel scatter below accumulates every vertex in the same order. interpolate_grad_raster.hlsl
  * gives the raster gradient. */
+/* Threaded without changing any sum: the raster gradient is per pixel; for the attribute gradient
+ * each thread owns a range of vertices and scans all pixels in order, so every vertex's sum keeps the
+ * sequential (pixel) order and the result is bit-identical for any thread count. */
 #define IB_BODY(REAL)                                                                                \
-    memset(grad_attr, 0, (size_t)V * A * sizeof(REAL));                                              \
+    _Pragma("omp parallel for schedule(static)")                                                     \
     for (uint64_t p = 0; p < P; ++p) {                                                               \
         const uint32_t id = rid(raster[p * 4 + 3]);                                                  \
         REAL* gr = grad_raster + p * 4;                                                              \
         gr[0] = gr[1] = gr[2] = gr[3] = 0;                                                           \
         if (id == 0 || id > T) continue;                                                             \
         const uint32_t i0 = idx[(id - 1) * 3 + 0], i1 = idx[(id - 1) * 3 + 1], i2 = idx[(id - 1) * 3 + 2]; \
-        const float u = raster[p * 4 + 0], v = raster[p * 4 + 1];                                    \
-        const uint32_t vs[3] = {i0, i1, i2};                                                         \
-        for (int k = 0; k < 3; ++k) {                                                                \
-            const uint32_t vx = vs[k];                                                               \
-            int first = 1;                                                                           \
-            for (int j = 0; j < k; ++j) if (vs[j] == vx) first = 0;                                  \
-            if (!first) continue;                                                                    \
-            REAL wgt = 0;                                                                            \
-            if (i0 == vx) wgt += (REAL)u;                                                            \
-            if (i1 == vx) wgt += (REAL)v;                                                            \
-            if (i2 == vx) wgt += (REAL)1 - (REAL)u - (REAL)v;                                        \
-            for (uint32_t a = 0; a < A; ++a) grad_attr[(uint64_t)vx * A + a] += ACC(wgt * (REAL)grad_out[p * A + a]); \
-        }                                                                                            \
         if (i0 < V && i1 < V && i2 < V) {                                                            \
             REAL gx = 0, gy = 0;                                                                     \
             for (uint32_t a = 0; a < A; ++a) {                                                       \
@@ -517,6 +511,31 @@ int ora_interpolate_forward(const float* attr, uint32_t V, uint32_t A, const uin
             }                                                                                        \
             gr[0] = gx;                                                                              \
             gr[1] = gy;                                                                              \
+        }                                                                                            \
+    }                                                                                                \
+    _Pragma("omp parallel")                                                                          \
+    {                                                                                                \
+        const uint32_t nt = (uint32_t)omp_get_num_threads(), tid = (uint32_t)omp_get_thread_num();   \
+        const uint32_t v_lo = (uint32_t)((uint64_t)V * tid / nt), v_hi = (uint32_t)((uint64_t)V * (tid + 1) / nt); \
+        memset(grad_attr + (uint64_t)v_lo * A, 0, (size_t)(v_hi - v_lo) * A * sizeof(REAL));        \
+        for (uint64_t p = 0; p < P && v_lo < v_hi; ++p) {                                            \
+            const uint32_t id = rid(raster[p * 4 + 3]);                                              \
+            if (id == 0 || id > T) continue;                                                         \
+            const uint32_t i0 = idx[(id - 1) * 3 + 0], i1 = idx[(id - 1) * 3 + 1], i2 = idx[(id - 1) * 3 + 2]; \
+            const uint32_t vs[3] = {i0, i1, i2};                                                     \
+            const float u = raster[p * 4 + 0], v = raster[p * 4 + 1];                                \
+            for (int k = 0; k < 3; ++k) {                                                            \
+                const uint32_t vx = vs[k];                                                           \
+                if (vx < v_lo || vx >= v_hi) continue;                                               \
+                int first = 1;                                                                       \
+                for (int j = 0; j < k; ++j) if (vs[j] == vx) first = 0;                              \
+                if (!first) continue;                                                                \
+                REAL wgt = 0;                                                                        \
+                if (i0 == vx) wgt += (REAL)u;                                                        \
+                if (i1 == vx) wgt += (REAL)v;                                                        \
+                if (i2 == vx) wgt += (REAL)1 - (REAL)u - (REAL)v;                                    \
+                for (uint32_t a = 0; a < A; ++a) grad_attr[(uint64_t)vx * A + a] += ACC(wgt * (REAL)grad_out[p * A + a]); \
+            }                                                                                        \
         }                                                                                            \
     }
 
@@ -572,24 +591,43 @@ int ora_texture_forward(const float* tex, uint32_t tw, uint32_t th, uint32_t C, 
  * which the ascending-entry scatter below reproduces. texture_grad_uv.hlsl:38-80 for uv. */
 #define TB_BODY(REAL)                                                                                \
     const uint64_t texels = (uint64_t)tw * th;                                                       \
-    memset(grad_tex, 0, texels * C * sizeof(REAL));                                                  \
-    for (uint64_t p = 0; p < P; ++p) {                                                               \
+    for (uint64_t p = 0; p < P; ++p) { /* the reference throws at the first bad pixel, in order */ \
         if (raster[p * 4 + 3] == 0.0f) continue;                                                     \
         const float u = uv[p * 2 + 0], v = uv[p * 2 + 1];                                            \
         if (!isfinite(u) || !isfinite(v)) return ORA_INVALID;                                        \
-        const double tx = (double)u * tw - 0.5, ty = (double)v * th - 0.5;                           \
-        if (fabs(tx) > 1.0e9 || fabs(ty) > 1.0e9) return ORA_RANGE;                                  \
-        const int32_t bx = d2i_sat(floor(tx)), by = d2i_sat(floor(ty));                              \
-        const REAL fx = (REAL)(tx - floor(tx)), fy = (REAL)(ty - floor(ty));                         \
-        const int32_t xs[2] = {address_coordinate(bx, tw, mode), address_coordinate(bx + 1, tw, mode)}; \
-        const int32_t ys[2] = {address_coordinate(by, th, mode), address_coordinate(by + 1, th, mode)}; \
-        const REAL w[4] = {((REAL)1 - fx) * ((REAL)1 - fy), fx * ((REAL)1 - fy), ((REAL)1 - fx) * fy, fx * fy}; \
-        const uint64_t tx4[4] = {(uint64_t)ys[0] * tw + xs[0], (uint64_t)ys[0] * tw + xs[1],        \
-                                 (uint64_t)ys[1] * tw + xs[0], (uint64_t)ys[1] * tw + xs[1]};        \
-        for (int k = 0; k < 4; ++k)                                                                  \
-            for (uint32_t c = 0; c < C; ++c) grad_tex[tx4[k] * C + c] += ACC(w[k] * (REAL)grad[p * C + c]); \
+        if (fabs((double)u * tw - 0.5) > 1.0e9 || fabs((double)v * th - 0.5) > 1.0e9) return ORA_RANGE; \
     }                                                                                                \
+    /* each thread owns a band of texel rows and scans all pixels in order: every texel's sum keeps \
+     * the sequential order, bit-identical for any thread count */                                 \
+    _Pragma("omp parallel")                                                                          \
+    {                                                                                                \
+        const uint32_t nt = (uint32_t)omp_get_num_threads(), tid = (uint32_t)omp_get_thread_num();   \
+        const uint32_t y_lo = (uint32_t)((uint64_t)th * tid / nt), y_hi = (uint32_t)((uint64_t)th * (tid + 1) / nt); \
+        memset(grad_tex + (uint64_t)y_lo * tw * C, 0, (size_t)(y_hi - y_lo) * tw * C * sizeof(REAL)); \
+        for (uint64_t p = 0; p < P && y_lo < y_hi; ++p) {                                            \
+            if (raster[p * 4 + 3] == 0.0f) continue;                                                 \
+            const float u = uv[p * 2 + 0], v = uv[p * 2 + 1];                                        \
+            const double tx = (double)u * tw - 0.5, ty = (double)v * th - 0.5;                       \
+            const int32_t by = d2i_sat(floor(ty));                                                   \
+            const int32_t ys[2] = {address_coordinate(by, th, mode), address_coordinate(by + 1, th, mode)}; \
+            const int in0 = (uint32_t)ys[0] >= y_lo && (uint32_t)ys[0] < y_hi;                       \
+            const int in1 = (uint32_t)ys[1] >= y_lo && (uint32_t)ys[1] < y_hi;                       \
+            if (!in0 && !in1) continue;                                                              \
+            const int32_t bx = d2i_sat(floor(tx));                                                   \
+            const REAL fx = (REAL)(tx - floor(tx)), fy = (REAL)(ty - floor(ty));                     \
+            const int32_t xs[2] = {address_coordinate(bx, tw, mode), address_coordinate(bx + 1, tw, mode)}; \
+            const REAL w[4] = {((REAL)1 - fx) * ((REAL)1 - fy), fx * ((REAL)1 - fy), ((REAL)1 - fx) * fy, fx * fy}; \
+            const uint64_t tx4[4] = {(uint64_t)ys[0] * tw + xs[0], (uint64_t)ys[0] * tw + xs[1],    \
+                                     (uint64_t)ys[1] * tw + xs[0], (uint64_t)ys[1] * tw + xs[1]};    \
+            for (int k = 0; k < 4; ++k) {                                                            \
+                if (!(k < 2 ? in0 : in1)) continue;                                                  \
+                for (uint32_t c = 0; c < C; ++c) grad_tex[tx4[k] * C + c] += ACC(w[k] * (REAL)grad[p * C + c]); \
+            }                                                                                        \
+        }                                                                                            \
+    }                                                                                                \
+    (void)texels;                                                                                    \
     if (grad_uv) {                                                                                   \
+        _Pragma("omp parallel for schedule(static)")                                                 \
         for (uint64_t p = 0; p < P; ++p) {                                                           \
             if (rid(raster[p * 4 + 3]) == 0) { grad_uv[p * 2] = grad_uv[p * 2 + 1] = 0; continue; } \
             REAL tx, ty, fx, fy; int32_t bx, by;                                                     \
@@ -646,6 +684,13 @@ int ora_texture_backward_f64(const float* tex, uint32_t tw, uint32_t th, uint32_
 #undef UVPOS
     return ORA_OK;
 }
+
+/* Host threads the oracle's parallel loops use (0: all); results do not depend on it. */
+void ora_set_threads(int threads) {
+    omp_set_num_threads(threads > 0 ? threads : omp_get_num_procs());
+}
+
+int ora_get_threads(void) { return omp_get_max_threads(); }
 
 /* ---- transforms and softmax scale ---------------------------------------------------- */
 

@@ -22,6 +22,11 @@
 extern "C" {
 #endif
 
+/* Host threads of the parallel loops (0: all processors). Every result is independent of the
+ * thread count: sums are partitioned by owner, never split. */
+void ora_set_threads(int threads);
+int ora_get_threads(void);
+
 #define ORA_OK 0
 #define ORA_INVALID (-1)
 #define ORA_RANGE (-2)

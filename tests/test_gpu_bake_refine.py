@@ -123,10 +123,15 @@ def test_refine_matches_oracle(baker):
                                                    seam_uv_pairs=pairs, **kw)
     o_color, o_loss, o_seam = api.refine(init, pos3, uv, idx, images, mats, visibility_masks=masks,
                                          seam_uv_pairs=pairs, **kw)
+    # the reference adds gradients with atomics: the oracle in reversed order is another result it may
+    # give, and the GPU must stay within a small multiple of that order noise
+    r_color, r_loss, r_seam = api.refine(init, pos3, uv, idx, images, mats, visibility_masks=masks,
+                                         seam_uv_pairs=pairs, reverse_order=True, **kw)
     assert loss.shape == (12,) and seam.shape == (5,)
     assert np.allclose(loss, o_loss, rtol=1e-5, atol=1e-7), (loss, o_loss)
-    assert np.allclose(seam, o_seam, rtol=1e-4, atol=1e-7), (seam, o_seam)
-    assert np.abs(color - o_color).max() < 1e-4
+    seam_noise = np.abs(r_seam - o_seam).max()
+    assert np.abs(seam - o_seam).max() <= 4.0 * seam_noise + 1e-5 * np.abs(o_seam).max(), (seam, o_seam, r_seam)
+    assert np.abs(color - o_color).max() <= 4.0 * np.abs(r_color - o_color).max() + 1e-6
     assert loss[-1] < loss[0]
 
 
