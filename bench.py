@@ -30,7 +30,7 @@ WORKLOAD = dict(name="c2_fwdbwd_200k_64x1024sq_atlas4096", triangles=200_000, vi
                 attributes=3, atlas=4096, channels=4, seed=0)
 METRIC = "fwd+bwd Mpix/s"
 CPU_SAMPLE_SECONDS = 10.0  # bounded CPU-baseline sample: whole views until this much oracle time
-SKIP_CPU_PAD = False  # set by --skip-cpu: no oracle padding beside the GPU padding
+SKIP_CPU = False  # set by --skip-cpu: no CPU-baseline legs beside the GPU legs
 
 
 def scene(w=WORKLOAD):
@@ -143,14 +143,15 @@ def max_over_ranks(x: float, world: int) -> float:
 
 # ---- CPU restatement (reference arm and cpu_baseline) -------------------------------------------------
 
-def cpu_fwdbwd_sample(pos3, uv, idx, mats, attrs, tex, view: int, rng):
-    """One view's forward + backward through the oracle, returns seconds."""
+def cpu_fwdbwd_sample(clip, uv, idx, attrs, tex, rng, res=None):
+    """One view's forward + backward through the oracle (clip positions [V, 4] of the view, resolution
+    `res`, default the workload's), returns seconds. Every stage runs on the oracle's host threads (forward
+    per pixel, adjoints by owner partitions that keep the reference's summation order)."""
+    w = WORKLOAD
     from oracle import api
 
-    w = WORKLOAD
-    clip = api.transform_positions(pos3, mats[view])
     t0 = time.perf_counter()
-    raster, deriv = api.rasterize_forward(clip, idx, (w["height"], w["width"]))
+    raster, deriv = api.rasterize_forward(clip, idx, res or (w["height"], w["width"]))
     a = api.interpolate_forward(attrs, idx, raster)
     u = api.interpolate_forward(uv, idx, raster)
     s = api.texture_forward(tex, u, raster)
@@ -166,24 +167,85 @@ def cpu_fwdbwd_sample(pos3, uv, idx, mats, attrs, tex, view: int, rng):
     return (t1 - t0) + (t3 - t2)
 
 
+def oracle_threads(n: int) -> None:
+    """Host threads of the oracle's parallel loops (0: all); its results do not depend on it."""
+    from oracle import api
+
+    api.lib().ora_set_threads(int(n))
+
+
+def cpu_sample_views(clips, uv, idx, attrs, tex, threads: int, budget_s: float, res=None):
+    """Whole views (clips: [views, V, 4]) through the oracle's forward + backward with `threads` host threads
+    until `budget_s` seconds of work (at least one view): (views done, seconds)."""
+    oracle_threads(threads)
+    rng = np.random.default_rng(1)
+    secs, done = 0.0, 0
+    try:
+        while done < len(clips) and (done == 0 or secs < budget_s):
+            secs += cpu_fwdbwd_sample(np.ascontiguousarray(clips[done]), uv, idx, attrs, tex, rng, res)
+            done += 1
+    finally:
+        oracle_threads(0)
+    return done, secs
+
+
+def cpu_refine_sample(st, tv_weight, nsteps, threads):
+    """Seconds per step of the refiner on the host: for each of the first `nsteps` steps, the oracle's
+    photometric gradient over the step's batch views (the refine state's own view caches), the chart-aware
+    TV gradient when tv_weight is set, and the dense Adam update, with `threads` host threads."""
+    from oracle import api
+
+    o = st.options
+    n, B = len(st.weights), int(o.batch_size)
+    need = sorted({(k * B + b) % n for k in range(nsteps) for b in range(B)})
+    caches = {k: tuple(st.keep[3 * k + j].cpu().numpy() for j in range(3)) for k in need}
+    th, tw = int(o.height), int(o.width)
+    tex = np.full((th, tw, 3), 0.5, np.float32)
+    g, m, v = np.zeros_like(tex), np.zeros_like(tex), np.zeros_like(tex)
+    valid = st.tv_valid.cpu().numpy() if st.tv_valid is not None else None
+    chart = st.tv_chart.cpu().numpy() if st.tv_chart is not None else None
+    oracle_threads(threads)
+    secs = 0.0
+    try:
+        for k in range(nsteps):
+            t0 = time.perf_counter()
+            bvw = sum(st.weights[(k * B + b) % n] for b in range(B))
+            norm = float(np.float32(1.0 / (bvw * 3.0))) if bvw > 0 else 0.0
+            for b in range(B):
+                uv, tgt, msk = caches[(k * B + b) % n]
+                api.photometric_gradient(tex, uv, tgt, msk, float(o.photometric_epsilon), norm, grad=g)
+            if tv_weight and valid is not None:
+                api.tv_gradient(tex, valid=valid, chart=chart, eps=float(o.tv_epsilon), weight=tv_weight, grad=g)
+            lr = float(o.minimum_learning_rate) + 0.5 * (float(o.learning_rate) - float(o.minimum_learning_rate)) * (
+                1.0 + np.cos(np.pi * k / max(int(o.steps), 1)))
+            b1, b2 = float(o.adam_beta1), float(o.adam_beta2)
+            api.adam_update(tex, g, m, v, lr, b1, b2, float(o.adam_epsilon), 1.0 - b1 ** (k + 1), 1.0 - b2 ** (k + 1),
+                            float(o.clamp_min), float(o.clamp_max))
+            secs += time.perf_counter() - t0
+    finally:
+        oracle_threads(0)
+    return secs / nsteps
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from oracle import api  # noqa: F401  (builds the oracle when needed)
+    from oracle import api  # builds the oracle when needed
 
     w = WORKLOAD
     pos3, uv, idx, mats, attrs = scene()
     rng = np.random.default_rng(1)
     tex = rng.uniform(size=(w["atlas"], w["atlas"], w["channels"])).astype(np.float32)
     cores = os.cpu_count() or 1
+    clips = [api.transform_positions(pos3, mats[k]) for k in range(w["views"])]
     for k in range(args.warmup):
-        cpu_fwdbwd_sample(pos3, uv, idx, mats, attrs, tex, k % w["views"], rng)
-    times = [cpu_fwdbwd_sample(pos3, uv, idx, mats, attrs, tex, k % w["views"], rng) for k in range(args.steps)]
+        cpu_fwdbwd_sample(clips[k % w["views"]], uv, idx, attrs, tex, rng)
+    times = [cpu_fwdbwd_sample(clips[k % w["views"]], uv, idx, attrs, tex, rng) for k in range(args.steps)]
     per_view = float(np.mean(times))
     mpix = w["height"] * w["width"] / 1e6 / per_view
     sample = (f"one of the {w['views']} views per step (view k mod {w['views']}), full forward+backward at "
-              f"{w['height']}x{w['width']}; rasterize/interpolate/texture forward multi-threaded (OpenMP), adjoints "
-              f"single-threaded as the reference's loops")
+              f"{w['height']}x{w['width']}; every stage on all {cores} host threads (OpenMP: forward per pixel, "
+              f"adjoints partitioned by texel rows / vertices / triangles so sums keep the reference's order)")
     line = {
         "metric": METRIC, "value": mpix, "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_view * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -247,7 +309,7 @@ def render_views(r, t_pos, t_uv, t_idx, mats, H, W, atlas_rgb, dev):
 
 
 C1 = dict(name="c1_fwdbwd_ico4_8x512sq_tex1024", subdivisions=4, views=8, height=512, width=512, attributes=3,
-          texture=1024, channels=4, seed=0, steps=200)
+          texture=1024, channels=4, seed=0, steps=200, e2e_steps=50)
 
 
 def c1_leg(dev, hbm):
@@ -298,10 +360,30 @@ def c1_leg(dev, hbm):
     P = views * H * W
     alg = P * 96 + 2 * c["texture"] ** 2 * c["channels"] * 4 + views * V * 16 * 2 + T * 12 + V * (c["attributes"] + 2) * 8
     best = min(ms_launch, ms_graph)
-    return {"workload": c["name"], "mpix_per_s": P / 1e6 / (best / 1e3), "ms_per_step_graph": ms_graph,
-            "ms_per_step_launches": ms_launch, "tile_entries": entries, "algorithmic_bytes": alg,
-            "achieved_gbs": alg / (best / 1e3) / 1e9, "frac": alg / (best / 1e3) / 1e9 / hbm,
-            "timing": f"CUDA events over {c['steps']} fused fwd+bwd steps, device-resident inputs (which fit in L2)"}
+    res = {"workload": c["name"], "mpix_per_s": P / 1e6 / (best / 1e3), "ms_per_step_graph": ms_graph,
+           "ms_per_step_launches": ms_launch, "tile_entries": entries, "algorithmic_bytes": alg,
+           "achieved_gbs": alg / (best / 1e3) / 1e9, "frac": alg / (best / 1e3) / 1e9 / hbm,
+           "timing": f"CUDA events over {c['steps']} fused fwd+bwd steps, device-resident inputs (which fit in L2)"}
+    host = {k: v.cpu().pin_memory() for k, v in dict(clip=clip, attrs=attrs, uv=uv, tex=tex, g_attr=g_attr,
+                                                     g_samp=g_samp).items()}
+    host["idx"] = torch.tensor(idx.astype(np.int64)).pin_memory()
+    e2e_ms, h2d, d2h = e2e_render(dev, r, host, H, W, c["e2e_steps"])
+    res["e2e"] = {"value": P / 1e6 / (e2e_ms / 1e3), "unit": "Mpix/s", "ms_per_step": e2e_ms,
+                  "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                  "api": f"photara_drender_gb300.torch.render + backward with host buffers, {c['e2e_steps']} steps"}
+    if not SKIP_CPU:
+        args_h = (clip.cpu().numpy(), S.spherical_uv(pos3).astype(np.float32), idx, attrs.cpu().numpy(),
+                  tex.cpu().numpy())
+        done, secs = cpu_sample_views(*args_h, 0, 5.0, res=(H, W))
+        done1, secs1 = cpu_sample_views(*args_h, 1, 5.0, res=(H, W))
+        cores = os.cpu_count() or 1
+        res["cpu_baseline"] = {
+            "value": done * H * W / 1e6 / secs, "unit": "Mpix/s", "cores": cores, "kind": "port",
+            "sample": f"{done} of the {views} views (until 5 s of work), full forward+backward through the oracle "
+                      f"on all {cores} host threads, {secs:.2f} s",
+            "one_core": {"value": done1 * H * W / 1e6 / secs1, "unit": "Mpix/s", "cores": 1,
+                         "sample": f"{done1} views on one thread, {secs1:.2f} s"}}
+    return res
 
 
 def bake_leg(dev, hbm):
@@ -383,8 +465,37 @@ def bake_leg(dev, hbm):
     res["surface_fill"] = {"seconds": s_fill, "stats": list(sf[2]),
                            "note": "fill_texture_on_surface on the ray-query atlas with the welded mesh topology "
                                    "(copies of colour and filled_mask included)"}
-    if not SKIP_CPU_PAD:
+    if not SKIP_CPU:
         from oracle import api as oracle_api
+
+        try:
+            cores = os.cpu_count() or 1
+            imgs_h = [images[k].cpu().numpy() for k in range(4)]
+            bake_args = (pos3, nrm, uv, idx)
+
+            def cpu_bake(nv, threads):
+                oracle_threads(threads)
+                try:
+                    t0 = time.perf_counter()
+                    oracle_api.bake(*bake_args, imgs_h[:nv], mats[:nv], eyes[:nv], resolution=(b["atlas"], b["atlas"]),
+                                    blend_mode="weighted_average", pcf_radius=1)
+                    return time.perf_counter() - t0
+                finally:
+                    oracle_threads(0)
+
+            s1, s4 = cpu_bake(1, 0), cpu_bake(4, 0)
+            per_view = max((s4 - s1) / 3.0, 1e-9)
+            one = cpu_bake(1, 1)
+            res["cpu_baseline"] = {
+                "value": N / 1e9 / per_view, "unit": "Gtexel-views/s", "cores": cores, "kind": "port",
+                "sample": f"the oracle's shadow-map bake (weighted average, PCF 1) of views 0-3 into the "
+                          f"{b['atlas']}^2 atlas on all {cores} host threads: 1 view {s1:.2f} s, 4 views {s4:.2f} s "
+                          f"(per view {per_view:.2f} s after the atlas G-buffer); all {b['views']} views would take "
+                          f"{s1 + per_view * (b['views'] - 1):.1f} s",
+                "one_core": {"value": None, "unit": "Gtexel-views/s", "cores": 1,
+                             "sample": f"1 view on one thread (G-buffer included): {one:.2f} s"}}
+        except Exception as e:
+            res["cpu_baseline"] = {"value": None, "kind": "port", "sample": f"failed: {e}"}
 
         host = (out.color.cpu().numpy(), valid.cpu().numpy(), cov.cpu().numpy())
         t0 = time.perf_counter()
@@ -452,7 +563,8 @@ def refine_leg(dev, hbm):
     baker = TextureBaker(dev.index or 0)
     sc = refine_scene(c, dev, baker)
     with baker.context.lock:
-        tex, hist, seam, pre_s, opt_s = baker._refine(*refine_args(c, sc, c["steps"]), use_graph=True)
+        st = baker._refine_prepare(*refine_args(c, sc, c["steps"]))
+        tex, hist, seam, pre_s, opt_s = baker._refine_finish(st, True)
     torch.cuda.synchronize(dev)
     pairs = sc["pairs"]
     steps = c["steps"] + (c["seam_steps"] if pairs.shape[0] else 0)
@@ -469,7 +581,27 @@ def refine_leg(dev, hbm):
             "algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_bytes * c["steps"] / opt_s / 1e9,
             "frac": step_bytes * c["steps"] / opt_s / 1e9 / hbm, "mean_abs_error_vs_ground_truth": err,
             "timing": "TextureBaker refinement optimisation wall time (graph record + instantiate + launch + "
-                      "sync), texture starting at 0.5"}
+                      "sync), texture starting at 0.5",
+            "cpu_baseline": refine_cpu_baseline(st, c)}
+
+
+def refine_cpu_baseline(st, c):
+    """The refiner's photometric + TV + Adam steps on the host (the oracle's restatement of the shaders), a
+    reduced number of steps timed and stated, with all host threads and with one."""
+    if SKIP_CPU:
+        return None
+    try:
+        cores = os.cpu_count() or 1
+        all_s = cpu_refine_sample(st, c["tv_weight"], 2, 0)
+        one_s = cpu_refine_sample(st, c["tv_weight"], 1, 1)
+        return {"value": all_s, "unit": "s/step", "cores": cores, "kind": "port",
+                "sample": f"steps 0-1 of {c['steps']} (batch {c['batch']} views of {c['height']}x{c['width']}, "
+                          f"{c['atlas']}^2 atlas): photometric gradient, chart-aware TV and dense Adam through the "
+                          f"oracle on all {cores} host threads; {c['steps']} steps would take "
+                          f"{all_s * c['steps']:.0f} s",
+                "one_core": {"value": one_s, "unit": "s/step", "cores": 1, "sample": "step 0 on one thread"}}
+    except Exception as e:  # the CPU leg never hides a GPU result
+        return {"value": None, "unit": "s/step", "kind": "port", "sample": f"failed: {e}"}
 
 
 C4 = dict(name="c4_uneven_batch_16_meshes", meshes=16, tri_min=10_000, tri_max=1_000_000, views=(4, 48),
@@ -507,6 +639,8 @@ def c4_leg(dev, hbm):
                       texture=torch.rand((ts, ts, 4), device=dev, generator=g))
         m.grads["interp"] = torch.randn((views, h, w, c["attributes"]), device=dev, generator=g)
         m.grads["sampled"] = torch.randn((views, h, w, 4), device=dev, generator=g)
+        if k == 0:
+            first = (m.clip.cpu().numpy(), uv, idx, m.attributes.cpu().numpy(), m.texture.cpu().numpy(), (h, w))
         meshes.append(m)
         desc.append({"triangles": int(idx.shape[0]), "views": views, "resolution": [h, w], "texture": ts})
     batch = MeshBatch(r, meshes)
@@ -539,7 +673,21 @@ def c4_leg(dev, hbm):
     # forward outputs 16 + 16 + 4A + 8 + 16, backward inputs 4A + 16 per pixel; textures read and
     # their gradients written once
     alg = P * (16 + 16 + 4 * A + 8 + 16 + 4 * A + 16) + sum(2 * d["texture"] ** 2 * 16 for d in desc)
-    return {"workload": c["name"], "batch_ms": batch_ms, "mpix_per_s": P / 1e6 / (batch_ms / 1e3),
+    cpu = None
+    if not SKIP_CPU:
+        clips, uv0, idx0, attrs0, tex0, res0 = first
+        cores = os.cpu_count() or 1
+        done, secs = cpu_sample_views(clips, uv0, idx0, attrs0, tex0, 0, 5.0, res=res0)
+        done1, secs1 = cpu_sample_views(clips, uv0, idx0, attrs0, tex0, 1, 5.0, res=res0)
+        px = res0[0] * res0[1]
+        cpu = {"value": done * px / 1e6 / secs, "unit": "Mpix/s", "cores": cores, "kind": "port",
+               "sample": f"mesh 0 of the batch ({desc[0]['triangles']} triangles, {desc[0]['texture']}^2 texture, "
+                         f"8 attributes): {done} of its {desc[0]['views']} views at {res0[0]}x{res0[1]} (until 5 s "
+                         f"of work), forward+backward through the oracle on all {cores} host threads, {secs:.2f} s; "
+                         f"the whole batch at this rate: {P / (done * px / secs):.0f} s",
+               "one_core": {"value": done1 * px / 1e6 / secs1, "unit": "Mpix/s", "cores": 1,
+                            "sample": f"{done1} views on one thread, {secs1:.2f} s"}}
+    return {"workload": c["name"], "batch_ms": batch_ms, "mpix_per_s": P / 1e6 / (batch_ms / 1e3), "cpu_baseline": cpu,
             "pixels": P, "meshes": desc, "autotune_ms": {f"{a}x{b}/{k}": t for (a, b, k), t in tune.items()},
             "config": {"tile": [best[0], best[1]], "stage_triangles": best[2]},
             "per_mesh_ms_p50": float(np.percentile(per_mesh, 50)), "per_mesh_ms_p99": float(np.percentile(per_mesh, 99)),
@@ -612,11 +760,27 @@ def c5_leg(dev, hbm):
         for b in ev["budgets"]:
             runs[f"learned_{b}"] = learned(b)
             runs[f"plain_{b}"] = plain(b)
+    cpu = None
+    if not SKIP_CPU:
+        with baker.context.lock:
+            st = baker._refine_prepare(*refine_args(ev, sc, ev["steps"]))
+            try:
+                cores = os.cpu_count() or 1
+                per = cpu_refine_sample(st, ev["tv_weight"], 1, 0)
+                cpu = {"value": per, "unit": "s/step", "cores": cores, "kind": "port",
+                       "sample": f"one plain refine step at this size (batch {ev['batch']} views of "
+                                 f"{ev['height']}x{ev['width']}, {ev['atlas']}^2 atlas, photometric + TV + Adam) "
+                                 f"through the oracle on all {cores} host threads; the plain {ev['steps']}-step "
+                                 f"schedule would take {per * ev['steps']:.0f} s"}
+            except Exception as e:
+                cpu = {"value": None, "kind": "port", "sample": f"failed: {e}"}
+            del st
     target = runs["plain"]["loss"] * 1.01
     hit = [runs[f"learned_{b}"] for b in ev["budgets"] if runs[f"learned_{b}"]["loss"] <= target]
     best = min(hit, key=lambda r: r["seconds"]) if hit else None
     plain_hit = [runs[f"plain_{b}"] for b in ev["budgets"] if runs[f"plain_{b}"]["loss"] <= target]
-    return {"workload": ev["name"], "plain_loss": runs["plain"]["loss"], "plain_seconds": runs["plain"]["seconds"],
+    return {"workload": ev["name"], "cpu_baseline": cpu, "plain_loss": runs["plain"]["loss"],
+            "plain_seconds": runs["plain"]["seconds"],
             "target_loss": target,
             "learned_seconds_to_target": best["seconds"] if best else None,
             "learned_steps_to_target": best["steps"] if best else None,
@@ -657,11 +821,84 @@ def stage_bytes(w, T, V, entries):
     }
 
 
+def e2e_render(dev, r, host, H, W, steps, world=1):
+    """The fused pass through the public autograd API (photara_drender_gb300.torch.render + backward) with
+    host buffers: every step copies its inputs (`host`: pinned clip, attrs, uv, tex, g_attr, g_samp, idx)
+    to the device and reads the clip, attribute, uv and texture gradients back, all inside the timed
+    region. The copies of step k+1 run on a copy stream while step k computes (two device buffer sets),
+    so the step costs the larger of the two instead of their sum. Returns (ms per step or None, host to
+    device bytes per step, device to host bytes per step)."""
+    import torch
+
+    from photara_drender_gb300 import torch as pdr_torch
+
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    grads_host = {k: torch.empty(host[k].shape, dtype=torch.float32).pin_memory() for k in ("clip", "attrs", "uv", "tex")}
+    d2h = sum(t.numel() * t.element_size() for t in grads_host.values())
+    if not steps:
+        return None, h2d, d2h
+    bufs = [{k: torch.empty_like(v, device=dev) for k, v in host.items()} for _ in range(2)]
+    copy_stream = torch.cuda.Stream(dev)
+    compute = torch.cuda.current_stream(dev)
+    copied = [torch.cuda.Event() for _ in range(2)]
+    released = [torch.cuda.Event() for _ in range(2)]
+    computed = [torch.cuda.Event() for _ in range(2)]
+    in_flight = [None, None]  # the gradients a slot's readback still reads
+
+    def upload(slot):
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(released[slot])
+            for k, v in host.items():
+                bufs[slot][k].copy_(v, non_blocking=True)
+            copied[slot].record(copy_stream)
+
+    def step(i, total):
+        slot = i % 2
+        compute.wait_event(copied[slot])
+        if i + 1 < total:
+            upload((i + 1) % 2)
+        d = bufs[slot]
+        leaves = {k: d[k].detach().requires_grad_(True) for k in ("clip", "attrs", "uv", "tex")}
+        out = pdr_torch.render(leaves["clip"], d["idx"], (H, W), rasterizer=r, vertex_attributes=leaves["attrs"],
+                               vertex_uv=leaves["uv"], texture=leaves["tex"], deferred_errors=True)
+        torch.autograd.backward([out.interpolated, out.sampled], [d["g_attr"], d["g_samp"]])
+        released[slot].record(compute)
+        # gradients go back on the copy stream, after the next step's upload and overlapping its compute:
+        # the host link runs one direction at a time (pinned copies measured at 211 GB/s up and 194 GB/s
+        # down alone, 170 GB/s each way when both run), so the step costs upload + readback, not more
+        computed[slot].record(compute)
+        grads = {k: t.grad for k, t in leaves.items()}
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(computed[slot])
+            for k, t in grads.items():
+                grads_host[k].copy_(t, non_blocking=True)
+                t.record_stream(copy_stream)
+        in_flight[slot] = grads
+
+    def run(total):
+        for e in released:
+            e.record(compute)
+        upload(0)
+        for i in range(total):
+            step(i, total)
+        compute.wait_stream(copy_stream)
+
+    run(2)  # warm-up: allocations and the tile-list capacity (reported back without a wait)
+    torch.cuda.synchronize(dev)
+    pdr_torch.check_deferred_errors(r)
+    barrier(world)
+    t0 = time.perf_counter()
+    run(steps)  # no host wait inside: render(deferred_errors=True) queues its status checks
+    torch.cuda.synchronize(dev)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    pdr_torch.check_deferred_errors(r)
+    return max_over_ranks(ms, world), h2d, d2h
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
     from photara_drender_gb300 import Rasterizer, _native
-    from photara_drender_gb300 import torch as pdr_torch
     from photara_drender_gb300.pipeline import RenderFwdBwd
     from photara_drender_gb300.rasterizer import _ptr
 
@@ -742,89 +979,28 @@ def run_gpu(args, world, rank, local):
     step_bytes = P * 96 + 2 * w["atlas"] ** 2 * w["channels"] * 4
 
     # ---- e2e: public autograd API with host buffers ---------------------------------------------------
-    # Every step copies its inputs from pinned host memory and reads the gradients back. The copies of
-    # step k+1 run on a copy stream while step k computes (two device buffer sets), so the step costs the
-    # larger of the two instead of their sum; all copies lie inside the timed region.
     e2e_steps = 0 if args.skip_e2e else max(2, args.steps)
     host = {k: v.cpu().pin_memory() for k, v in dict(clip=clip, attrs=t_attrs, uv=t_uv, tex=tex, g_attr=g_attr,
                                                      g_samp=g_samp).items()}
-    h_idx = torch.tensor(idx.astype(np.int64)).pin_memory()
-    host["idx"] = h_idx
-    h2d = sum(t.numel() * t.element_size() for t in host.values())
-    bufs = [{k: torch.empty_like(v, device=dev) for k, v in host.items()} for _ in range(2)]
-    grads_host = {k: torch.empty(host[k].shape, dtype=torch.float32).pin_memory() for k in ("clip", "attrs", "uv", "tex")}
-    d2h = sum(t.numel() * t.element_size() for t in grads_host.values())
-    copy_stream = torch.cuda.Stream(dev)
-    compute = torch.cuda.current_stream(dev)
-    copied = [torch.cuda.Event() for _ in range(2)]
-    released = [torch.cuda.Event() for _ in range(2)]
-    computed = [torch.cuda.Event() for _ in range(2)]
-    in_flight = [None, None]  # the gradients a slot's readback still reads
-
-    def upload(slot):
-        with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(released[slot])
-            for k, v in host.items():
-                bufs[slot][k].copy_(v, non_blocking=True)
-            copied[slot].record(copy_stream)
-
-    def e2e_step(i, total):
-        slot = i % 2
-        compute.wait_event(copied[slot])
-        if i + 1 < total:
-            upload((i + 1) % 2)
-        d = bufs[slot]
-        leaves = {k: d[k].detach().requires_grad_(True) for k in ("clip", "attrs", "uv", "tex")}
-        out = pdr_torch.render(leaves["clip"], d["idx"], (H, W), rasterizer=r, vertex_attributes=leaves["attrs"],
-                               vertex_uv=leaves["uv"], texture=leaves["tex"])
-        torch.autograd.backward([out.interpolated, out.sampled], [d["g_attr"], d["g_samp"]])
-        released[slot].record(compute)
-        # gradients go back on the copy stream, after the next step's upload and overlapping its compute:
-        # the host link runs one direction at a time (pinned copies measured at 211 GB/s up and 194 GB/s
-        # down alone, 170 GB/s each way when both run), so the step costs upload + readback, not more
-        computed[slot].record(compute)
-        grads = {k: t.grad for k, t in leaves.items()}
-        with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(computed[slot])
-            for k, t in grads.items():
-                grads_host[k].copy_(t, non_blocking=True)
-                t.record_stream(copy_stream)
-        in_flight[slot] = grads
-
-    def e2e_run(total):
-        for e in released:
-            e.record(compute)
-        upload(0)
-        for i in range(total):
-            e2e_step(i, total)
-        compute.wait_stream(copy_stream)
-
-    e2e_value = e2e_ms = None
-    if e2e_steps:
-        e2e_run(1)  # warm-up: allocations and the tile-list capacity
-        torch.cuda.synchronize(dev)
-        barrier(world)
-        t0 = time.perf_counter()
-        e2e_run(e2e_steps)
-        torch.cuda.synchronize(dev)
-        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world)
-        e2e_value = world * P / 1e6 / (e2e_ms / 1e3)
+    host["idx"] = torch.tensor(idx.astype(np.int64)).pin_memory()
+    e2e_ms, h2d, d2h = e2e_render(dev, r, host, H, W, e2e_steps, world)
+    e2e_value = world * P / 1e6 / (e2e_ms / 1e3) if e2e_ms else None
 
     # ---- CPU baseline (oracle restatement, bounded sample) --------------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         try:
-            rng = np.random.default_rng(1)
             tex_h = tex.cpu().numpy()
-            secs, done = 0.0, 0
-            while done < views and secs < CPU_SAMPLE_SECONDS:
-                secs += cpu_fwdbwd_sample(pos3, uv, idx, mats, attrs, tex_h, done, rng)
-                done += 1
-            cpu = {"value": done * H * W / 1e6 / secs, "unit": "Mpix/s", "cores": os.cpu_count() or 1,
-                   "kind": "port",
+            cores = os.cpu_count() or 1
+            clips_h = clip.cpu().numpy()
+            done, secs = cpu_sample_views(clips_h, uv, idx, attrs, tex_h, 0, CPU_SAMPLE_SECONDS)
+            done1, secs1 = cpu_sample_views(clips_h, uv, idx, attrs, tex_h, 1, CPU_SAMPLE_SECONDS)
+            cpu = {"value": done * H * W / 1e6 / secs, "unit": "Mpix/s", "cores": cores, "kind": "port",
                    "sample": f"views 0..{done - 1} of {views} (until {CPU_SAMPLE_SECONDS:.0f} s of work): full "
-                             f"forward+backward at {H}x{W} through the oracle (forward stages OpenMP over all "
-                             f"{os.cpu_count()} host threads, adjoint stages single-threaded), {secs:.1f} s"}
+                             f"forward+backward at {H}x{W} through the oracle, every stage on all {cores} host "
+                             f"threads, {secs:.1f} s",
+                   "one_core": {"value": done1 * H * W / 1e6 / secs1, "unit": "Mpix/s", "cores": 1,
+                                "sample": f"views 0..{done1 - 1}, the same path on one thread, {secs1:.1f} s"}}
         except Exception as e:  # the CPU leg never hides a GPU result
             cpu = {"value": None, "unit": "Mpix/s", "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"failed: {e}"}
@@ -881,16 +1057,17 @@ def run_gpu(args, world, rank, local):
                               "frac": step_bytes / (ms / 1e3) / 1e9 / hbm},
             "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                    "api": "photara_drender_gb300.torch.render (fused autograd op) + backward; inputs copied from "
-                           "pinned host memory every step (double-buffered on a copy stream), gradients read back "
-                           "on the same copy stream after the next step's upload (one link direction at a time)"},
+                    "api": "photara_drender_gb300.torch.render (fused autograd op, deferred_errors=True: no host "
+                           "wait per call) + backward; inputs copied from pinned host memory every step "
+                           "(double-buffered on a copy stream), gradients read back on the same copy stream after "
+                           "the next step's upload (one link direction at a time)"},
             "cpu_baseline": cpu,
             "parity": parity,
             "clocks": clocks.summary(),
         }
         if world == 1:
-            global SKIP_CPU_PAD
-            SKIP_CPU_PAD = args.skip_cpu
+            global SKIP_CPU
+            SKIP_CPU = args.skip_cpu
             for key, skip, leg in (("c1", args.skip_c1, c1_leg), ("bake", args.skip_bake, bake_leg),
                                    ("refine", args.skip_refine, refine_leg), ("c4", args.skip_c4, c4_leg),
                                    ("precond", args.skip_precond, c5_leg)):

@@ -999,35 +999,30 @@ static int g_reverse_order = 0;
 void ora_set_reverse_order(int reverse) { g_reverse_order = reverse != 0; }
 
 /* atlas_photometric_gradient.hlsl:45-108: per-pixel math in pixel order; the loss is
- * reduced per 64-pixel group with the shader's tree, then groups in order. */
-float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const float* uv,
-                               const float* target, const float* mask, uint32_t P, float eps,
-                               float norm, float* grad) {
+ * reduced per 64-pixel group with the shader's tree, then groups in order. Threaded without changing
+ * any sum: per-pixel loss terms in parallel, the gradient by texel-row owners that each visit all
+ * pixels in order (every texel's sum keeps the sequential order), the loss tree sequentially. */
+static void photometric_pixel(const float* tex, uint32_t tw, uint32_t th, const float* uv, const float* target,
+                              uint32_t p, float eps, float m, float norm, uint32_t tx[4], float w[4], float og[3],
+                              float* local) {
+    clamp_layout(uv[(uint64_t)p * 2], uv[(uint64_t)p * 2 + 1], tw, th, tx, w);
+    float l = 0.0f;
+    for (uint32_t c = 0; c < 3; ++c) {
+        float rendered = 0.0f;
+        for (int k = 0; k < 4; ++k) rendered += tex[(uint64_t)tx[k] * 3 + c] * w[k];
+        const float d = rendered - target[(uint64_t)p * 3 + c];
+        const float robust = sqrtf(d * d + eps * eps);
+        og[c] = d / robust * m * norm;
+        l += robust * m * norm;
+    }
+    *local = l;
+}
+
+static float group_tree_sum(const float* local, uint64_t n) {
     float loss = 0.0f;
     float group[64];
-    for (uint32_t g0 = 0; g0 < P; g0 += 64) {
-        for (uint32_t gi = 0; gi < 64; ++gi) {
-            const uint32_t p = g_reverse_order ? (g0 + gi < P ? P - 1 - (g0 + gi) : P) : g0 + gi;
-            float local = 0.0f;
-            if (p < P) {
-                const float m = mask[p];
-                if (m > 0.0f) {
-                    uint32_t tx[4];
-                    float w[4];
-                    clamp_layout(uv[(uint64_t)p * 2], uv[(uint64_t)p * 2 + 1], tw, th, tx, w);
-                    for (uint32_t c = 0; c < 3; ++c) {
-                        float rendered = 0.0f;
-                        for (int k = 0; k < 4; ++k) rendered += tex[(uint64_t)tx[k] * 3 + c] * w[k];
-                        const float d = rendered - target[(uint64_t)p * 3 + c];
-                        const float robust = sqrtf(d * d + eps * eps);
-                        const float og = d / robust * m * norm;
-                        local += robust * m * norm;
-                        for (int k = 0; k < 4; ++k) grad[(uint64_t)tx[k] * 3 + c] += og * w[k];
-                    }
-                }
-            }
-            group[gi] = local;
-        }
+    for (uint64_t g0 = 0; g0 < n; g0 += 64) {
+        for (uint32_t gi = 0; gi < 64; ++gi) group[gi] = g0 + gi < n ? local[g0 + gi] : 0.0f;
         for (uint32_t stride = 32; stride > 0; stride >>= 1)
             for (uint32_t gi = 0; gi < stride; ++gi) group[gi] += group[gi + stride];
         if (group[0] != 0.0f) loss += group[0];
@@ -1035,41 +1030,96 @@ float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const
     return loss;
 }
 
+float ora_photometric_gradient(const float* tex, uint32_t tw, uint32_t th, const float* uv,
+                               const float* target, const float* mask, uint32_t P, float eps,
+                               float norm, float* grad) {
+    const int rev = g_reverse_order;
+    float* local = (float*)malloc(((size_t)P + 1) * sizeof(float));  /* by visiting position */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)P; ++i) {
+        const uint32_t p = rev ? P - 1 - (uint32_t)i : (uint32_t)i;
+        local[i] = 0.0f;
+        const float m = mask[p];
+        if (m > 0.0f) {
+            uint32_t tx[4];
+            float w[4], og[3];
+            photometric_pixel(tex, tw, th, uv, target, p, eps, m, norm, tx, w, og, &local[i]);
+        }
+    }
+#pragma omp parallel
+    {
+        const uint32_t nt = (uint32_t)omp_get_num_threads(), tid = (uint32_t)omp_get_thread_num();
+        const uint32_t y_lo = (uint32_t)((uint64_t)th * tid / nt), y_hi = (uint32_t)((uint64_t)th * (tid + 1) / nt);
+        for (uint32_t i = 0; i < P && y_lo < y_hi; ++i) {
+            const uint32_t p = rev ? P - 1 - i : i;
+            const float m = mask[p];
+            if (!(m > 0.0f)) continue;
+            uint32_t tx[4];
+            float w[4], og[3], l;
+            clamp_layout(uv[(uint64_t)p * 2], uv[(uint64_t)p * 2 + 1], tw, th, tx, w);
+            const uint32_t ya = tx[0] / tw, yb = tx[2] / tw;
+            const int in0 = ya >= y_lo && ya < y_hi, in1 = yb >= y_lo && yb < y_hi;
+            if (!in0 && !in1) continue;
+            photometric_pixel(tex, tw, th, uv, target, p, eps, m, norm, tx, w, og, &l);
+            for (uint32_t c = 0; c < 3; ++c)
+                for (int k = 0; k < 4; ++k)
+                    if (k < 2 ? in0 : in1) grad[(uint64_t)tx[k] * 3 + c] += og[c] * w[k];
+        }
+    }
+    const float loss = group_tree_sum(local, P);
+    free(local);
+    return loss;
+}
+
 float ora_seam_gradient(const float* tex, uint32_t tw, uint32_t th, const float* pairs,
                         uint32_t npairs, float eps, float norm, float* grad) {
-    float loss = 0.0f;
-    float group[64];
-    for (uint32_t g0 = 0; g0 < npairs; g0 += 64) {
-        for (uint32_t gi = 0; gi < 64; ++gi) {
-            const uint32_t i = g_reverse_order ? (g0 + gi < npairs ? npairs - 1 - (g0 + gi) : npairs) : g0 + gi;
-            float local = 0.0f;
-            if (i < npairs) {
-                uint32_t t0[4], t1[4];
-                float w0[4], w1[4];
-                clamp_layout(pairs[(uint64_t)i * 4], pairs[(uint64_t)i * 4 + 1], tw, th, t0, w0);
-                clamp_layout(pairs[(uint64_t)i * 4 + 2], pairs[(uint64_t)i * 4 + 3], tw, th, t1, w1);
-                for (uint32_t c = 0; c < 3; ++c) {
-                    float c0 = 0.0f, c1 = 0.0f;
-                    for (int k = 0; k < 4; ++k) {
-                        c0 += tex[(uint64_t)t0[k] * 3 + c] * w0[k];
-                        c1 += tex[(uint64_t)t1[k] * 3 + c] * w1[k];
-                    }
-                    const float d = c0 - c1;
-                    const float robust = sqrtf(d * d + eps * eps);
-                    const float g = d / robust * norm;
-                    local += robust * norm;
-                    for (int k = 0; k < 4; ++k) {
-                        grad[(uint64_t)t0[k] * 3 + c] += g * w0[k];
-                        grad[(uint64_t)t1[k] * 3 + c] += -g * w1[k];
-                    }
+    const int rev = g_reverse_order;
+    float* local = (float*)malloc(((size_t)npairs + 1) * sizeof(float));
+    float* gs = (float*)malloc(((size_t)npairs * 3 + 1) * sizeof(float));
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)npairs; ++ii) {
+        const uint32_t i = rev ? npairs - 1 - (uint32_t)ii : (uint32_t)ii;
+        uint32_t t0[4], t1[4];
+        float w0[4], w1[4];
+        clamp_layout(pairs[(uint64_t)i * 4], pairs[(uint64_t)i * 4 + 1], tw, th, t0, w0);
+        clamp_layout(pairs[(uint64_t)i * 4 + 2], pairs[(uint64_t)i * 4 + 3], tw, th, t1, w1);
+        float l = 0.0f;
+        for (uint32_t c = 0; c < 3; ++c) {
+            float c0 = 0.0f, c1 = 0.0f;
+            for (int k = 0; k < 4; ++k) {
+                c0 += tex[(uint64_t)t0[k] * 3 + c] * w0[k];
+                c1 += tex[(uint64_t)t1[k] * 3 + c] * w1[k];
+            }
+            const float d = c0 - c1;
+            const float robust = sqrtf(d * d + eps * eps);
+            gs[(uint64_t)i * 3 + c] = d / robust * norm;
+            l += robust * norm;
+        }
+        local[ii] = l;
+    }
+#pragma omp parallel
+    {
+        const uint32_t nt = (uint32_t)omp_get_num_threads(), tid = (uint32_t)omp_get_thread_num();
+        const uint32_t y_lo = (uint32_t)((uint64_t)th * tid / nt), y_hi = (uint32_t)((uint64_t)th * (tid + 1) / nt);
+        for (uint32_t ii = 0; ii < npairs && y_lo < y_hi; ++ii) {
+            const uint32_t i = rev ? npairs - 1 - ii : ii;
+            uint32_t t0[4], t1[4];
+            float w0[4], w1[4];
+            clamp_layout(pairs[(uint64_t)i * 4], pairs[(uint64_t)i * 4 + 1], tw, th, t0, w0);
+            clamp_layout(pairs[(uint64_t)i * 4 + 2], pairs[(uint64_t)i * 4 + 3], tw, th, t1, w1);
+            for (uint32_t c = 0; c < 3; ++c) {
+                const float g = gs[(uint64_t)i * 3 + c];
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t ya = t0[k] / tw, yb = t1[k] / tw;
+                    if (ya >= y_lo && ya < y_hi) grad[(uint64_t)t0[k] * 3 + c] += g * w0[k];
+                    if (yb >= y_lo && yb < y_hi) grad[(uint64_t)t1[k] * 3 + c] += -g * w1[k];
                 }
             }
-            group[gi] = local;
         }
-        for (uint32_t stride = 32; stride > 0; stride >>= 1)
-            for (uint32_t gi = 0; gi < stride; ++gi) group[gi] += group[gi + stride];
-        if (group[0] != 0.0f) loss += group[0];
     }
+    const float loss = group_tree_sum(local, npairs);
+    free(local);
+    free(gs);
     return loss;
 }
 
@@ -1275,6 +1325,7 @@ int ora_refine(const float* init, const float* pos3, const float* uv2, uint32_t 
 double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C, const uint8_t* valid,
                        const int32_t* chart, float eps, float weight, float* grad) {
     uint64_t pairs = 0;
+#pragma omp parallel for schedule(static) reduction(+ : pairs)
     for (uint32_t y = 0; y < th; ++y)
         for (uint32_t x = 0; x < tw; ++x) {
             const uint64_t i = (uint64_t)y * tw + x;
@@ -1283,25 +1334,42 @@ double ora_tv_gradient(const float* tex, uint32_t tw, uint32_t th, uint32_t C, c
         }
     const double denom = (double)(pairs > 0 ? pairs : 1) * C;
     const float scale = (float)((double)weight / denom);
-    double loss = 0.0;
-    for (uint32_t y = 0; y < th; ++y)
-        for (uint32_t x = 0; x < tw; ++x) {
-            const uint64_t i = (uint64_t)y * tw + x;
-            for (int dir = 0; dir < 2; ++dir) {
-                uint64_t j;
-                if (dir == 0) { if (x + 1 >= tw) continue; j = i + 1; }
-                else { if (y + 1 >= th) continue; j = i + tw; }
-                if (!(valid[i] && valid[j] && (!chart || chart[i] == chart[j]))) continue;
-                for (uint32_t c = 0; c < C; ++c) {
-                    const float d = tex[j * C + c] - tex[i * C + c];
-                    const float r = sqrtf(d * d + eps * eps);
-                    loss += r;
-                    const float gg = d / r * scale;
-                    grad[j * C + c] += gg;
-                    grad[i * C + c] -= gg;
+    /* Texel-row owners: a thread owning rows [y_lo, y_hi) visits the pairs of rows y_lo - 1 .. y_hi - 1
+     * in the sequential (row-major, right then down) order and updates only its own texels, so every
+     * texel's sum keeps the sequential order. The loss (double) is summed per band, bands in order. */
+    const uint32_t nbands = (uint32_t)omp_get_max_threads();
+    double* band_loss = (double*)calloc(nbands, sizeof(double));
+#pragma omp parallel num_threads(nbands)
+    {
+        const uint32_t nt = (uint32_t)omp_get_num_threads(), tid = (uint32_t)omp_get_thread_num();
+        const uint32_t y_lo = (uint32_t)((uint64_t)th * tid / nt), y_hi = (uint32_t)((uint64_t)th * (tid + 1) / nt);
+        double bl = 0.0;
+        for (uint32_t y = y_lo > 0 ? y_lo - 1 : 0; y < y_hi; ++y)
+            for (uint32_t x = 0; x < tw; ++x) {
+                const uint64_t i = (uint64_t)y * tw + x;
+                const int own_i = y >= y_lo;
+                for (int dir = 0; dir < 2; ++dir) {
+                    uint64_t j;
+                    if (dir == 0) { if (x + 1 >= tw) continue; j = i + 1; }
+                    else { if (y + 1 >= th) continue; j = i + tw; }
+                    const int own_j = dir == 0 ? own_i : (y + 1 < y_hi);
+                    if (!own_i && !own_j) continue;
+                    if (!(valid[i] && valid[j] && (!chart || chart[i] == chart[j]))) continue;
+                    for (uint32_t c = 0; c < C; ++c) {
+                        const float d = tex[j * C + c] - tex[i * C + c];
+                        const float r = sqrtf(d * d + eps * eps);
+                        if (own_i) bl += r;
+                        const float gg = d / r * scale;
+                        if (own_j) grad[j * C + c] += gg;
+                        if (own_i) grad[i * C + c] -= gg;
+                    }
                 }
             }
-        }
+        band_loss[tid] = bl;
+    }
+    double loss = 0.0;
+    for (uint32_t b = 0; b < nbands; ++b) loss += band_loss[b];
+    free(band_loss);
     return loss * (double)weight / denom;
 }
 

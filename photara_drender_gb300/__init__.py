@@ -8,7 +8,7 @@ from .baking import (BakedTexture, TextureBakeOutput, TextureBaker, UnwrappedMes
 from .padding import (SurfaceFillStats, TexturePaddingStats, fill_texture_on_surface, pad_texture_atlas,
                       pad_texture_atlas_native)
 from . import formats
-from .torch import RenderOutput, interpolate, rasterize, render, texture
+from .torch import RenderOutput, check_deferred_errors, interpolate, rasterize, render, texture
 from .atlas import (AtlasOptimizationOptions, TexturedRender, atlas_total_variation, masked_charbonnier_loss,
                     optimize_texture_atlas, render_textured_mesh, seam_consistency_loss)
 
@@ -16,6 +16,7 @@ __version__ = "0.4.0+gb300"
 
 __all__ = [
     "ADDRESS_MODES", "AtlasOptimizationOptions", "BakedTexture", "CULL_MODES", "Context", "DeviceInfo", "Rasterizer",
+    "check_deferred_errors",
     "TextureBakeOutput", "TextureBaker", "TexturedRender", "UnwrappedMesh", "atlas_total_variation",
     "enumerate_devices", "fill_texture_on_surface", "formats", "interpolate", "pad_texture_atlas", "pad_texture_atlas_native",
     "SurfaceFillStats", "TexturePaddingStats", "masked_charbonnier_loss", "optimize_texture_atlas", "project_texture_atlas",

@@ -110,7 +110,8 @@ pdr_status pdr_render_raster(const pdr_render_args* a, void* stream) {
     const cudaError_t err = launch_raster_forward(
         a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count, a->width, a->height,
         a->viewports, a->cull_mode, a->tile_offsets, a->tile_triangles, a->capacity, a->raster,
-        a->barycentric_derivatives, (cudaStream_t)stream, (a->attributes || a->uv_attributes) ? &shade : nullptr);
+        a->barycentric_derivatives, (cudaStream_t)stream, (a->attributes || a->uv_attributes) ? &shade : nullptr,
+        a->status);
     return set_cuda_error(err, "render_raster");
 }
 

@@ -50,7 +50,7 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
                                   float* raster, float* deriv, cudaStream_t stream,
-                                  const RasterShade* shade = nullptr);
+                                  const RasterShade* shade = nullptr, const uint32_t* status = nullptr);
 
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,

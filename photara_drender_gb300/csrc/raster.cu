@@ -299,12 +299,12 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA, eight 8x4 warp regions
 
 template <bool kDeriv, bool kShade>
-__global__ void __launch_bounds__(kRasterThreads)
+__global__ void __launch_bounds__(kRasterThreads, 5)
 raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
                       const uint32_t* __restrict__ list, unsigned long long capacity, float4* __restrict__ raster,
-                      float4* __restrict__ deriv, ShadeArgs shade) {
+                      float4* __restrict__ deriv, ShadeArgs shade, const uint32_t* __restrict__ status) {
     const uint32_t view = blockIdx.y;
     const uint32_t tile = blockIdx.x;
     const size_t P = (size_t)W * H;
@@ -327,10 +327,13 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
     }
     const uint32_t seg = view * tiles + tile;
     const uint32_t b = offsets[seg];
-    uint32_t e = offsets[seg + 1];
-    if (e > capacity) e = (uint32_t)capacity;
-    if (b > e) e = b;
-    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, list, b, e);
+    const uint32_t e = offsets[seg + 1];
+    // A tile whose list did not fit the capacity (or whose offsets overflowed u32) visits every triangle
+    // with the binning rule instead: the result is the same, only slower, so no caller has to wait for
+    // the entry count before rasterizing.
+    const bool all = e > capacity || b > e || (status && status[kStatusTotalHi] != 0u);
+    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, all ? nullptr : list,
+                                                              all ? 0u : b, all ? T : e);
 }
 
 // ---- rasterize backward: shaders/rasterize_backward.hlsl:36-158 -------------------------
@@ -476,7 +479,8 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
-                                  float* raster, float* deriv, cudaStream_t stream, const RasterShade* shade) {
+                                  float* raster, float* deriv, cudaStream_t stream, const RasterShade* shade,
+                                  const uint32_t* status) {
     const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
     const dim3 grid(tcx * tcy, views);
     ShadeArgs sa{};
@@ -501,17 +505,17 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
     if (shade) {
         if (deriv)
             raster_forward_kernel<true, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                  offsets, list, capacity, r4, d4, sa);
+                                                                                  offsets, list, capacity, r4, d4, sa, status);
         else
             raster_forward_kernel<false, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                   offsets, list, capacity, r4, nullptr, sa);
+                                                                                   offsets, list, capacity, r4, nullptr, sa, status);
     } else {
         if (deriv)
             raster_forward_kernel<true, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                   offsets, list, capacity, r4, d4, sa);
+                                                                                   offsets, list, capacity, r4, d4, sa, status);
         else
             raster_forward_kernel<false, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                    offsets, list, capacity, r4, nullptr, sa);
+                                                                                    offsets, list, capacity, r4, nullptr, sa, status);
     }
     return cudaGetLastError();
 }

@@ -30,6 +30,7 @@
 
 #include <cuda_runtime.h>
 
+#include "bin_rect.cuh"
 #include "pdr_common.cuh"
 
 namespace pdr {
@@ -173,7 +174,10 @@ __device__ __forceinline__ unsigned long long depth_key(float depth, uint32_t t)
     return ((unsigned long long)o << 32) | t;
 }
 
-// Rasterizes tile (tx, ty) of view `v` from the triangle ids list[b..e).
+// Rasterizes tile (tx, ty) of view `v` from the triangle ids list[b..e). With list == nullptr the tile
+// visits the triangles [b, e) themselves and keeps those the binning would have listed for it (the
+// tile rectangle of src/rasterizer.cpp:73-125, as bin_count_kernel computes it): the path for a tile
+// whose list did not fit the tile-list capacity, with the same result.
 template <bool kDeriv, bool kShade, int TW, int TH, int CHUNK>
 __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, uint32_t ty,
                                             const uint32_t* __restrict__ list, uint32_t b, uint32_t e) {
@@ -213,20 +217,26 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
         __syncthreads();
         const uint32_t i = chunk + threadIdx.x;
         if (threadIdx.x < (uint32_t)CHUNK && i < e) {
-            const uint32_t t = list[i];
+            const uint32_t t = list ? list[i] : i;
             float sgn = 0.0f;
             uint32_t rect = kRectNone;
             float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
             float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f, s2x = 0.f, s2y = 0.f;
             const uint3 vi = idx[t];
-            if (vi.x < v.V && vi.y < v.V && vi.z < v.V) {
+            bool binned = vi.x < v.V && vi.y < v.V && vi.z < v.V;
+            if (!list && binned) {
+                const TriRect tr = triangle_tile_rect(clip, vi, v.W, v.H, vp, TW, TH);
+                binned = tr.x != kNoRect && tx >= (tr.x & 0xffffu) && tx <= (tr.x >> 16) && ty >= (tr.y & 0xffffu) &&
+                         ty <= (tr.y >> 16);
+            }
+            if (binned) {
                 p0 = clip[vi.x];
                 p1 = clip[vi.y];
                 p2 = clip[vi.z];
             }
             tri.t[threadIdx.x] = t;
             tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
-            if (vi.x < v.V && vi.y < v.V && vi.z < v.V) {
+            if (binned) {
                 if (!(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f)) {
                     s0x = p0.x / p0.w; s0y = p0.y / p0.w;
                     s1x = p1.x / p1.w; s1y = p1.y / p1.w;

@@ -87,9 +87,39 @@ class Context:
         self.lock = threading.RLock()
         self.info = _device_info(device_index)
         self.status = torch.zeros(_native.STATUS_WORDS, dtype=torch.int32, device=self.device)
+        self._pending = []  # (event, pinned copy of the status block, kind) of calls that did not wait
+        self._spare = []    # pinned buffers ready for reuse
 
     def stream(self):
         return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def defer_status(self, kind: str) -> None:
+        """Queues a copy of the status block to pinned host memory behind the work just enqueued,
+        without waiting for it; poll_status() hands it back once that work has finished. Inside a CUDA
+        graph capture nothing is queued (the captured work's status is not observable per replay)."""
+        if torch.cuda.is_current_stream_capturing():
+            return
+        if len(self._pending) >= 64:  # bound the queue: wait for the oldest copy
+            self._pending[0][0].synchronize()
+        buf = self._spare.pop() if self._spare else torch.empty(_native.STATUS_WORDS, dtype=torch.int32,
+                                                                  pin_memory=True)
+        buf.copy_(self.status, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self._pending.append((ev, buf, kind))
+
+    def poll_status(self, wait: bool = False):
+        """[(kind, status words)] of the queued copies whose work has finished (all of them when `wait`),
+        oldest first."""
+        done = []
+        if torch.cuda.is_current_stream_capturing():  # no event queries while a capture is recording
+            return done
+        while self._pending and (wait or self._pending[0][0].query()):
+            ev, buf, kind = self._pending.pop(0)
+            ev.synchronize()
+            done.append((kind, [int(x) for x in buf.tolist()]))
+            self._spare.append(buf)
+        return done
 
 
 class _Io:

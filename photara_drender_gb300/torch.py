@@ -185,7 +185,32 @@ _MODES = {"none": 0, "back": 1, "front": 2}
 _ADDRESS = {"clamp": 0, "wrap": 1, "mirror": 2}
 
 
-def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, cull, mode):
+def _apply_status(r: Rasterizer, reports) -> None:
+    """Acts on status blocks of earlier calls that did not wait for their work: grows the tile-list
+    capacity to what the binning needed, raises the errors the device recorded."""
+    from . import _native
+
+    for kind, st in reports:
+        if kind == "render_forward":
+            if st[_native.STATUS_TILE_ENTRIES_HI] != 0:
+                raise OverflowError("Tile triangle list exceeds backend limits")
+            total = st[_native.STATUS_TILE_ENTRIES] & 0xFFFFFFFF
+            r._render_capacity = max(getattr(r, "_render_capacity", 0), total + total // 8 + 1024)
+        elif st[_native.STATUS_TEXEL_ERROR] == 1:
+            raise ValueError("uv contains a non-finite value in a covered pixel")
+        elif st[_native.STATUS_TEXEL_ERROR] == 2:
+            raise IndexError("uv is too large for portable texture addressing")
+
+
+def check_deferred_errors(rasterizer: Rasterizer) -> None:
+    """Waits for every `render(..., deferred_errors=True)` call made on this rasterizer and raises the
+    first error the device recorded for them (ValueError / IndexError / OverflowError, as the
+    synchronous path raises at once)."""
+    with rasterizer.context.lock:
+        _apply_status(rasterizer, rasterizer.context.poll_status(wait=True))
+
+
+def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, cull, mode, deferred=False):
     from . import _native
     from .pipeline import RenderArgsC
     from .rasterizer import TILE, _ptr
@@ -201,9 +226,10 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
                uv=torch.empty((views, h, w, 2), **f) if uv_attrs is not None else None,
                sampled=torch.empty((views, h, w, 4), **f) if tex is not None else None)
     offsets = torch.empty(views * tiles + 1, dtype=torch.int32, device=dev)
+    _apply_status(r, ctx.poll_status())
     capacity = max(getattr(r, "_render_capacity", 0), 2 * T * views + 1024)
     L = _native.lib()
-    for _ in range(3):
+    for _ in range(1 if deferred else 3):
         lst = torch.empty(capacity, dtype=torch.int32, device=dev)
         ws_bytes = L.pdr_render_workspace_bytes(views, T, w, h, capacity)
         ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
@@ -223,6 +249,12 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
         a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
         a.raster, a.barycentric_derivatives = out["raster"].data_ptr(), out["deriv"].data_ptr()
         _native.check(L.pdr_render_forward(C.addressof(a), ctx.stream()))
+        if deferred:
+            # No wait: a tile whose list overflowed the capacity is rasterized from all triangles with the
+            # binning rule (same result, slower); the entry count reaches the host later and sizes the
+            # capacity of the next calls.
+            ctx.defer_status("render_forward")
+            return out
         st = ctx.status.cpu()
         total = int(st[_native.STATUS_TILE_ENTRIES]) & 0xFFFFFFFF
         if int(st[_native.STATUS_TILE_ENTRIES_HI]) != 0:
@@ -237,10 +269,11 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
 class _RenderFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, positions, vertex_attributes, vertex_uv, texture_values, indices, resolution, rasterizer,
-                viewport, cull_mode, address_mode):
+                viewport, cull_mode, address_mode, deferred_errors):
         from .rasterizer import _viewports
 
         r = rasterizer
+        deferred = bool(deferred_errors) or torch.cuda.is_current_stream_capturing()
         with r.context.lock:
             clip = positions.detach()
             batched = clip.ndim == 3
@@ -251,8 +284,10 @@ class _RenderFunction(torch.autograd.Function):
             attrs = vertex_attributes.detach().contiguous() if vertex_attributes is not None else None
             uva = vertex_uv.detach().contiguous() if vertex_uv is not None else None
             tex = texture_values.detach().contiguous() if texture_values is not None else None
-            out = _render_forward(r, clip, idx, h, w, attrs, uva, tex, vps, _MODES[cull_mode], _ADDRESS[address_mode])
+            out = _render_forward(r, clip, idx, h, w, attrs, uva, tex, vps, _MODES[cull_mode], _ADDRESS[address_mode],
+                                  deferred)
         ctx.r, ctx.vps, ctx.batched, ctx.viewport = r, vps, batched, viewport
+        ctx.deferred = deferred
         ctx.mode = _ADDRESS[address_mode]
         # outputs the loss does not use get no gradient (None), not a zero tensor: a zero raster or uv
         # gradient would otherwise run the separate adjoints over every pixel for nothing
@@ -302,13 +337,18 @@ class _RenderFunction(torch.autograd.Function):
                                                                                 tex.shape[0], ctx.mode)
                 a.grad_sampled, a.grad_texture = gs.data_ptr(), grad_tex.data_ptr()
             a.grad_clip_positions, a.status = grad_clip.data_ptr(), r.context.status.data_ptr()
+            deferred = ctx.deferred or torch.cuda.is_current_stream_capturing()
+            _apply_status(r, r.context.poll_status())
             r.context.status.zero_()
             _native.check(_native.lib().pdr_render_backward(C.addressof(a), r.context.stream()))
-            st = r.context.status.cpu()
-            if int(st[_native.STATUS_TEXEL_ERROR]) == 1:
-                raise ValueError("uv contains a non-finite value in a covered pixel")
-            if int(st[_native.STATUS_TEXEL_ERROR]) == 2:
-                raise IndexError("uv is too large for portable texture addressing")
+            if deferred:
+                r.context.defer_status("render_backward")
+            else:
+                st = r.context.status.cpu()
+                if int(st[_native.STATUS_TEXEL_ERROR]) == 1:
+                    raise ValueError("uv contains a non-finite value in a covered pixel")
+                if int(st[_native.STATUS_TEXEL_ERROR]) == 2:
+                    raise IndexError("uv is too large for portable texture addressing")
         # upstream gradients on the raster or uv outputs themselves go through the separate adjoints
         extra = g_raster.contiguous() if g_raster is not None else None
         if g_uv is not None and uva is not None:
@@ -319,17 +359,24 @@ class _RenderFunction(torch.autograd.Function):
             grad_clip = grad_clip + r.backward(clip, idx, raster, extra.contiguous(), ctx.viewport)
         if not ctx.batched:
             grad_clip = grad_clip[0]
-        return grad_clip, grad_attr, grad_uv, grad_tex, None, None, None, None, None, None
+        return grad_clip, grad_attr, grad_uv, grad_tex, None, None, None, None, None, None, None
 
 
 def render(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequence[int], *, rasterizer: Rasterizer,
            vertex_attributes: Optional[torch.Tensor] = None, vertex_uv: Optional[torch.Tensor] = None,
            texture: Optional[torch.Tensor] = None, viewport=None, cull_mode: str = "none",
-           address_mode: str = "clamp") -> RenderOutput:
+           address_mode: str = "clamp", deferred_errors: bool = False) -> RenderOutput:
     """rasterize -> interpolate(vertex_attributes), interpolate(vertex_uv) -> texture in one fused forward
     kernel and one fused backward kernel: the outputs of `rasterize`, two `interpolate` calls and `texture`,
     bit-identical to them, with the same gradients. vertex_attributes [V, A] (A <= 8) and vertex_uv [V, 2]
-    are shared by all views; the texture is [H, W, 4] and needs vertex_uv."""
+    are shared by all views; the texture is [H, W, 4] and needs vertex_uv.
+
+    By default each forward and backward waits for its kernels to check the device status (tile-list
+    capacity, non-finite or out-of-range uv) and raises at once, as the separate calls do. With
+    deferred_errors=True (and always inside a CUDA graph capture) neither waits: the host can run ahead
+    of the GPU and the pass can be captured. A tile-list overflow then costs time, not correctness (the
+    tiles concerned rasterize from all triangles with the binning rule), and errors the device records
+    are raised by a later call on the same rasterizer, or by check_deferred_errors(rasterizer)."""
     if positions.dtype != torch.float32 or positions.ndim not in (2, 3) or positions.shape[-1] != 4:
         raise ValueError("positions must be a float32 tensor with shape [vertex_count, 4]")
     if indices.ndim != 2 or indices.shape[1] != 3:
@@ -347,4 +394,5 @@ def render(positions: torch.Tensor, indices: torch.Tensor, resolution: Sequence[
     if texture is not None and (vertex_uv is None or texture.ndim != 3 or texture.shape[2] != 4):
         raise ValueError("texture must have shape [height, width, 4] and needs vertex_uv")
     return RenderOutput(*_RenderFunction.apply(positions, vertex_attributes, vertex_uv, texture, indices,
-                                               tuple(resolution), rasterizer, viewport, cull_mode, address_mode))
+                                               tuple(resolution), rasterizer, viewport, cull_mode, address_mode,
+                                               deferred_errors))

@@ -171,3 +171,115 @@ def test_fused_render_equals_separate_ops(rast, batched):
         assert x.shape == y.shape
         scale = float(y.abs().max())
         assert float((x - y).abs().max()) <= 1e-4 * scale + 1e-7, k
+
+
+def _render_case(seed=4, views=3, res=(96, 112)):
+    rng = np.random.default_rng(seed)
+    pos3, idx = S.icosphere(4)
+    mats, _ = S.orbit_cameras(views)
+    V = pos3.shape[0]
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)  # noqa: E731
+    inputs = dict(clip=t(S.clip_positions(pos3, mats)), attrs=t(rng.uniform(size=(V, 3))),
+                  uv=t(S.spherical_uv(pos3)), tex=t(rng.uniform(size=(64, 48, 4))))
+    grads = dict(a=t(rng.normal(size=(views,) + res + (3,))), s=t(rng.normal(size=(views,) + res + (4,))))
+    return inputs, torch.tensor(idx.astype(np.int64), device=dev), res, grads
+
+
+def test_render_without_host_waits_captures_in_a_cuda_graph():
+    """torch.render with deferred_errors=True waits for nothing, so its forward and backward can be
+    captured in a CUDA graph: replays give the forward outputs of an ordinary call bit for bit and its
+    gradients up to the summation order of the atomics."""
+    r = pdr.Rasterizer()
+    inputs, tidx, res, grads = _render_case()
+    static = {k: v.clone().requires_grad_(True) for k, v in inputs.items()}
+
+    def step():
+        out = pdr.render(static["clip"], tidx, res, rasterizer=r, vertex_attributes=static["attrs"],
+                         vertex_uv=static["uv"], texture=static["tex"], deferred_errors=True)
+        torch.autograd.backward([out.interpolated, out.sampled], [grads["a"], grads["s"]])
+        return out
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):  # warm-up outside the capture sizes the tile-list capacity
+        for _ in range(2):
+            for v in static.values():
+                v.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    pdr.check_deferred_errors(r)
+    for v in static.values():
+        v.grad = None
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = step()
+    ref_leaves = {k: v.clone().requires_grad_(True) for k, v in inputs.items()}
+    ref = pdr.render(ref_leaves["clip"], tidx, res, rasterizer=r, vertex_attributes=ref_leaves["attrs"],
+                     vertex_uv=ref_leaves["uv"], texture=ref_leaves["tex"])
+    torch.autograd.backward([ref.interpolated, ref.sampled], [grads["a"], grads["s"]])
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        for x, y in ((out.raster, ref.raster), (out.interpolated, ref.interpolated), (out.uv, ref.uv),
+                     (out.sampled, ref.sampled)):
+            assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+        for k in inputs:
+            x, y = static[k].grad, ref_leaves[k].grad
+            assert float((x - y).abs().max()) <= 1e-5 * float(y.abs().max()) + 1e-7, k
+    pdr.check_deferred_errors(r)
+
+
+def test_tile_list_overflow_keeps_results_exact():
+    """A tile list far below the binning's need: the raster kernel rasterizes the tiles whose lists were
+    cut from all triangles with the binning rule, so the fused forward (and the separate rasterize call)
+    give exactly the outputs of a sufficient list, and the status reports the overflow."""
+    import ctypes as C
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.pipeline import RenderFwdBwd
+
+    inputs, tidx, res, grads = _render_case(seed=5, views=2, res=(80, 72))
+    r = pdr.Rasterizer()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    V = inputs["clip"].shape[1]
+    outs = []
+    for cap in (None, 300):
+        p = RenderFwdBwd(r, tidx, V, 2, res[0], res[1], 3, tuple(inputs["tex"].shape), capacity=cap)
+        p.forward(inputs["clip"], inputs["attrs"], inputs["uv"], inputs["tex"], stream)
+        torch.cuda.synchronize()
+        overflow = int(p.status[_native.STATUS_TILE_OVERFLOW])
+        outs.append(({k: getattr(p, k).clone() for k in ("raster", "deriv", "attr_out", "uv", "sampled")}, overflow))
+    (full, ov0), (cut, ov1) = outs
+    assert ov0 == 0 and ov1 == 1
+    for k in full:
+        assert torch.equal(full[k].view(torch.int32), cut[k].view(torch.int32)), k
+    # the separate, reference-shaped path (sorted bins) with the same cut list
+    sep = RenderFwdBwd(r, tidx, V, 2, res[0], res[1], 3, tuple(inputs["tex"].shape), capacity=300, fused=False)
+    sep.forward(inputs["clip"], inputs["attrs"], inputs["uv"], inputs["tex"], stream)
+    torch.cuda.synchronize()
+    assert int(sep.status[_native.STATUS_TILE_OVERFLOW]) == 1
+    assert torch.equal(sep.raster.view(torch.int32), full["raster"].view(torch.int32))
+
+
+def test_deferred_errors_raise_later():
+    """A non-finite uv in a covered pixel: the synchronous render raises in backward as the reference's
+    texture adjoint does; with deferred_errors=True nothing waits and the error is raised by
+    check_deferred_errors."""
+    inputs, tidx, res, grads = _render_case(seed=6, views=1)
+    uv = inputs["uv"].clone()
+    uv[:] = float("nan")
+    r = pdr.Rasterizer()
+
+    def run(deferred):
+        leaves = {k: v.clone().requires_grad_(True) for k, v in dict(inputs, uv=uv).items()}
+        out = pdr.render(leaves["clip"][:1], tidx, res, rasterizer=r, vertex_attributes=leaves["attrs"],
+                         vertex_uv=leaves["uv"], texture=leaves["tex"], deferred_errors=deferred)
+        torch.autograd.backward([out.interpolated, out.sampled], [grads["a"][:1], grads["s"][:1]])
+
+    with pytest.raises(ValueError, match="non-finite"):
+        run(False)
+    run(True)
+    with pytest.raises(ValueError, match="non-finite"):
+        pdr.check_deferred_errors(r)
+    pdr.check_deferred_errors(r)  # reported once
