@@ -582,7 +582,76 @@ def refine_leg(dev, hbm):
             "frac": step_bytes * c["steps"] / opt_s / 1e9 / hbm, "mean_abs_error_vs_ground_truth": err,
             "timing": "TextureBaker refinement optimisation wall time (graph record + instantiate + launch + "
                       "sync), texture starting at 0.5",
-            "cpu_baseline": refine_cpu_baseline(st, c)}
+            "cpu_baseline": refine_cpu_baseline(st, c),
+            "photometric_reductions": photometric_reduction_rate(dev, st)}
+
+
+def photometric_reduction_rate(dev, st):
+    """The photometric gradient kernel of step 0 (its batch of views) timed alone: its bilinear-tap
+    reductions (four red.v4 per masked pixel) per second against the calibrated scattered-reduction rates."""
+    import torch
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    o = st.options
+    n, B = len(st.weights), int(o.batch_size)
+    masked = sum(int((st.keep[3 * (b % n) + 2] > 0).sum().item()) for b in range(B))
+    tex = torch.full((int(o.height), int(o.width), 3), 0.5, device=dev)
+    grad = torch.zeros((int(o.height), int(o.width), 4), device=dev)
+    loss = torch.zeros(1, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def run():
+        _native.call("pdr_refine_photometric", _ptr(tex), int(o.width), int(o.height), _ptr(st.table_dev), n,
+                     st.max_pixels, 0, B, float(o.photometric_epsilon), 1e-6, _ptr(grad), _ptr(loss), stream)
+
+    run()
+    times = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(np.median(times))
+    peaks = reduction_peaks(dev)
+    rate = 4 * masked / t
+    return {"kernel": "photometric_kernel (one step: batch views of step 0)", "seconds": t,
+            "reductions": 4 * masked, "reductions_per_s": rate, "calibrated_peaks_per_s": peaks,
+            "frac_of_l2_resident_peak": rate / peaks["l2_resident_32MB"],
+            "frac_of_hbm_peak": rate / peaks["hbm_268MB"],
+            "note": "peaks: pdr_calibrate_reductions (red.global.add.v4.f32 to pseudo-random 16-byte slots) into "
+                    "a 32 MB buffer that stays in L2 and a 268 MB one that does not"}
+
+
+def reduction_peaks(dev):
+    """Scattered red.global.add.v4.f32 rates (reductions / s) of pdr_calibrate_reductions: into a 32 MB
+    buffer that stays in L2, and into a 268 MB one (the size of a 4096^2 RGBA gradient) that does not."""
+    import torch
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    out = {}
+    for name, mb in (("l2_resident_32MB", 32), ("hbm_268MB", 268)):
+        slots = mb * 1024 * 1024 // 16
+        buf = torch.zeros((slots, 4), dtype=torch.float32, device=dev)
+        n = 64 * 1024 * 1024
+        _native.call("pdr_calibrate_reductions", _ptr(buf), slots, n, 1, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for k in range(3):
+            _native.call("pdr_calibrate_reductions", _ptr(buf), slots, n, 2 + k, stream)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        out[name] = 3 * n / (e0.elapsed_time(e1) / 1e3)
+        del buf
+    return out
 
 
 def refine_cpu_baseline(st, c):
@@ -796,10 +865,31 @@ def c5_leg(dev, hbm):
 # ---- GPU arm ------------------------------------------------------------------------------------------
 
 STAGES = ["bin_tiles", "rasterize_forward+shade", "render_backward"]
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the two fused kernels on this
-# 64-view workload, from a single-pass ncu capture of the full-size run (the capture cannot run inside
-# the timed region; it is re-taken whenever these kernels change).
-KERNEL_TRAFFIC = {"rasterize_forward+shade": 2160528713 + 4589287790, "render_backward": 6810716197 + 1586401207}
+# Source files each timed kernel is compiled from, and DRAM bytes per launch (dram__bytes_read.sum +
+# dram__bytes_write.sum) of that kernel on this 64-view workload from a single-pass ncu capture of the
+# full-size run, recorded with the SHA-256 of those sources at capture time. A capture cannot run
+# inside the timed region; when the sources no longer hash to the recorded value the figure belongs to
+# other code and the line reports traffic as null.
+KERNEL_SOURCES = {
+    "rasterize_forward+shade": ["raster.cu", "raster_tile.cuh", "bin_rect.cuh", "pdr_common.cuh"],
+    "render_backward": ["fused.cu", "render_bwd_tile.cuh", "pdr_common.cuh"],
+}
+KERNEL_TRAFFIC = {}  # stage -> (sha256 of its sources, bytes per launch)
+
+
+def kernel_source_hash(stage: str) -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES[stage]:
+        with open(os.path.join(ROOT, "photara_drender_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def recorded_traffic(stage: str):
+    rec = KERNEL_TRAFFIC.get(stage)
+    return rec[1] if rec and rec[0] == kernel_source_hash(stage) else None
 
 
 def stage_bytes(w, T, V, entries):
@@ -1049,7 +1139,8 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": pipe.kernels_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": KERNEL_TRAFFIC.get(dom_name) if views == 64 and w["atlas"] == 4096 else None,
+                         "traffic": recorded_traffic(dom_name) if views == 64 and w["atlas"] == 4096 else None,
+                         "traffic_source_sha256": kernel_source_hash(dom_name),
                          "algorithmic_bytes": sbytes[dom_name], "ms": float(stage_ms[dom])},
             "stages_ms": {n: float(t) for n, t in zip(STAGES, stage_ms)},
             "pipeline": "fused" if pipe.fused else "separate kernels",

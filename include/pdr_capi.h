@@ -318,6 +318,11 @@ typedef struct {
     float* grad_attributes;       /* [V][A] summed over views */
     float* grad_uv_attributes;    /* [V][2] summed over views */
     float* grad_texture;          /* [texture_height][texture_width][4] summed over views */
+    /* Optional [views][H][W][8], 16-byte aligned: the texel differences of the bilinear sample along u
+     * and v per channel ((1-fy)(c10-c00) + fy(c11-c01), then the same along v), written by the forward
+     * for covered pixels and read by the backward for texture_grad_uv instead of gathering the four
+     * texels again. Null: the backward gathers them. Results are identical either way. */
+    float* sample_differences;
 } pdr_render_args;
 
 PDR_API size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
@@ -335,6 +340,15 @@ PDR_API pdr_status pdr_render_raster(const pdr_render_args* args, void* stream);
 /* The adjoints of the forward in one pixel pass: texture_backward, interpolate_backward for both
  * attribute sets (raster gradients summed) and rasterize_backward. */
 PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream);
+
+
+/* ---- calibration --------------------------------------------------------------------------------
+ * No counterpart in the reference. `reductions` red.global.add.v4.f32 operations (1.0 into each of
+ * four floats) to pseudo-random 16-byte slots of buffer [slots][4], from a grid of 8 CTAs per SM:
+ * timed by the caller, the rate of scattered vector reductions the GPU sustains, against which the
+ * gradient scatters of the refiner and the fused adjoint are reported. */
+PDR_API pdr_status pdr_calibrate_reductions(float* buffer, uint64_t slots, uint64_t reductions, uint32_t seed,
+                                            void* stream);
 
 
 /* ---- allocation-free binning ------------------------------------------------------------------ */

@@ -13,10 +13,20 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphotara_drender_gb300.so")
 CPP_LIB = os.path.join(HERE, "libphotara_drender.so")  # the C++ API of include/photara_drender/*.hpp
 CPP_SOURCES = [os.path.join(HERE, "cpp", "photara_drender.cpp")]
-SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "precond.cu", "batch.cu", "bvh.cu", "padding.cu", "mip.cu", "near.cu", "capi.cu"]
+SOURCES = ["raster.cu", "shading.cu", "bake.cu", "refine.cu", "drivers.cu", "fused.cu", "no_alloc.cu", "precond.cu", "batch.cu", "bvh.cu", "padding.cu", "mip.cu", "near.cu", "calibrate.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-         "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
+         "-I", CSRC, "-I", INCLUDE]
+# Multiply-add contraction stays off wherever a result is compared bit for bit with the reference's
+# arithmetic (every fp32 operation rounding on its own), including the discrete decisions adjoints make
+# from fp32 values (visit rules, texel addresses). Translation units whose every result is held to a
+# tolerance contract a*b+c into one FMA: the ray caster (visibility decided against a 1e-5 band) and
+# the calibration kernel.
+FMA_SOURCES = {"bvh.cu", "calibrate.cu"}
+
+
+def fmad_flag(src: str) -> str:
+    return "-fmad=true" if src in FMA_SOURCES else "-fmad=false"
 
 
 def nvcc() -> str:
@@ -45,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, fmad_flag(src), "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         res = subprocess.run(cmd, capture_output=True, text=True)

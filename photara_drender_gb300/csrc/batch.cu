@@ -167,6 +167,7 @@ batch_raster_kernel(const BatchJob* __restrict__ jobs, const unsigned long long*
     v.shade.th = b.th;
     v.shade.mode = mode;
     v.shade.sampled = b.tex ? b.sampled : nullptr;
+    v.shade.sdiff = nullptr;
     const uint32_t s = offsets[tg];
     uint32_t e = offsets[tg + 1];
     if (e > capacity) e = (uint32_t)capacity;
@@ -205,6 +206,7 @@ batch_backward_kernel(const BatchJob* __restrict__ jobs, const unsigned long lon
     v.g_attr = b.g_attr;
     v.g_uv = b.g_uv;
     v.g_tex = b.g_tex;
+    v.sdiff = nullptr;
     v.status = status;
     render_backward_tile<kA>(v, tile % b.btcx, tile / b.btcx);
 }

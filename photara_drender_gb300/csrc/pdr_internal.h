@@ -44,6 +44,7 @@ struct RasterShade {
     const float* texture;
     uint32_t texture_width, texture_height, address_mode;
     float* sampled;
+    float* sample_differences;  // optional [views][H][W][8] (pdr_render_args.sample_differences)
 };
 
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <float.h>
 
+#include <algorithm>
+
 #include "pdr_common.cuh"
 #include "pdr_internal.h"
 #include "bin_rect.cuh"
@@ -298,8 +300,14 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 
 constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA, eight 8x4 warp regions
 
+// true when tile list [b, e) lost entries to the capacity, or the list offsets overflowed u32
+__device__ __forceinline__ bool tile_list_cut(uint32_t b, uint32_t e, unsigned long long capacity,
+                                              const uint32_t* __restrict__ status) {
+    return e > capacity || b > e || (status && status[kStatusTotalHi] != 0u);
+}
+
 template <bool kDeriv, bool kShade>
-__global__ void __launch_bounds__(kRasterThreads, 5)
+__global__ void __launch_bounds__(kRasterThreads)
 raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
@@ -324,16 +332,53 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
         if (shade.attr_out) v.shade.attr_out = shade.attr_out + view * P * shade.A;
         if (shade.uv_out) v.shade.uv_out = shade.uv_out + view * P;
         if (shade.sampled) v.shade.sampled = shade.sampled + view * P;
+        if (shade.sdiff) v.shade.sdiff = shade.sdiff + view * P * 2;
     }
     const uint32_t seg = view * tiles + tile;
     const uint32_t b = offsets[seg];
     const uint32_t e = offsets[seg + 1];
-    // A tile whose list did not fit the capacity (or whose offsets overflowed u32) visits every triangle
-    // with the binning rule instead: the result is the same, only slower, so no caller has to wait for
-    // the entry count before rasterizing.
-    const bool all = e > capacity || b > e || (status && status[kStatusTotalHi] != 0u);
-    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, all ? nullptr : list,
-                                                              all ? 0u : b, all ? T : e);
+    // a tile whose list did not fit the capacity is left to raster_overflow_kernel
+    if (tile_list_cut(b, e, capacity, status)) return;
+    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, list, b, e);
+}
+
+// The tiles whose lists did not fit the tile-list capacity (or whose offsets overflowed u32), each
+// rasterized from all triangles with the binning rule: the result is the one a sufficient list gives,
+// only slower, so no caller has to wait for the entry count before rasterizing. Launched after
+// raster_forward_kernel with a few CTAs per SM that walk all tiles; when nothing overflowed every CTA
+// only reads offsets.
+template <bool kDeriv, bool kShade>
+__global__ void __launch_bounds__(kRasterThreads)
+raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
+                       uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
+                       uint32_t tiles, uint32_t views, const uint32_t* __restrict__ offsets,
+                       unsigned long long capacity, float4* __restrict__ raster, float4* __restrict__ deriv,
+                       ShadeArgs shade, const uint32_t* __restrict__ status) {
+    const size_t P = (size_t)W * H;
+    for (uint32_t seg = blockIdx.x; seg < tiles * views; seg += gridDim.x) {
+        if (!tile_list_cut(offsets[seg], offsets[seg + 1], capacity, status)) continue;  // block-uniform
+        const uint32_t view = seg / tiles, tile = seg % tiles;
+        RasterView v;
+        v.clip = clip_all + (size_t)view * V;
+        v.idx = idx;
+        v.V = V;
+        v.T = T;
+        v.W = W;
+        v.H = H;
+        v.cull = cull;
+        v.vp = viewports[view];
+        v.raster = raster + view * P;
+        v.deriv = kDeriv ? deriv + view * P : nullptr;
+        v.shade = shade;
+        if (kShade) {
+            if (shade.attr_out) v.shade.attr_out = shade.attr_out + view * P * shade.A;
+            if (shade.uv_out) v.shade.uv_out = shade.uv_out + view * P;
+            if (shade.sampled) v.shade.sampled = shade.sampled + view * P;
+            if (shade.sdiff) v.shade.sdiff = shade.sdiff + view * P * 2;
+        }
+        raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads, true>(v, tile % tcx, tile / tcx, nullptr, 0u, T);
+        __syncthreads();  // the tile routine's shared memory is reused by the next tile
+    }
 }
 
 // ---- rasterize backward: shaders/rasterize_backward.hlsl:36-158 -------------------------
@@ -495,6 +540,7 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
         sa.th = shade->texture_height;
         sa.mode = shade->address_mode;
         sa.sampled = reinterpret_cast<float4*>(shade->sampled);
+        sa.sdiff = reinterpret_cast<float4*>(shade->sample_differences);
     }
     const float4* c4 = reinterpret_cast<const float4*>(clip);
     const uint3* i3 = reinterpret_cast<const uint3*>(idx);
@@ -517,6 +563,18 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
             raster_forward_kernel<false, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
                                                                                     offsets, list, capacity, r4, nullptr, sa, status);
     }
+    // after the main launch: the tiles it skipped because their lists were cut
+    const unsigned overflow_blocks = (unsigned)std::min<uint64_t>((uint64_t)tiles * views, (uint64_t)num_sms() * 4u);
+#define PDR_RASTER_OVERFLOW(D, S, DP)                                                                              \
+    raster_overflow_kernel<D, S><<<overflow_blocks, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, \
+                                                                                  tiles, views, offsets, capacity, r4, \
+                                                                                  DP, sa, status)
+    if (shade) {
+        if (deriv) PDR_RASTER_OVERFLOW(true, true, d4); else PDR_RASTER_OVERFLOW(false, true, nullptr);
+    } else {
+        if (deriv) PDR_RASTER_OVERFLOW(true, false, d4); else PDR_RASTER_OVERFLOW(false, false, nullptr);
+    }
+#undef PDR_RASTER_OVERFLOW
     return cudaGetLastError();
 }
 

@@ -45,6 +45,7 @@ struct ShadeArgs {
     const float4* tex;      // [th][tw][4], or nullptr
     uint32_t tw, th, mode;
     float4* sampled;        // [H][W][4]
+    float4* sdiff;          // [H][W][2]: texel differences along u and v per channel, or nullptr
 };
 
 // One view of one mesh as the tile routine sees it.
@@ -174,11 +175,11 @@ __device__ __forceinline__ unsigned long long depth_key(float depth, uint32_t t)
     return ((unsigned long long)o << 32) | t;
 }
 
-// Rasterizes tile (tx, ty) of view `v` from the triangle ids list[b..e). With list == nullptr the tile
-// visits the triangles [b, e) themselves and keeps those the binning would have listed for it (the
+// Rasterizes tile (tx, ty) of view `v` from the triangle ids list[b..e). With kAll the tile visits the
+// triangles [b, e) themselves (list unused) and keeps those the binning would have listed for it (the
 // tile rectangle of src/rasterizer.cpp:73-125, as bin_count_kernel computes it): the path for a tile
 // whose list did not fit the tile-list capacity, with the same result.
-template <bool kDeriv, bool kShade, int TW, int TH, int CHUNK>
+template <bool kDeriv, bool kShade, int TW, int TH, int CHUNK, bool kAll = false>
 __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, uint32_t ty,
                                             const uint32_t* __restrict__ list, uint32_t b, uint32_t e) {
     constexpr int kThreads = TW * TH;
@@ -217,14 +218,14 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
         __syncthreads();
         const uint32_t i = chunk + threadIdx.x;
         if (threadIdx.x < (uint32_t)CHUNK && i < e) {
-            const uint32_t t = list ? list[i] : i;
+            const uint32_t t = kAll ? i : list[i];
             float sgn = 0.0f;
             uint32_t rect = kRectNone;
             float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
             float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f, s2x = 0.f, s2y = 0.f;
             const uint3 vi = idx[t];
             bool binned = vi.x < v.V && vi.y < v.V && vi.z < v.V;
-            if (!list && binned) {
+            if (kAll && binned) {
                 const TriRect tr = triangle_tile_rect(clip, vi, v.W, v.H, vp, TW, TH);
                 binned = tr.x != kNoRect && tx >= (tr.x & 0xffffu) && tx <= (tr.x >> 16) && ty >= (tr.y & 0xffffu) &&
                          ty <= (tr.y >> 16);
@@ -394,6 +395,21 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                 r.z = c0.z * w0 + c1.z * w1 + c2.z * w2 + c3.z * w3;
                 r.w = c0.w * w0 + c1.w * w1 + c2.w * w2 + c3.w * w3;
                 shade.sampled[pix] = r;
+                if (shade.sdiff) {
+                    // texture_grad_uv.hlsl's texel differences (c0 = c00, c1 = c10, c2 = c01, c3 = c11),
+                    // kept for the backward so it does not gather the texels again
+                    float4 du, dv;
+                    du.x = (1.0f - fy) * (c1.x - c0.x) + fy * (c3.x - c2.x);
+                    du.y = (1.0f - fy) * (c1.y - c0.y) + fy * (c3.y - c2.y);
+                    du.z = (1.0f - fy) * (c1.z - c0.z) + fy * (c3.z - c2.z);
+                    du.w = (1.0f - fy) * (c1.w - c0.w) + fy * (c3.w - c2.w);
+                    dv.x = (1.0f - fx) * (c2.x - c0.x) + fx * (c3.x - c1.x);
+                    dv.y = (1.0f - fx) * (c2.y - c0.y) + fx * (c3.y - c1.y);
+                    dv.z = (1.0f - fx) * (c2.z - c0.z) + fx * (c3.z - c1.z);
+                    dv.w = (1.0f - fx) * (c2.w - c0.w) + fx * (c3.w - c1.w);
+                    shade.sdiff[pix * 2] = du;
+                    shade.sdiff[pix * 2 + 1] = dv;
+                }
             }
         }
     }

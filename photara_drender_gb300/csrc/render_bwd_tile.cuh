@@ -92,6 +92,7 @@ struct BackwardView {
     float* g_attr;                // [V][A]
     float* g_uv;                  // [V][2]
     float* g_tex;                 // [th][tw][4]
+    const float4* sdiff;          // [H][W][2] texel differences of the forward's sample, or nullptr
     uint32_t* status;
 };
 
@@ -162,24 +163,35 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
             }
             // texture_grad_uv (fp32)
             if (id != 0) {
-                const float tx = u.x * (float)tw - 0.5f, ty = u.y * (float)th - 0.5f;
-                const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
-                const float fx = tx - floorf(tx), fy = ty - floorf(ty);
-                const int32_t x0 = address_coordinate(bx, tw, mode), x1 = address_coordinate(add1(bx), tw, mode);
-                const int32_t y0 = address_coordinate(by, th, mode), y1 = address_coordinate(add1(by), th, mode);
-                const float4 c00 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x0);
-                const float4 c10 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x1);
-                const float4 c01 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x0);
-                const float4 c11 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x1);
-                const float cs00[4] = {c00.x, c00.y, c00.z, c00.w}, cs10[4] = {c10.x, c10.y, c10.z, c10.w};
-                const float cs01[4] = {c01.x, c01.y, c01.z, c01.w}, cs11[4] = {c11.x, c11.y, c11.z, c11.w};
+                float dxs[4], dys[4];
+                if (v.sdiff) {
+                    // the forward's texel differences: the same values the gathers below compute
+                    const float4 du = v.sdiff[pix * 2], dv = v.sdiff[pix * 2 + 1];
+                    dxs[0] = du.x; dxs[1] = du.y; dxs[2] = du.z; dxs[3] = du.w;
+                    dys[0] = dv.x; dys[1] = dv.y; dys[2] = dv.z; dys[3] = dv.w;
+                } else {
+                    const float tx = u.x * (float)tw - 0.5f, ty = u.y * (float)th - 0.5f;
+                    const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
+                    const float fx = tx - floorf(tx), fy = ty - floorf(ty);
+                    const int32_t x0 = address_coordinate(bx, tw, mode), x1 = address_coordinate(add1(bx), tw, mode);
+                    const int32_t y0 = address_coordinate(by, th, mode), y1 = address_coordinate(add1(by), th, mode);
+                    const float4 c00 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x0);
+                    const float4 c10 = __ldg(tex + (size_t)(uint32_t)y0 * tw + (uint32_t)x1);
+                    const float4 c01 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x0);
+                    const float4 c11 = __ldg(tex + (size_t)(uint32_t)y1 * tw + (uint32_t)x1);
+                    const float cs00[4] = {c00.x, c00.y, c00.z, c00.w}, cs10[4] = {c10.x, c10.y, c10.z, c10.w};
+                    const float cs01[4] = {c01.x, c01.y, c01.z, c01.w}, cs11[4] = {c11.x, c11.y, c11.z, c11.w};
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        dxs[c] = (1.0f - fy) * (cs10[c] - cs00[c]) + fy * (cs11[c] - cs01[c]);
+                        dys[c] = (1.0f - fx) * (cs01[c] - cs00[c]) + fx * (cs11[c] - cs10[c]);
+                    }
+                }
                 const float g4[4] = {gs.x, gs.y, gs.z, gs.w};
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const float dx = (1.0f - fy) * (cs10[c] - cs00[c]) + fy * (cs11[c] - cs01[c]);
-                    const float dy = (1.0f - fx) * (cs01[c] - cs00[c]) + fx * (cs11[c] - cs10[c]);
-                    gux += g4[c] * (dx * (float)tw);
-                    guy += g4[c] * (dy * (float)th);
+                    gux += g4[c] * (dxs[c] * (float)tw);
+                    guy += g4[c] * (dys[c] * (float)th);
                 }
             }
         }

@@ -30,7 +30,7 @@ class RenderArgsC(C.Structure):
         ("barycentric_derivatives", C.c_void_p), ("interpolated", C.c_void_p), ("uv", C.c_void_p),
         ("sampled", C.c_void_p), ("grad_interpolated", C.c_void_p), ("grad_sampled", C.c_void_p),
         ("grad_clip_positions", C.c_void_p), ("grad_attributes", C.c_void_p), ("grad_uv_attributes", C.c_void_p),
-        ("grad_texture", C.c_void_p),
+        ("grad_texture", C.c_void_p), ("sample_differences", C.c_void_p),
     ]
 
 
@@ -40,7 +40,7 @@ class RenderFwdBwd:
 
     def __init__(self, rasterizer: Rasterizer, indices: torch.Tensor, vertex_count: int, views: int, height: int,
                  width: int, attribute_count: int, texture_shape, viewports=None, capacity: Optional[int] = None,
-                 address_mode: int = 0, fused: bool = True):
+                 address_mode: int = 0, fused: bool = True, keep_sample_differences: bool = True):
         self.r = rasterizer
         self.fused = fused
         ctx = rasterizer.context
@@ -72,6 +72,9 @@ class RenderFwdBwd:
         self.grad_uv_attr = torch.empty((vertex_count, 2), **f)
         self.grad_raster = torch.empty((views, height, width, 4), **f)
         self.grad_clip = torch.empty((views, vertex_count, 4), **f)
+        # the forward's texel differences per covered pixel, read by the fused backward instead of
+        # gathering the texels again (32 bytes per pixel)
+        self.sample_diff = torch.empty((views, height, width, 8), **f) if fused and keep_sample_differences else None
 
     def check_capacity(self) -> int:
         """Entry count of the last binning; raises when the tile list overflowed its capacity."""
@@ -95,6 +98,8 @@ class RenderFwdBwd:
             a.grad_interpolated, a.grad_sampled = grad_attr_out.data_ptr(), grad_sampled.data_ptr()
         a.grad_clip_positions, a.grad_attributes = self.grad_clip.data_ptr(), self.grad_attr.data_ptr()
         a.grad_uv_attributes, a.grad_texture = self.grad_uv_attr.data_ptr(), self.grad_tex.data_ptr()
+        if self.sample_diff is not None:
+            a.sample_differences = self.sample_diff.data_ptr()
         return a
 
     def forward(self, clip: torch.Tensor, attrs: torch.Tensor, uv_attrs: torch.Tensor, texture: torch.Tensor,

@@ -202,6 +202,26 @@ def _apply_status(r: Rasterizer, reports) -> None:
             raise IndexError("uv is too large for portable texture addressing")
 
 
+def _cached_viewports(r: Rasterizer, viewport, views: int, w: int, h: int) -> torch.Tensor:
+    """The device viewport rows of render calls, kept per (viewport, views, size) on the rasterizer: an
+    upload from pageable host memory is not allowed inside a CUDA graph capture, so a captured call
+    reuses the rows an earlier call made."""
+    from .rasterizer import _viewports
+
+    try:
+        key = (views, w, h, None if viewport is None else tuple(
+            tuple(float(x) for x in v) if isinstance(v, (list, tuple)) else float(v) for v in viewport))
+    except TypeError:
+        key = None
+    cache = r.__dict__.setdefault("_render_viewports", {})
+    if key is not None and key in cache:
+        return cache[key]
+    vps, _ = _viewports(viewport, views, w, h, r.context.device)
+    if key is not None:
+        cache[key] = vps
+    return vps
+
+
 def check_deferred_errors(rasterizer: Rasterizer) -> None:
     """Waits for every `render(..., deferred_errors=True)` call made on this rasterizer and raises the
     first error the device recorded for them (ValueError / IndexError / OverflowError, as the
@@ -224,7 +244,9 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
     out = dict(raster=torch.empty((views, h, w, 4), **f), deriv=torch.empty((views, h, w, 4), **f),
                interp=torch.empty((views, h, w, attrs.shape[1]), **f) if attrs is not None else None,
                uv=torch.empty((views, h, w, 2), **f) if uv_attrs is not None else None,
-               sampled=torch.empty((views, h, w, 4), **f) if tex is not None else None)
+               sampled=torch.empty((views, h, w, 4), **f) if tex is not None else None,
+               # texel differences of each covered pixel's sample, kept for the backward (32 B per pixel)
+               sdiff=torch.empty((views, h, w, 8), **f) if tex is not None else None)
     offsets = torch.empty(views * tiles + 1, dtype=torch.int32, device=dev)
     _apply_status(r, ctx.poll_status())
     capacity = max(getattr(r, "_render_capacity", 0), 2 * T * views + 1024)
@@ -245,6 +267,7 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
         if tex is not None:
             a.texture, a.texture_width, a.texture_height = tex.data_ptr(), tex.shape[1], tex.shape[0]
             a.address_mode, a.sampled = mode, out["sampled"].data_ptr()
+            a.sample_differences = out["sdiff"].data_ptr()
         a.tile_offsets, a.tile_triangles, a.capacity = offsets.data_ptr(), lst.data_ptr(), capacity
         a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
         a.raster, a.barycentric_derivatives = out["raster"].data_ptr(), out["deriv"].data_ptr()
@@ -280,7 +303,7 @@ class _RenderFunction(torch.autograd.Function):
             clip = (clip if batched else clip.unsqueeze(0)).contiguous()
             idx = indices.detach().to(r.context.device, torch.int32).contiguous()
             h, w = int(resolution[0]), int(resolution[1])
-            vps, _ = _viewports(viewport, clip.shape[0], w, h, r.context.device)
+            vps = _cached_viewports(r, viewport, clip.shape[0], w, h)
             attrs = vertex_attributes.detach().contiguous() if vertex_attributes is not None else None
             uva = vertex_uv.detach().contiguous() if vertex_uv is not None else None
             tex = texture_values.detach().contiguous() if texture_values is not None else None
@@ -292,7 +315,7 @@ class _RenderFunction(torch.autograd.Function):
         # outputs the loss does not use get no gradient (None), not a zero tensor: a zero raster or uv
         # gradient would otherwise run the separate adjoints over every pixel for nothing
         ctx.set_materialize_grads(False)
-        ctx.save_for_backward(clip, idx, attrs, uva, tex, out["raster"], out["uv"])
+        ctx.save_for_backward(clip, idx, attrs, uva, tex, out["raster"], out["uv"], out["sdiff"])
         squeeze = (lambda t: t) if batched else (lambda t: t[0] if t is not None else None)
         result = (squeeze(out["raster"]), squeeze(out["deriv"]), squeeze(out["interp"]), squeeze(out["uv"]),
                   squeeze(out["sampled"]))
@@ -304,7 +327,7 @@ class _RenderFunction(torch.autograd.Function):
         from . import _native
         from .pipeline import RenderArgsC
 
-        clip, idx, attrs, uva, tex, raster, uv_out = ctx.saved_tensors
+        clip, idx, attrs, uva, tex, raster, uv_out, sdiff = ctx.saved_tensors
         r = ctx.r
         unb = (lambda t: t) if ctx.batched else (lambda t: t.unsqueeze(0) if t is not None else None)
         g_raster, g_interp, g_uv, g_sampled = unb(g_raster), unb(g_interp), unb(g_uv), unb(g_sampled)
@@ -336,6 +359,7 @@ class _RenderFunction(torch.autograd.Function):
                 a.texture, a.texture_width, a.texture_height, a.address_mode = (tex.data_ptr(), tex.shape[1],
                                                                                 tex.shape[0], ctx.mode)
                 a.grad_sampled, a.grad_texture = gs.data_ptr(), grad_tex.data_ptr()
+                a.sample_differences = sdiff.data_ptr()
             a.grad_clip_positions, a.status = grad_clip.data_ptr(), r.context.status.data_ptr()
             deferred = ctx.deferred or torch.cuda.is_current_stream_capturing()
             _apply_status(r, r.context.poll_status())
