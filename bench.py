@@ -1187,6 +1187,8 @@ def main():
     ap.add_argument("--skip-refine", action="store_true", help="omit the refine leg")
     ap.add_argument("--skip-c4", action="store_true", help="omit the uneven multi-mesh batch leg")
     ap.add_argument("--skip-precond", action="store_true", help="omit the learned-preconditioner leg")
+    ap.add_argument("--c4-meshes", type=int, default=None, help="override the C4 mesh count (small profiling cases)")
+    ap.add_argument("--refine-steps", type=int, default=None, help="override the refine leg's step count (profiling)")
     args = ap.parse_args()
     if args.views:
         WORKLOAD["views"] = args.views
@@ -1197,6 +1199,12 @@ def main():
     if args.atlas:
         WORKLOAD["name"] = WORKLOAD["name"].replace(f"atlas{WORKLOAD['atlas']}", f"atlas{args.atlas}")
         WORKLOAD["atlas"] = args.atlas
+    if args.c4_meshes:
+        C4["meshes"] = args.c4_meshes
+        C4["name"] = C4["name"].replace("16_meshes", f"{args.c4_meshes}_meshes")
+    if args.refine_steps:
+        REFINE["name"] = REFINE["name"].replace(f"{REFINE['steps']}steps", f"{args.refine_steps}steps")
+        REFINE["steps"] = args.refine_steps
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))

@@ -1,9 +1,14 @@
 """Differentiable texture-atlas rendering and optimisation helpers
 (python/photara_drender/atlas.py:36-257), on the GB300 rasterize/interpolate/texture kernels.
 
-The losses are the reference's research objective written with torch tensor ops; the renderer under
-them is the hand-written CUDA path (photara_drender_gb300.torch). For the fused native refinement
-(one CUDA graph for the whole optimisation) see TextureBaker.refine_texture.
+The losses are the reference's research objective. optimize_texture_atlas runs it on the native refiner
+kernels when the atlas is RGB float32 with clamp addressing and no prior term: per step one view's masked
+Charbonnier gradient (pdr_refine_photometric), the chart-aware TV (pdr_refine_total_variation) and the
+seam term (pdr_refine_seam) into one gradient buffer, then the Adam update with the clamp
+(pdr_refine_adam, torch.optim.Adam's arithmetic), with the loss history read back once at the end.
+Other cases run the same objective as torch tensor ops over the CUDA renderer
+(photara_drender_gb300.torch). For the reference's native refinement (one CUDA graph for the whole
+optimisation) see TextureBaker.refine_texture.
 """
 from __future__ import annotations
 
@@ -12,7 +17,8 @@ from typing import List, NamedTuple, Optional, Sequence, Tuple
 
 import torch
 
-from .rasterizer import Rasterizer
+from . import _native
+from .rasterizer import Rasterizer, _ptr
 from .torch import interpolate, rasterize, render, texture as sample_texture
 
 
@@ -136,6 +142,10 @@ def optimize_texture_atlas(initial_texture: torch.Tensor, clip_positions_by_view
         raise ValueError("viewports and visibility_masks must match the view count")
     if options.steps <= 0 or options.learning_rate <= 0:
         raise ValueError("optimization steps and learning_rate must be positive")
+    if _native_path_applies(initial_texture, target_images, options):
+        return _optimize_native(initial_texture, clip_positions_by_view, indices, vertex_uv, target_images,
+                                rasterizer, viewports, visibility_masks, atlas_valid_mask, chart_ids, seam_uv_pairs,
+                                options)
     parameter = torch.nn.Parameter(initial_texture.detach().clone())
     initial = initial_texture.detach().clone()
     optimizer = torch.optim.Adam([parameter], lr=options.learning_rate)
@@ -178,3 +188,98 @@ def optimize_texture_atlas(initial_texture: torch.Tensor, clip_positions_by_view
             parameter.clamp_(options.clamp_min, options.clamp_max)
         history.append(float(loss.detach().cpu()))
     return parameter.detach(), history
+
+
+def _native_path_applies(initial_texture, target_images, options) -> bool:
+    """The native kernels hold an RGB atlas and sample with clamp addressing; the prior term and other
+    channel counts or address modes take the torch path."""
+    return (isinstance(initial_texture, torch.Tensor) and initial_texture.is_cuda and initial_texture.ndim == 3
+            and initial_texture.shape[2] == 3 and initial_texture.dtype == torch.float32
+            and options.address_mode == "clamp" and options.initial_prior_weight == 0
+            and all(isinstance(t, torch.Tensor) and t.ndim == 3 and t.shape[2] == 3 for t in target_images))
+
+
+def _optimize_native(initial_texture, clip_positions_by_view, indices, vertex_uv, target_images, rasterizer,
+                     viewports, visibility_masks, atlas_valid_mask, chart_ids, seam_uv_pairs, options):
+    """atlas.py:147-257 on the refiner kernels. Per step, as the reference's loop: the round-robin view's
+    masked Charbonnier loss over valid_mask * visibility mask (mean over masked pixels and channels),
+    plus total_variation_weight * the chart-aware TV, plus seam_weight * the seam Charbonnier mean;
+    then Adam (torch.optim.Adam's update with its bias corrections, eps 1e-8) and the clamp."""
+    from .baking import RefineViewC
+
+    ctx = rasterizer.context
+    dev = ctx.device
+    tex = initial_texture.detach().to(dev).contiguous().clone()
+    th, tw, _ = tex.shape
+    grad = torch.zeros((th, tw, 4), dtype=torch.float32, device=dev)  # RGB + pad, cleared by the Adam pass
+    m1, m2 = torch.zeros_like(tex), torch.zeros_like(tex)
+    steps = int(options.steps)
+    losses = torch.zeros((steps, 3), dtype=torch.float32, device=dev)  # photometric, seam, TV per step
+    idx = indices.to(dev)
+    uvv = vertex_uv.to(dev)
+    pairs = None
+    if options.seam_weight != 0 and seam_uv_pairs is not None and seam_uv_pairs.shape[0] > 0:
+        pairs = seam_uv_pairs.to(dev, torch.float32).reshape(-1, 4).contiguous()
+    tv_valid = tv_chart = None
+    tv_scale = 0.0
+    if options.total_variation_weight != 0:
+        valid = (torch.ones((th, tw), dtype=torch.bool, device=dev) if atlas_valid_mask is None
+                 else atlas_valid_mask.to(dev).bool())
+        ph, pv = valid[:, 1:] & valid[:, :-1], valid[1:, :] & valid[:-1, :]
+        if chart_ids is not None:
+            ids = chart_ids.to(dev)
+            ph, pv = ph & (ids[:, 1:] == ids[:, :-1]), pv & (ids[1:, :] == ids[:-1, :])
+            tv_chart = ids.to(torch.int32).contiguous()
+        pair_count = max(int(ph.sum().item() + pv.sum().item()), 1)
+        tv_scale = float(options.total_variation_weight) / (pair_count * 3)
+        tv_valid = valid.to(torch.uint8).contiguous()
+    stream = ctx.stream()
+    cache: dict = {}
+
+    def view_inputs(k):
+        if k in cache:
+            return cache[k]
+        target = target_images[k].to(dev, torch.float32).contiguous()
+        h, w = target.shape[:2]
+        raster, _ = rasterize(clip_positions_by_view[k].detach(), idx, (h, w), rasterizer=rasterizer,
+                              viewport=viewports[k], output_barycentric_derivatives=False)
+        uv = interpolate(uvv.detach(), raster, idx, rasterizer=rasterizer).contiguous()
+        mask = (raster[..., 3] > 0).to(torch.float32)
+        external = visibility_masks[k]
+        if external is not None:
+            mask = mask * (external[..., 0] if external.ndim == 3 else external).to(dev, torch.float32)
+        mask = mask.contiguous()
+        table = (RefineViewC * 1)()
+        table[0].uv, table[0].target, table[0].mask, table[0].pixel_count = (uv.data_ptr(), target.data_ptr(),
+                                                                             mask.data_ptr(), h * w)
+        entry = (torch.frombuffer(bytearray(bytes(table)), dtype=torch.uint8).to(dev), uv, target, mask,
+                 float(mask.double().sum().item()), h * w)
+        # the geometry does not change during the optimisation, so a view's raster, uv and mask are the
+        # same at every visit: kept after the first (the reference re-rasterizes unless
+        # cache_view_rasters is set, with identical results)
+        cache[k] = entry
+        return entry
+
+    lr, b1, b2, eps = float(options.learning_rate), 0.9, 0.999, 1e-8
+    view_count = clip_positions_by_view.shape[0]
+    with ctx.lock:
+        for step in range(steps):
+            table, _uv, _target, _mask, weight, pixels = view_inputs(step % view_count)
+            norm = 1.0 / (max(weight, 1.0) * 3)
+            row = losses[step]
+            _native.call("pdr_refine_photometric", _ptr(tex), tw, th, _ptr(table), 1, pixels, 0, 1,
+                         float(options.photometric_epsilon), norm, _ptr(grad), _ptr(row), stream)
+            if pairs is not None:
+                _native.call("pdr_refine_seam", _ptr(tex), tw, th, _ptr(pairs), pairs.shape[0], 1e-4,
+                             float(options.seam_weight) / (pairs.shape[0] * 3), _ptr(grad), _ptr(row), 1, stream)
+            if tv_valid is not None:
+                with torch.no_grad():
+                    row[2] = options.total_variation_weight * atlas_total_variation(
+                        tex, valid_mask=tv_valid.bool(), chart_ids=tv_chart)
+                _native.call("pdr_refine_total_variation", _ptr(tex), tw, th, _ptr(tv_valid), _ptr(tv_chart), 1e-4,
+                             tv_scale, _ptr(grad), stream)
+            t = step + 1
+            _native.call("pdr_refine_adam", _ptr(tex), _ptr(grad), _ptr(m1), _ptr(m2), tex.numel(), lr, b1, b2, eps,
+                         1.0 - b1 ** t, 1.0 - b2 ** t, float(options.clamp_min), float(options.clamp_max), stream)
+        history = losses.sum(1).tolist()
+    return tex, history

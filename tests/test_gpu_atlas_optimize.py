@@ -1,0 +1,158 @@
+"""optimize_texture_atlas (python/photara_drender/atlas.py:147-257) on the native refiner kernels,
+against a float64 torch restatement of the reference's loop; and one Rasterizer shared by concurrent
+callers (the reference serialises dispatches per context: src/context_internal.hpp:101,
+docs/architecture.md:52-53)."""
+import threading
+
+import numpy as np
+import pytest
+import torch
+
+import photara_drender_gb300 as pdr
+from oracle import api
+from photara_drender_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+def scene(seed=2, views=3, res=(72, 88), atlas=64):
+    rng = np.random.default_rng(seed)
+    pos3, _, uv, idx, chart, remap = S.displaced_sphere(3000, seed=seed, atlas_size=atlas)
+    mats, _ = S.orbit_cameras(views)
+    clip = S.clip_positions(pos3, mats)
+    truth = rng.uniform(0.1, 0.9, size=(atlas, atlas, 3)).astype(np.float32)
+    targets, masks = [], []
+    for k in range(views):
+        r, _ = api.rasterize_forward(clip[k], idx, res, output_derivatives=False)
+        img = api.texture_forward(truth, api.interpolate_forward(uv, idx, r), r)
+        targets.append((img + rng.normal(scale=0.02, size=img.shape)).astype(np.float32))
+        masks.append((rng.uniform(size=res) > 0.1).astype(np.float32) if k == 1 else None)
+    pairs = S.seam_uv_pairs(uv, idx, remap, chart, samples_per_edge=2).astype(np.float32)
+    valid = rng.uniform(size=(atlas, atlas)) < 0.95
+    charts = ((np.arange(atlas)[None, :] // 21) + 4 * (np.arange(atlas)[:, None] // 32)).astype(np.int32)
+    init = np.full((atlas, atlas, 3), 0.5, np.float32)
+    return clip, idx, uv, targets, masks, pairs, valid, charts, init
+
+
+def bilinear64(tex, uv):
+    """Texel-centre bilinear sampling with clamp addressing in float64 (texture_forward.hlsl's formula)."""
+    th, tw, _ = tex.shape
+    tx, ty = uv[..., 0] * tw - 0.5, uv[..., 1] * th - 0.5
+    x0f, y0f = torch.floor(tx), torch.floor(ty)
+    fx, fy = (tx - x0f)[..., None], (ty - y0f)[..., None]
+    x0, y0 = x0f.long(), y0f.long()
+    cx = lambda x: x.clamp(0, tw - 1)  # noqa: E731
+    cy = lambda y: y.clamp(0, th - 1)  # noqa: E731
+    t00, t10 = tex[cy(y0), cx(x0)], tex[cy(y0), cx(x0 + 1)]
+    t01, t11 = tex[cy(y0 + 1), cx(x0)], tex[cy(y0 + 1), cx(x0 + 1)]
+    return t00 * (1 - fx) * (1 - fy) + t10 * fx * (1 - fy) + t01 * (1 - fx) * fy + t11 * fx * fy
+
+
+def reference_loop_f64(init, uvs, rasters, targets, masks, valid, charts, pairs, o):
+    """atlas.py:147-257 in float64 with the rasters and uv of the views fixed (the geometry does not
+    change): masked Charbonnier of the round-robin view + TV + seam, torch.optim.Adam, clamp."""
+    dev = uvs[0].device
+    param = torch.nn.Parameter(torch.tensor(init, dtype=torch.float64, device=dev))
+    opt = torch.optim.Adam([param], lr=o.learning_rate)
+    valid_t = torch.tensor(valid, device=dev)
+    chart_t = torch.tensor(charts, device=dev)
+    pairs_t = torch.tensor(pairs, dtype=torch.float64, device=dev)
+    history = []
+    for step in range(o.steps):
+        opt.zero_grad(set_to_none=True)
+        k = step % len(uvs)
+        covered = (rasters[k][..., 3] > 0).double()[..., None]
+        image = bilinear64(param, uvs[k].double()) * covered
+        mask = covered if masks[k] is None else covered * torch.tensor(masks[k], dtype=torch.float64,
+                                                                        device=dev)[..., None]
+        target = torch.tensor(targets[k], dtype=torch.float64, device=dev)
+        robust = torch.sqrt((image - target).square() + o.photometric_epsilon ** 2)
+        loss = (robust * mask).sum() / (mask.sum().clamp_min(1.0) * 3)
+        loss = loss + o.total_variation_weight * pdr.atlas_total_variation(param, valid_mask=valid_t,
+                                                                           chart_ids=chart_t)
+        colors = bilinear64(param, pairs_t)
+        loss = loss + o.seam_weight * torch.sqrt((colors[:, 0] - colors[:, 1]).square() + 1e-8).mean()
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            param.clamp_(o.clamp_min, o.clamp_max)
+        history.append(float(loss))
+    return param.detach(), history
+
+
+def test_optimize_texture_atlas_native_against_float64_reference_loop():
+    clip, idx, uv, targets, masks, pairs, valid, charts, init = scene()
+    dev = torch.device("cuda", 0)
+    r = pdr.Rasterizer()
+    o = pdr.AtlasOptimizationOptions(steps=12, learning_rate=1e-2, total_variation_weight=1e-2, seam_weight=1e-2)
+    t = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    tex, hist = pdr.optimize_texture_atlas(
+        t(init), t(clip), t(idx.astype(np.int64)), t(uv), [t(x) for x in targets], rasterizer=r,
+        visibility_masks=[None if m is None else t(m) for m in masks], atlas_valid_mask=t(valid),
+        chart_ids=t(charts), seam_uv_pairs=t(pairs), options=o)
+    rasters, uvs = [], []
+    for k in range(clip.shape[0]):
+        raster, _ = r.forward(t(clip[k]), t(idx.astype(np.int32)), targets[k].shape[:2],
+                              output_barycentric_derivatives=False)
+        rasters.append(raster)
+        uvs.append(r.interpolate_forward(t(uv), t(idx.astype(np.int32)), raster))
+    ref, ref_hist = reference_loop_f64(init, uvs, rasters, targets, masks, valid, charts, pairs, o)
+    rel = np.abs(np.asarray(hist) - np.asarray(ref_hist)) / np.abs(np.asarray(ref_hist))
+    diff = (tex.double() - ref).abs()
+    frac = float((diff > 1e-5).double().mean())
+    print(f"\noptimize_texture_atlas, {o.steps} steps: loss history worst relative {rel.max():.2e}; atlas "
+          f"|native - float64| max {float(diff.max()):.2e}, share above 1e-5 {frac:.2e}")
+    assert rel.max() <= 1e-5, (hist, ref_hist)
+    # Adam normalises each texel's step: texels whose gradient cancels to within fp32 rounding may step
+    # differently, but never by more than the step size per step
+    assert frac <= 1e-3 and float(diff.max()) <= 2 * o.learning_rate * o.steps
+    assert hist[-1] < hist[0]
+
+
+def test_shared_rasterizer_concurrent_callers():
+    """Two threads drive one Rasterizer with different views at once: every result equals the same
+    call made alone (the per-context lock serialises the dispatches)."""
+    pos3, idx = S.icosphere(4)
+    mats, _ = S.orbit_cameras(6)
+    clip = S.clip_positions(pos3, mats)
+    rng = np.random.default_rng(3)
+    tex = rng.uniform(size=(64, 64, 4)).astype(np.float32)
+    uva = S.spherical_uv(pos3).astype(np.float32)
+    r = pdr.Rasterizer()
+    dev = torch.device("cuda", 0)
+    t_idx = torch.tensor(idx.astype(np.int32), device=dev)
+    t_tex, t_uv = torch.tensor(tex, device=dev), torch.tensor(uva, device=dev)
+
+    def work(k):
+        raster, deriv = r.forward(torch.tensor(clip[k], device=dev), t_idx, (96, 80))
+        uv = r.interpolate_forward(t_uv, t_idx, raster)
+        img = r.texture_forward(t_tex, uv, raster)
+        gt, gu = r.texture_backward(t_tex, uv, raster, torch.ones_like(img))
+        gp = r.backward(torch.tensor(clip[k], device=dev), t_idx, raster, torch.ones_like(raster))
+        torch.cuda.synchronize()
+        return [x.cpu().numpy() for x in (raster, deriv, uv, img, gu)], [gt.cpu().numpy(), gp.cpu().numpy()]
+
+    alone = [work(k) for k in range(6)]
+    results = [None] * 6
+    errors = []
+
+    def thread(ks):
+        try:
+            for _ in range(3):
+                for k in ks:
+                    results[k] = work(k)
+        except Exception as e:  # pragma: no cover - reported below
+            errors.append(e)
+
+    th = [threading.Thread(target=thread, args=(ks,)) for ks in ((0, 2, 4), (1, 3, 5))]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errors, errors
+    for k in range(6):
+        exact, summed = results[k]
+        for a, b in zip(exact, alone[k][0]):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        for a, b in zip(summed, alone[k][1]):  # atomic sums: equal up to their summation order
+            assert np.allclose(a, b, rtol=1e-5, atol=1e-6 * max(np.abs(b).max(), 1e-30))
