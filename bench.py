@@ -848,12 +848,19 @@ def c5_leg(dev, hbm):
     hit = [runs[f"learned_{b}"] for b in ev["budgets"] if runs[f"learned_{b}"]["loss"] <= target]
     best = min(hit, key=lambda r: r["seconds"]) if hit else None
     plain_hit = [runs[f"plain_{b}"] for b in ev["budgets"] if runs[f"plain_{b}"]["loss"] <= target]
+    # the fair control: the fastest plain schedule (of the same budgets, or the full one) that reaches the target
+    best_plain = min(plain_hit + [runs["plain"]], key=lambda r: r["seconds"])
+    ratio_best = best["seconds"] / best_plain["seconds"] if best else None
     return {"workload": ev["name"], "cpu_baseline": cpu, "plain_loss": runs["plain"]["loss"],
             "plain_seconds": runs["plain"]["seconds"],
             "target_loss": target,
             "learned_seconds_to_target": best["seconds"] if best else None,
             "learned_steps_to_target": best["steps"] if best else None,
             "time_ratio_vs_plain": best["seconds"] / runs["plain"]["seconds"] if best else None,
+            "best_plain_steps_to_target": best_plain["steps"], "best_plain_seconds_to_target": best_plain["seconds"],
+            "time_ratio_vs_best_plain": ratio_best,
+            "target_met": bool(ratio_best is not None and ratio_best <= 0.5),
+            "fell_back": {f"learned_{b}": runs[f"learned_{b}"]["fell_back"] for b in ev["budgets"]},
             "plain_short_schedule_reaches_target": [r["steps"] for r in plain_hit],
             "runs": runs, "training": {"scenes": tr["scenes"], "samples": int(F_.shape[0]),
                                        "collect_seconds": t1 - t0, "fit_seconds": t2 - t1,

@@ -342,21 +342,14 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
     raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, list, b, e);
 }
 
-// The tiles whose lists did not fit the tile-list capacity (or whose offsets overflowed u32), each
-// rasterized from all triangles with the binning rule: the result is the one a sufficient list gives,
-// only slower, so no caller has to wait for the entry count before rasterizing. Launched after
-// raster_forward_kernel with a few CTAs per SM that walk all tiles; when nothing overflowed every CTA
-// only reads offsets.
+// One tile whose list was cut, rasterized from all triangles with the binning rule.
 template <bool kDeriv, bool kShade>
-__global__ void __launch_bounds__(kRasterThreads)
-raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
-                       uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
-                       uint32_t tiles, uint32_t views, const uint32_t* __restrict__ offsets,
-                       unsigned long long capacity, float4* __restrict__ raster, float4* __restrict__ deriv,
-                       ShadeArgs shade, const uint32_t* __restrict__ status) {
-    const size_t P = (size_t)W * H;
-    for (uint32_t seg = blockIdx.x; seg < tiles * views; seg += gridDim.x) {
-        if (!tile_list_cut(offsets[seg], offsets[seg + 1], capacity, status)) continue;  // block-uniform
+__device__ __forceinline__ void raster_cut_tile(const float4* __restrict__ clip_all, uint32_t V,
+                                                const uint3* __restrict__ idx, uint32_t T, uint32_t W, uint32_t H,
+                                                const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
+                                                uint32_t tiles, uint32_t seg, size_t P, float4* __restrict__ raster,
+                                                float4* __restrict__ deriv, const ShadeArgs& shade) {
+    {
         const uint32_t view = seg / tiles, tile = seg % tiles;
         RasterView v;
         v.clip = clip_all + (size_t)view * V;
@@ -377,9 +370,43 @@ raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
             if (shade.sdiff) v.shade.sdiff = shade.sdiff + view * P * 2;
         }
         raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads, true>(v, tile % tcx, tile / tcx, nullptr, 0u, T);
-        __syncthreads();  // the tile routine's shared memory is reused by the next tile
     }
 }
+
+// The tiles whose lists did not fit the tile-list capacity (or whose offsets overflowed u32), each
+// rasterized from all triangles with the binning rule: the result is the one a sufficient list gives,
+// only slower, so no caller has to wait for the entry count before rasterizing. Launched after
+// raster_forward_kernel with a few CTAs per SM that walk all tiles; when nothing overflowed every CTA
+// only reads offsets.
+template <bool kDeriv, bool kShade>
+__global__ void __launch_bounds__(kRasterThreads)
+raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
+                       uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
+                       uint32_t tiles, uint32_t views, const uint32_t* __restrict__ offsets,
+                       unsigned long long capacity, float4* __restrict__ raster, float4* __restrict__ deriv,
+                       ShadeArgs shade, const uint32_t* __restrict__ status) {
+    const size_t P = (size_t)W * H;
+    __shared__ uint32_t cut_tiles[kRasterThreads];
+    __shared__ uint32_t cut_count;
+    const uint32_t total = tiles * views;
+    // each pass checks kRasterThreads tiles at once (one per thread) and rasterizes the cut ones
+    for (uint32_t base = blockIdx.x * kRasterThreads; base < total; base += gridDim.x * kRasterThreads) {
+        if (threadIdx.x == 0) cut_count = 0;
+        __syncthreads();
+        const uint32_t mine = base + threadIdx.x;
+        const bool cut = mine < total && tile_list_cut(offsets[mine], offsets[mine + 1], capacity, status);
+        if (cut) cut_tiles[atomicAdd(&cut_count, 1u)] = mine;
+        __syncthreads();
+        const uint32_t n = cut_count;
+        for (uint32_t i = 0; i < n; ++i) {
+            const uint32_t seg = cut_tiles[i];
+            raster_cut_tile<kDeriv, kShade>(clip_all, V, idx, T, W, H, viewports, cull, tcx, tiles, seg, P, raster,
+                                            deriv, shade);
+            __syncthreads();  // the tile routine's shared memory is reused by the next tile
+        }
+    }
+}
+
 
 // ---- rasterize backward: shaders/rasterize_backward.hlsl:36-158 -------------------------
 // One thread per pixel. A pixel contributes to triangle t exactly when the reference's
