@@ -878,6 +878,7 @@ STAGES = ["bin_tiles", "rasterize_forward+shade", "render_backward"]
 # inside the timed region; when the sources no longer hash to the recorded value the figure belongs to
 # other code and the line reports traffic as null.
 KERNEL_SOURCES = {
+    "bin_tiles": ["raster.cu", "bin_rect.cuh", "pdr_common.cuh"],
     "rasterize_forward+shade": ["raster.cu", "raster_tile.cuh", "bin_rect.cuh", "pdr_common.cuh"],
     "render_backward": ["fused.cu", "render_bwd_tile.cuh", "pdr_common.cuh"],
 }
@@ -1022,11 +1023,12 @@ def run_gpu(args, world, rank, local):
     g_samp = torch.randn((views, H, W, w["channels"]), device=dev, generator=g)
 
     pipe = RenderFwdBwd(r, t_idx, V, views, H, W, w["attributes"], tuple(tex.shape), capacity=4 * T * views)
+    # tile shape and stage depth of the fused forward from the project's autotuner (outputs identical for
+    # every choice); it also sizes the tile list to the measured need
+    tune = pipe.autotune(clip, t_attrs, t_uv, tex)
+    r.render_tile_config = pipe.tile_config
     pipe.step(clip, t_attrs, t_uv, tex, g_attr, g_samp, stream)
     entries = pipe.check_capacity()
-    if entries * 1.25 + 1024 < pipe.capacity:  # shrink the list to the measured need
-        pipe = RenderFwdBwd(r, t_idx, V, views, H, W, w["attributes"], tuple(tex.shape),
-                            capacity=int(entries * 1.25) + 1024)
     for _ in range(args.warmup):
         pipe.step(clip, t_attrs, t_uv, tex, g_attr, g_samp, stream)
     torch.cuda.synchronize(dev)
@@ -1141,6 +1143,8 @@ def run_gpu(args, world, rank, local):
             "config": {"workload": w["name"], "views": views, "resolution": [H, W], "triangles": int(T),
                        "vertices": int(V), "atlas": [w["atlas"], w["atlas"], w["channels"]],
                        "attributes": w["attributes"], "tile_entries": entries,
+                       "tile": list(pipe.tile_config[:2]), "stage_triangles": pipe.tile_config[2],
+                       "autotune_forward_ms": {f"{a}x{b}/{k}": v for (a, b, k), v in tune.items()},
                        "l2": "inputs larger than L2 (6.5 GB of per-view buffers per step)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": pipe.kernels_per_step() * args.steps,

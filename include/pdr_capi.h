@@ -323,10 +323,19 @@ typedef struct {
      * for covered pixels and read by the backward for texture_grad_uv instead of gathering the four
      * texels again. Null: the backward gathers them. Results are identical either way. */
     float* sample_differences;
+    /* Tile shape and triangles staged per pass of the fused render's binning and raster; zeros mean
+     * 16 x 16 and 256 (the reference's tile). Supported: 16x16 with 256 or 128, 16x8 with 128, 32x8
+     * with 256. Outputs are bit-identical for every shape; tile_offsets then has
+     * views * ceil(W / tile_width) * ceil(H / tile_height) + 1 entries. */
+    uint32_t tile_width, tile_height, stage_triangles;
 } pdr_render_args;
 
 PDR_API size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
                                           uint64_t capacity);
+/* pdr_render_workspace_bytes for a tile shape other than 16 x 16. */
+PDR_API size_t pdr_render_workspace_bytes_tiled(uint32_t views, uint32_t triangle_count, uint32_t width,
+                                                uint32_t height, uint64_t capacity, uint32_t tile_width,
+                                                uint32_t tile_height);
 /* Tile binning and one raster launch whose epilogue interpolates both attribute sets and samples the
  * texture for every pixel: the outputs of Rasterizer::forward + interpolate_forward (x2) +
  * texture_forward, bit-identical to the separate calls. The raster does not depend on the order of

@@ -190,10 +190,16 @@ def optimize_texture_atlas(initial_texture: torch.Tensor, clip_positions_by_view
     return parameter.detach(), history
 
 
+# optimize_texture_atlas takes the refiner kernels when they apply; False keeps the torch operations
+# (the reference's own loop over the CUDA renderer) for every call.
+USE_REFINER_KERNELS = True
+
+
 def _native_path_applies(initial_texture, target_images, options) -> bool:
     """The native kernels hold an RGB atlas and sample with clamp addressing; the prior term and other
     channel counts or address modes take the torch path."""
-    return (isinstance(initial_texture, torch.Tensor) and initial_texture.is_cuda and initial_texture.ndim == 3
+    return (USE_REFINER_KERNELS and isinstance(initial_texture, torch.Tensor) and initial_texture.is_cuda
+            and initial_texture.ndim == 3
             and initial_texture.shape[2] == 3 and initial_texture.dtype == torch.float32
             and options.address_mode == "clamp" and options.initial_prior_weight == 0
             and all(isinstance(t, torch.Tensor) and t.ndim == 3 and t.shape[2] == 3 for t in target_images))

@@ -74,7 +74,22 @@ size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint3
     return bins_workspace_bytes(views, triangle_count, width, height, capacity);
 }
 
+size_t pdr_render_workspace_bytes_tiled(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
+                                        uint64_t capacity, uint32_t tile_width, uint32_t tile_height) {
+    if (tile_width == 0 || tile_height == 0) return 0;
+    return bins_workspace_bytes(views, triangle_count, width, height, capacity, tile_width, tile_height);
+}
+
 namespace {
+
+struct TileConfig {
+    uint32_t w, h, k;
+};
+
+TileConfig tile_config(const pdr_render_args* a) {
+    if (a->tile_width == 0 && a->tile_height == 0 && a->stage_triangles == 0) return {16, 16, 256};
+    return {a->tile_width, a->tile_height, a->stage_triangles};
+}
 
 pdr_status check_render_forward(const pdr_render_args* a) {
     if (!a || !a->clip_positions || !a->indices || !a->viewports || !a->raster || !a->tile_offsets ||
@@ -87,7 +102,16 @@ pdr_status check_render_forward(const pdr_render_args* a) {
     if (a->texture && (!a->uv_attributes || !a->uv || !a->sampled || a->texture_width == 0 || a->texture_height == 0 ||
                        a->address_mode > 2))
         return set_error(PDR_INVALID_ARGUMENT, "texture sampling needs uv attributes and uv/sampled outputs");
-    if (a->workspace_bytes < bins_workspace_bytes(a->views, a->triangle_count, a->width, a->height, a->capacity))
+    const TileConfig tc = tile_config(a);
+    if (!raster_config_supported(tc.w, tc.h, tc.k))
+        return set_error(PDR_INVALID_ARGUMENT, "tile shape and stage depth must be 16x16/256, 16x16/128, 16x8/128 or "
+                                               "32x8/256");
+    const uint64_t tiles = (uint64_t)((a->width + tc.w - 1) / tc.w) * ((a->height + tc.h - 1) / tc.h);
+    if (tiles * a->views >= 0x7fffffffull || (uint64_t)a->triangle_count * a->views >= 0x7fffffffull)
+        return set_error(PDR_OVERFLOW, "Rasterization output size overflow");
+    if (a->capacity > 0xffffffffull) return set_error(PDR_OVERFLOW, "tile list capacity exceeds the u32 tile offsets");
+    if (a->workspace_bytes <
+        bins_workspace_bytes(a->views, a->triangle_count, a->width, a->height, a->capacity, tc.w, tc.h))
         return set_error(PDR_INVALID_ARGUMENT, "workspace is smaller than pdr_render_workspace_bytes()");
     return PDR_OK;
 }
@@ -97,10 +121,11 @@ pdr_status check_render_forward(const pdr_render_args* a) {
 pdr_status pdr_render_bin(const pdr_render_args* a, void* stream) {
     const pdr_status st = check_render_forward(a);
     if (st) return st;
+    const TileConfig tc = tile_config(a);
     const cudaError_t err = launch_bin_tiles(a->clip_positions, a->views, a->vertex_count, a->indices,
                                              a->triangle_count, a->width, a->height, a->viewports, a->tile_offsets,
                                              a->tile_triangles, a->capacity, a->workspace, a->status,
-                                             (cudaStream_t)stream, /*sorted=*/false);
+                                             (cudaStream_t)stream, /*sorted=*/false, tc.w, tc.h);
     return set_cuda_error(err, "render_bin");
 }
 
@@ -116,7 +141,7 @@ pdr_status pdr_render_raster(const pdr_render_args* a, void* stream) {
         a->clip_positions, a->views, a->vertex_count, a->indices, a->triangle_count, a->width, a->height,
         a->viewports, a->cull_mode, a->tile_offsets, a->tile_triangles, a->capacity, a->raster,
         a->barycentric_derivatives, (cudaStream_t)stream, (a->attributes || a->uv_attributes) ? &shade : nullptr,
-        a->status);
+        a->status, tile_config(a).w, tile_config(a).h, tile_config(a).k);
     return set_cuda_error(err, "render_raster");
 }
 

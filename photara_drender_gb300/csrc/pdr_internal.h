@@ -21,7 +21,8 @@ inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int num_sms();
 
-size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity);
+size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity,
+                            uint32_t tile_w = 16, uint32_t tile_h = 16);
 
 // Exclusive scan of per-segment counts into CSR offsets (offsets[segs] = total) and the fill cursors;
 // status gets the total and the overflow flag against capacity. block_sums holds scan_block_count(segs).
@@ -31,7 +32,7 @@ size_t scan_block_count(size_t segs);
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
                              unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream,
-                             bool sorted = true);
+                             bool sorted = true, uint32_t tile_w = 16, uint32_t tile_h = 16);
 
 // Optional fused forward epilogue: interpolate attributes and uv for the winning triangle and sample
 // a 4-channel texture at that uv, with the same arithmetic as the separate kernels.
@@ -51,7 +52,11 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
                                   float* raster, float* deriv, cudaStream_t stream,
-                                  const RasterShade* shade = nullptr, const uint32_t* status = nullptr);
+                                  const RasterShade* shade = nullptr, const uint32_t* status = nullptr,
+                                  uint32_t tile_w = 16, uint32_t tile_h = 16, uint32_t chunk = 256);
+// Tile shapes and stage depths the raster kernels are compiled for: 16x16 with 256 or 128 staged
+// triangles, 16x8 with 128, 32x8 with 256.
+bool raster_config_supported(uint32_t tile_w, uint32_t tile_h, uint32_t chunk);
 
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                    uint32_t W, uint32_t H, const float* viewports, const float* raster,

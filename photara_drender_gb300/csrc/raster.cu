@@ -30,14 +30,15 @@ constexpr uint32_t kWindowBits = 8192 * 32;  // id window of the large-tile bitm
 __global__ void bin_count_kernel(const float4* __restrict__ clip, uint32_t V, const uint3* __restrict__ idx,
                                  uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports,
                                  uint32_t tcx, uint32_t tiles, TriRect* __restrict__ rects,
-                                 uint32_t* __restrict__ counts) {
+                                 uint32_t* __restrict__ counts, uint32_t tile_w, uint32_t tile_h) {
     const uint32_t view = blockIdx.y;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = t < T;
     TriRect r{kNoRect, 0};
     if (live) {
         const uint3 vi = idx[t];
-        if (vi.x < V && vi.y < V && vi.z < V) r = triangle_tile_rect(clip + (size_t)view * V, vi, W, H, viewports[view]);
+        if (vi.x < V && vi.y < V && vi.z < V)
+            r = triangle_tile_rect(clip + (size_t)view * V, vi, W, H, viewports[view], tile_w, tile_h);
         rects[(size_t)view * T + t] = r;
     }
     uint32_t* cnt = counts + (size_t)view * tiles;
@@ -296,9 +297,12 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 
 // ---- rasterize forward: shaders/rasterize_forward.hlsl:45-175 ----------------------------
 //
-// One CTA per (view, 16x16 tile) running raster_tile (raster_tile.cuh) over the tile's bin.
+// One CTA per (view, TW x TH tile) running raster_tile (raster_tile.cuh) over the tile's bin, CHUNK
+// triangles staged at a time. pdr_bin_tiles' bins are the reference's 16x16 tiles; the fused render
+// may bin with another tile shape and stage depth (the result is the same: a pixel's candidates are
+// the triangles whose bounding box holds it, whatever the tiles).
 
-constexpr int kRasterThreads = 256;  // one 16x16 tile per CTA, eight 8x4 warp regions
+constexpr int kRasterThreads = 256;  // the default: one 16x16 tile per CTA, eight 8x4 warp regions
 
 // true when tile list [b, e) lost entries to the capacity, or the list offsets overflowed u32
 __device__ __forceinline__ bool tile_list_cut(uint32_t b, uint32_t e, unsigned long long capacity,
@@ -306,8 +310,8 @@ __device__ __forceinline__ bool tile_list_cut(uint32_t b, uint32_t e, unsigned l
     return e > capacity || b > e || (status && status[kStatusTotalHi] != 0u);
 }
 
-template <bool kDeriv, bool kShade>
-__global__ void __launch_bounds__(kRasterThreads)
+template <bool kDeriv, bool kShade, int TW = kTile, int TH = kTile, int CHUNK = kRasterThreads>
+__global__ void __launch_bounds__(TW * TH)
 raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,
@@ -339,11 +343,11 @@ raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uin
     const uint32_t e = offsets[seg + 1];
     // a tile whose list did not fit the capacity is left to raster_overflow_kernel
     if (tile_list_cut(b, e, capacity, status)) return;
-    raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads>(v, tile % tcx, tile / tcx, list, b, e);
+    raster_tile<kDeriv, kShade, TW, TH, CHUNK>(v, tile % tcx, tile / tcx, list, b, e);
 }
 
 // One tile whose list was cut, rasterized from all triangles with the binning rule.
-template <bool kDeriv, bool kShade>
+template <bool kDeriv, bool kShade, int TW, int TH, int CHUNK>
 __device__ __forceinline__ void raster_cut_tile(const float4* __restrict__ clip_all, uint32_t V,
                                                 const uint3* __restrict__ idx, uint32_t T, uint32_t W, uint32_t H,
                                                 const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
@@ -369,7 +373,7 @@ __device__ __forceinline__ void raster_cut_tile(const float4* __restrict__ clip_
             if (shade.sampled) v.shade.sampled = shade.sampled + view * P;
             if (shade.sdiff) v.shade.sdiff = shade.sdiff + view * P * 2;
         }
-        raster_tile<kDeriv, kShade, kTile, kTile, kRasterThreads, true>(v, tile % tcx, tile / tcx, nullptr, 0u, T);
+        raster_tile<kDeriv, kShade, TW, TH, CHUNK, true>(v, tile % tcx, tile / tcx, nullptr, 0u, T);
     }
 }
 
@@ -378,19 +382,20 @@ __device__ __forceinline__ void raster_cut_tile(const float4* __restrict__ clip_
 // only slower, so no caller has to wait for the entry count before rasterizing. Launched after
 // raster_forward_kernel with a few CTAs per SM that walk all tiles; when nothing overflowed every CTA
 // only reads offsets.
-template <bool kDeriv, bool kShade>
-__global__ void __launch_bounds__(kRasterThreads)
+template <bool kDeriv, bool kShade, int TW = kTile, int TH = kTile, int CHUNK = kRasterThreads>
+__global__ void __launch_bounds__(TW * TH)
 raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull, uint32_t tcx,
                        uint32_t tiles, uint32_t views, const uint32_t* __restrict__ offsets,
                        unsigned long long capacity, float4* __restrict__ raster, float4* __restrict__ deriv,
                        ShadeArgs shade, const uint32_t* __restrict__ status) {
     const size_t P = (size_t)W * H;
-    __shared__ uint32_t cut_tiles[kRasterThreads];
+    constexpr uint32_t kThreads = TW * TH;
+    __shared__ uint32_t cut_tiles[kThreads];
     __shared__ uint32_t cut_count;
     const uint32_t total = tiles * views;
-    // each pass checks kRasterThreads tiles at once (one per thread) and rasterizes the cut ones
-    for (uint32_t base = blockIdx.x * kRasterThreads; base < total; base += gridDim.x * kRasterThreads) {
+    // each pass checks kThreads tiles at once (one per thread) and rasterizes the cut ones
+    for (uint32_t base = blockIdx.x * kThreads; base < total; base += gridDim.x * kThreads) {
         if (threadIdx.x == 0) cut_count = 0;
         __syncthreads();
         const uint32_t mine = base + threadIdx.x;
@@ -400,8 +405,8 @@ raster_overflow_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
         const uint32_t n = cut_count;
         for (uint32_t i = 0; i < n; ++i) {
             const uint32_t seg = cut_tiles[i];
-            raster_cut_tile<kDeriv, kShade>(clip_all, V, idx, T, W, H, viewports, cull, tcx, tiles, seg, P, raster,
-                                            deriv, shade);
+            raster_cut_tile<kDeriv, kShade, TW, TH, CHUNK>(clip_all, V, idx, T, W, H, viewports, cull, tcx, tiles,
+                                                           seg, P, raster, deriv, shade);
             __syncthreads();  // the tile routine's shared memory is reused by the next tile
         }
     }
@@ -485,8 +490,9 @@ __global__ void raster_backward_kernel(const float4* __restrict__ clip_all, uint
 
 // ---- host launchers -----------------------------------------------------------------------
 
-size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity) {
-    const size_t tiles = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+size_t bins_workspace_bytes(uint32_t views, uint32_t T, uint32_t W, uint32_t H, unsigned long long capacity,
+                            uint32_t tile_w, uint32_t tile_h) {
+    const size_t tiles = (size_t)((W + tile_w - 1) / tile_w) * ((H + tile_h - 1) / tile_h);
     const size_t segs = tiles * views;
     const size_t nblocks = (segs + 1 + kScanBlock - 1) / kScanBlock;
     size_t bytes = 0;
@@ -513,8 +519,8 @@ size_t scan_block_count(size_t segs) { return (segs + 1 + kScanBlock - 1) / kSca
 cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                              uint32_t W, uint32_t H, const float* viewports, uint32_t* offsets, uint32_t* list,
                              unsigned long long capacity, void* workspace, uint32_t* status, cudaStream_t stream,
-                             bool sorted) {
-    const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
+                             bool sorted, uint32_t tile_w, uint32_t tile_h) {
+    const uint32_t tcx = (W + tile_w - 1) / tile_w, tcy = (H + tile_h - 1) / tile_h;
     const uint32_t tiles = tcx * tcy;
     const size_t segs = (size_t)tiles * views;
     const uint32_t nblocks = (uint32_t)((segs + 1 + kScanBlock - 1) / kScanBlock);
@@ -536,7 +542,8 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
     const dim3 tgrid((T + 255) / 256, views);
     bin_count_kernel<<<tgrid, 256, 0, stream>>>(reinterpret_cast<const float4*>(clip), V,
                                                 reinterpret_cast<const uint3*>(idx), T, W, H,
-                                                reinterpret_cast<const float4*>(viewports), tcx, tiles, rects, counts);
+                                                reinterpret_cast<const float4*>(viewports), tcx, tiles, rects, counts,
+                                                tile_w, tile_h);
     scan_local_kernel<<<nblocks, kScanThreads, 0, stream>>>(counts, (uint32_t)segs, offsets, block_sums);
     scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(block_sums, nblocks, offsets, (uint32_t)segs, status, capacity);
     scan_add_kernel<<<nblocks, kScanThreads, 0, stream>>>(offsets, (uint32_t)segs, block_sums, cursor);
@@ -548,13 +555,53 @@ cudaError_t launch_bin_tiles(const float* clip, uint32_t views, uint32_t V, cons
     return cudaGetLastError();
 }
 
+namespace {
+
+template <int TW, int TH, int CHUNK>
+cudaError_t launch_raster_config(const float4* c4, uint32_t views, uint32_t V, const uint3* i3, uint32_t T, uint32_t W,
+                                 uint32_t H, const float4* v4, uint32_t cull, const uint32_t* offsets,
+                                 const uint32_t* list, unsigned long long capacity, float4* r4, float4* d4,
+                                 const ShadeArgs& sa, bool shade, const uint32_t* status, cudaStream_t stream) {
+    const uint32_t tcx = (W + TW - 1) / TW, tcy = (H + TH - 1) / TH;
+    const uint32_t tiles = tcx * tcy;
+    const dim3 grid(tiles, views);
+    constexpr int kThreads = TW * TH;
+#define PDR_RASTER_MAIN(D, S, DP)                                                                                  \
+    raster_forward_kernel<D, S, TW, TH, CHUNK><<<grid, kThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx,   \
+                                                                              tiles, offsets, list, capacity, r4,  \
+                                                                              DP, sa, status)
+    if (shade) {
+        if (d4) PDR_RASTER_MAIN(true, true, d4); else PDR_RASTER_MAIN(false, true, nullptr);
+    } else {
+        if (d4) PDR_RASTER_MAIN(true, false, d4); else PDR_RASTER_MAIN(false, false, nullptr);
+    }
+#undef PDR_RASTER_MAIN
+    // after the main launch: the tiles it skipped because their lists were cut
+    const unsigned overflow_blocks = (unsigned)std::min<uint64_t>((uint64_t)tiles * views, (uint64_t)num_sms() * 4u);
+#define PDR_RASTER_OVERFLOW(D, S, DP)                                                                              \
+    raster_overflow_kernel<D, S, TW, TH, CHUNK><<<overflow_blocks, kThreads, 0, stream>>>(                         \
+        c4, V, i3, T, W, H, v4, cull, tcx, tiles, views, offsets, capacity, r4, DP, sa, status)
+    if (shade) {
+        if (d4) PDR_RASTER_OVERFLOW(true, true, d4); else PDR_RASTER_OVERFLOW(false, true, nullptr);
+    } else {
+        if (d4) PDR_RASTER_OVERFLOW(true, false, d4); else PDR_RASTER_OVERFLOW(false, false, nullptr);
+    }
+#undef PDR_RASTER_OVERFLOW
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool raster_config_supported(uint32_t tile_w, uint32_t tile_h, uint32_t chunk) {
+    return (tile_w == 16 && tile_h == 16 && (chunk == 256 || chunk == 128)) ||
+           (tile_w == 16 && tile_h == 8 && chunk == 128) || (tile_w == 32 && tile_h == 8 && chunk == 256);
+}
+
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
                                   uint32_t W, uint32_t H, const float* viewports, uint32_t cull,
                                   const uint32_t* offsets, const uint32_t* list, unsigned long long capacity,
                                   float* raster, float* deriv, cudaStream_t stream, const RasterShade* shade,
-                                  const uint32_t* status) {
-    const uint32_t tcx = (W + kTile - 1) / kTile, tcy = (H + kTile - 1) / kTile;
-    const dim3 grid(tcx * tcy, views);
+                                  const uint32_t* status, uint32_t tile_w, uint32_t tile_h, uint32_t chunk) {
     ShadeArgs sa{};
     if (shade) {
         sa.attrs = shade->attrs;
@@ -574,35 +621,20 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
     const float4* v4 = reinterpret_cast<const float4*>(viewports);
     float4* r4 = reinterpret_cast<float4*>(raster);
     float4* d4 = reinterpret_cast<float4*>(deriv);
-    const uint32_t tiles = tcx * tcy;
-    if (shade) {
-        if (deriv)
-            raster_forward_kernel<true, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                  offsets, list, capacity, r4, d4, sa, status);
-        else
-            raster_forward_kernel<false, true><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                   offsets, list, capacity, r4, nullptr, sa, status);
-    } else {
-        if (deriv)
-            raster_forward_kernel<true, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                   offsets, list, capacity, r4, d4, sa, status);
-        else
-            raster_forward_kernel<false, false><<<grid, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, tiles,
-                                                                                    offsets, list, capacity, r4, nullptr, sa, status);
-    }
-    // after the main launch: the tiles it skipped because their lists were cut
-    const unsigned overflow_blocks = (unsigned)std::min<uint64_t>((uint64_t)tiles * views, (uint64_t)num_sms() * 4u);
-#define PDR_RASTER_OVERFLOW(D, S, DP)                                                                              \
-    raster_overflow_kernel<D, S><<<overflow_blocks, kRasterThreads, 0, stream>>>(c4, V, i3, T, W, H, v4, cull, tcx, \
-                                                                                  tiles, views, offsets, capacity, r4, \
-                                                                                  DP, sa, status)
-    if (shade) {
-        if (deriv) PDR_RASTER_OVERFLOW(true, true, d4); else PDR_RASTER_OVERFLOW(false, true, nullptr);
-    } else {
-        if (deriv) PDR_RASTER_OVERFLOW(true, false, d4); else PDR_RASTER_OVERFLOW(false, false, nullptr);
-    }
-#undef PDR_RASTER_OVERFLOW
-    return cudaGetLastError();
+    const bool sh = shade != nullptr;
+    if (tile_w == 16 && tile_h == 16 && chunk == 256)
+        return launch_raster_config<16, 16, 256>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
+                                                 sa, sh, status, stream);
+    if (tile_w == 16 && tile_h == 16 && chunk == 128)
+        return launch_raster_config<16, 16, 128>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
+                                                 sa, sh, status, stream);
+    if (tile_w == 16 && tile_h == 8 && chunk == 128)
+        return launch_raster_config<16, 8, 128>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
+                                                sa, sh, status, stream);
+    if (tile_w == 32 && tile_h == 8 && chunk == 256)
+        return launch_raster_config<32, 8, 256>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
+                                                sa, sh, status, stream);
+    return cudaErrorInvalidValue;
 }
 
 // Gradient through the barycentric pixel derivatives (a capability the reference rejects,

@@ -30,8 +30,14 @@ class RenderArgsC(C.Structure):
         ("barycentric_derivatives", C.c_void_p), ("interpolated", C.c_void_p), ("uv", C.c_void_p),
         ("sampled", C.c_void_p), ("grad_interpolated", C.c_void_p), ("grad_sampled", C.c_void_p),
         ("grad_clip_positions", C.c_void_p), ("grad_attributes", C.c_void_p), ("grad_uv_attributes", C.c_void_p),
-        ("grad_texture", C.c_void_p), ("sample_differences", C.c_void_p),
+        ("grad_texture", C.c_void_p), ("sample_differences", C.c_void_p), ("tile_width", C.c_uint32),
+        ("tile_height", C.c_uint32), ("stage_triangles", C.c_uint32),
     ]
+
+
+# Tile shapes and stage depths of the fused render (pdr_render_args.tile_width / tile_height /
+# stage_triangles): the raster kernels are compiled for these.
+TILE_CONFIGS = ((16, 16, 256), (16, 16, 128), (16, 8, 128), (32, 8, 256))
 
 
 class RenderFwdBwd:
@@ -40,7 +46,8 @@ class RenderFwdBwd:
 
     def __init__(self, rasterizer: Rasterizer, indices: torch.Tensor, vertex_count: int, views: int, height: int,
                  width: int, attribute_count: int, texture_shape, viewports=None, capacity: Optional[int] = None,
-                 address_mode: int = 0, fused: bool = True, keep_sample_differences: bool = True):
+                 address_mode: int = 0, fused: bool = True, keep_sample_differences: bool = True,
+                 tile_config=(16, 16, 256)):
         self.r = rasterizer
         self.fused = fused
         ctx = rasterizer.context
@@ -51,13 +58,8 @@ class RenderFwdBwd:
         self.th, self.tw, self.C = texture_shape
         self.mode = address_mode
         self.vps, _ = _viewports(viewports, views, width, height, dev)
-        tiles = ((width + TILE - 1) // TILE) * ((height + TILE - 1) // TILE)
-        self.offsets = torch.empty(views * tiles + 1, dtype=torch.int32, device=dev)
-        self.capacity = int(capacity) if capacity else 4 * self.T * views + 1024
-        self.list = torch.empty(self.capacity, dtype=torch.int32, device=dev)
-        self.ws_bytes = _native.lib().pdr_bin_tiles_workspace_bytes(views, self.T, width, height, self.capacity)
-        self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=dev)
         self.status = torch.zeros(_native.STATUS_WORDS, dtype=torch.int32, device=dev)
+        self.set_tile_config(tile_config if fused else (16, 16, 256), capacity)
         f = dict(dtype=torch.float32, device=dev)
         P = height * width
         self.P = P
@@ -75,6 +77,52 @@ class RenderFwdBwd:
         # the forward's texel differences per covered pixel, read by the fused backward instead of
         # gathering the texels again (32 bytes per pixel)
         self.sample_diff = torch.empty((views, height, width, 8), **f) if fused and keep_sample_differences else None
+
+    def set_tile_config(self, config, capacity: Optional[int] = None) -> None:
+        """Tile shape and stage depth of the fused binning and raster (one of TILE_CONFIGS), with the
+        tile list, offsets and workspace they need."""
+        config = tuple(int(x) for x in config)
+        if config not in TILE_CONFIGS:
+            raise ValueError(f"tile configuration must be one of {TILE_CONFIGS}")
+        dev = self.r.context.device
+        tw, th, _ = config
+        self.tile_config = config
+        tiles = ((self.W + tw - 1) // tw) * ((self.H + th - 1) // th)
+        self.offsets = torch.empty(self.views * tiles + 1, dtype=torch.int32, device=dev)
+        self.capacity = int(capacity) if capacity else 4 * self.T * self.views + 1024
+        self.list = torch.empty(self.capacity, dtype=torch.int32, device=dev)
+        self.ws_bytes = _native.lib().pdr_render_workspace_bytes_tiled(self.views, self.T, self.W, self.H,
+                                                                       self.capacity, tw, th)
+        self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=dev)
+
+    def autotune(self, clip, attrs, uv_attrs, texture, reps: int = 5, configs=TILE_CONFIGS):
+        """Times the fused forward (binning + raster) of these inputs for every tile configuration, keeps the
+        fastest and sizes its tile list to the measured entry count (+25%). Returns {config: median ms}.
+        Outputs are the same for every configuration."""
+        if not self.fused:
+            return {}
+        dev = self.r.context.device
+        stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        times, needs = {}, {}
+        for cfg in configs:
+            self.set_tile_config(cfg)
+            self.forward(clip, attrs, uv_attrs, texture, stream)
+            entries = self.check_capacity()
+            needs[cfg] = int(entries * 1.25) + 1024
+            self.set_tile_config(cfg, needs[cfg])
+            samples = []
+            for i in range(reps + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self.forward(clip, attrs, uv_attrs, texture, stream)
+                e1.record()
+                torch.cuda.synchronize(dev)
+                if i:
+                    samples.append(e0.elapsed_time(e1))
+            times[cfg] = sorted(samples)[len(samples) // 2]
+        best = min(times, key=times.get)
+        self.set_tile_config(best, needs[best])
+        return times
 
     def check_capacity(self) -> int:
         """Entry count of the last binning; raises when the tile list overflowed its capacity."""
@@ -100,6 +148,7 @@ class RenderFwdBwd:
         a.grad_uv_attributes, a.grad_texture = self.grad_uv_attr.data_ptr(), self.grad_tex.data_ptr()
         if self.sample_diff is not None:
             a.sample_differences = self.sample_diff.data_ptr()
+        a.tile_width, a.tile_height, a.stage_triangles = self.tile_config
         return a
 
     def forward(self, clip: torch.Tensor, attrs: torch.Tensor, uv_attrs: torch.Tensor, texture: torch.Tensor,

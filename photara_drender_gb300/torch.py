@@ -239,7 +239,10 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
     dev = ctx.device
     views, V = clip.shape[0], clip.shape[1]
     T = idx.shape[0]
-    tiles = ((w + TILE - 1) // TILE) * ((h + TILE - 1) // TILE)
+    # tile shape and stage depth of the fused binning and raster (pipeline.TILE_CONFIGS; outputs do not
+    # depend on it): the rasterizer's render_tile_config, e.g. one RenderFwdBwd.autotune picked
+    tw_, th_, stage = getattr(r, "render_tile_config", (TILE, TILE, 256))
+    tiles = ((w + tw_ - 1) // tw_) * ((h + th_ - 1) // th_)
     f = dict(dtype=torch.float32, device=dev)
     out = dict(raster=torch.empty((views, h, w, 4), **f), deriv=torch.empty((views, h, w, 4), **f),
                interp=torch.empty((views, h, w, attrs.shape[1]), **f) if attrs is not None else None,
@@ -253,7 +256,7 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
     L = _native.lib()
     for _ in range(1 if deferred else 3):
         lst = torch.empty(capacity, dtype=torch.int32, device=dev)
-        ws_bytes = L.pdr_render_workspace_bytes(views, T, w, h, capacity)
+        ws_bytes = L.pdr_render_workspace_bytes_tiled(views, T, w, h, capacity, tw_, th_)
         ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
         ctx.status.zero_()
         a = RenderArgsC()
@@ -271,6 +274,7 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
         a.tile_offsets, a.tile_triangles, a.capacity = offsets.data_ptr(), lst.data_ptr(), capacity
         a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
         a.raster, a.barycentric_derivatives = out["raster"].data_ptr(), out["deriv"].data_ptr()
+        a.tile_width, a.tile_height, a.stage_triangles = tw_, th_, stage
         _native.check(L.pdr_render_forward(C.addressof(a), ctx.stream()))
         if deferred:
             # No wait: a tile whose list overflowed the capacity is rasterized from all triangles with the

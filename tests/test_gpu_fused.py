@@ -161,3 +161,43 @@ def test_gradient_sums_at_scale(atlas):
     err_a = ((p.grad_attr.double().sum(0) - ref_a).abs() / abs_a).max().item()
     assert cov.sum().item() > 1e6
     assert err_t <= 1e-5 and err_a <= 1e-5, (err_t, err_a)
+
+
+def test_tile_configurations_give_identical_outputs():
+    """The fused forward with every compiled tile shape and stage depth (pipeline.TILE_CONFIGS) gives the
+    outputs of the default 16x16/256 bins bit for bit, also when a configuration's tile list overflows;
+    the autotuner picks one of them and sizes its list."""
+    from photara_drender_gb300 import Rasterizer
+    from photara_drender_gb300.pipeline import TILE_CONFIGS, RenderFwdBwd
+
+    rng = np.random.default_rng(12)
+    pos3, idx = S.icosphere(5)
+    mats, _ = S.orbit_cameras(3)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)  # noqa: E731
+    clip, V = t(S.clip_positions(pos3, mats)), pos3.shape[0]
+    attrs, uva = t(rng.uniform(size=(V, 3))), t(S.spherical_uv(pos3))
+    tex = t(rng.uniform(size=(128, 96, 4)))
+    H, W = 150, 131  # ragged: partial tiles in both directions for every shape
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    r = Rasterizer(0)
+    outs = {}
+    for cfg in TILE_CONFIGS:
+        for cap in (None, 2000):
+            p = RenderFwdBwd(r, torch.tensor(idx.astype(np.int32)), V, 3, H, W, 3, tuple(tex.shape), capacity=cap,
+                             tile_config=cfg, viewports=[None, (5.0, -3.0, 120.0, 140.0), None])
+            p.forward(clip, attrs, uva, tex, stream)
+            torch.cuda.synchronize()
+            outs[(cfg, cap)] = [getattr(p, k).clone() for k in ("raster", "deriv", "attr_out", "uv", "sampled")]
+            if cap:
+                assert int(p.status[2]) == 1  # the small list overflowed
+    ref = outs[((16, 16, 256), None)]
+    for key, got in outs.items():
+        for a, b in zip(got, ref):
+            assert torch.equal(a.view(torch.int32), b.view(torch.int32)), key
+    p = RenderFwdBwd(r, torch.tensor(idx.astype(np.int32)), V, 3, H, W, 3, tuple(tex.shape))
+    times = p.autotune(clip, attrs, uva, tex, reps=2)
+    assert set(times) == set(TILE_CONFIGS) and p.tile_config in TILE_CONFIGS
+    p.forward(clip, attrs, uva, tex, stream)
+    torch.cuda.synchronize()
+    assert p.check_capacity() > 0 and torch.equal(p.raster.view(torch.int32), ref[0].view(torch.int32))
