@@ -1025,7 +1025,15 @@ def run_gpu(args, world, rank, local):
     pipe = RenderFwdBwd(r, t_idx, V, views, H, W, w["attributes"], tuple(tex.shape), capacity=4 * T * views)
     # tile shape and stage depth of the fused forward from the project's autotuner (outputs identical for
     # every choice); it also sizes the tile list to the measured need
-    tune = pipe.autotune(clip, t_attrs, t_uv, tex)
+    if args.tile:
+        tw_th, k = args.tile.split("/")
+        cfg = tuple(int(x) for x in tw_th.split("x")) + (int(k),)
+        pipe.set_tile_config(cfg)
+        tune = {}
+        pipe.step(clip, t_attrs, t_uv, tex, g_attr, g_samp, stream)
+        pipe.set_tile_config(cfg, int(pipe.check_capacity() * 1.25) + 1024)
+    else:
+        tune = pipe.autotune(clip, t_attrs, t_uv, tex)
     r.render_tile_config = pipe.tile_config
     pipe.step(clip, t_attrs, t_uv, tex, g_attr, g_samp, stream)
     entries = pipe.check_capacity()
@@ -1199,6 +1207,7 @@ def main():
     ap.add_argument("--skip-c4", action="store_true", help="omit the uneven multi-mesh batch leg")
     ap.add_argument("--skip-precond", action="store_true", help="omit the learned-preconditioner leg")
     ap.add_argument("--c4-meshes", type=int, default=None, help="override the C4 mesh count (small profiling cases)")
+    ap.add_argument("--tile", default=None, help="fused tile shape and stage depth, e.g. 16x8/128 (default: autotune)")
     ap.add_argument("--refine-steps", type=int, default=None, help="override the refine leg's step count (profiling)")
     args = ap.parse_args()
     if args.views:
