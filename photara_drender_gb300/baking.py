@@ -149,20 +149,45 @@ class TextureBaker:
 
     # -- helpers ---------------------------------------------------------------------------------
     def _rasters(self, clip: torch.Tensor, idx: torch.Tensor, sizes: List[Tuple[int, int]], viewports):
-        """Rasterizes every view (no derivatives), batching views of equal size into one launch."""
+        """Rasterizes every view (no derivatives), batching views of equal size into one launch. The bins
+        are the fused render's (unsorted: the raster does not depend on the order of a tile's triangles)
+        and nothing waits for their entry count: tiles whose lists overflow the capacity are rasterized
+        from all triangles with the binning rule, and the count sizes the capacity of later calls."""
+        from .pipeline import RenderArgsC
+
         out: List[Optional[torch.Tensor]] = [None] * len(sizes)
         groups = {}
         for k, s in enumerate(sizes):
             groups.setdefault(s, []).append(k)
         ctx = self.context
-        V = clip.shape[1]
+        V, T = clip.shape[1], idx.shape[0]
+        L = _native.lib()
+        for kind, st in ctx.poll_status(kinds=("bake_raster",)):
+            if kind == "bake_raster":
+                self._raster_capacity = max(getattr(self, "_raster_capacity", 0),
+                                            (st[_native.STATUS_TILE_ENTRIES] & 0xFFFFFFFF) * 9 // 8 + 1024)
         for (h, w), ks in groups.items():
+            n = len(ks)
             sub = clip[ks].contiguous()
-            vps, _ = _viewports([viewports[k] for k in ks], len(ks), w, h, ctx.device)
-            offsets, lst, capacity, _ = self.rasterizer._bin(sub, idx, w, h, vps)
-            raster = torch.empty((len(ks), h, w, 4), dtype=torch.float32, device=ctx.device)
-            _native.call("pdr_rasterize_forward", _ptr(sub), len(ks), V, _ptr(idx), idx.shape[0], w, h, _ptr(vps), 0,
-                         _ptr(offsets), _ptr(lst), capacity, _ptr(raster), None, ctx.stream())
+            vps, _ = _viewports([viewports[k] for k in ks], n, w, h, ctx.device)
+            tiles = ((w + 15) // 16) * ((h + 15) // 16)
+            # four tiles per triangle plus one entry per tile covers meshes of small triangles; a larger need
+            # costs time on the first call only (the count then sizes later calls)
+            capacity = max(getattr(self, "_raster_capacity", 0), 4 * T * n + tiles * n + 1024)
+            offsets = torch.empty(n * tiles + 1, dtype=torch.int32, device=ctx.device)
+            lst = torch.empty(capacity, dtype=torch.int32, device=ctx.device)
+            ws_bytes = L.pdr_render_workspace_bytes(n, T, w, h, capacity)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=ctx.device)
+            raster = torch.empty((n, h, w, 4), dtype=torch.float32, device=ctx.device)
+            a = RenderArgsC()
+            a.clip_positions, a.views, a.vertex_count = sub.data_ptr(), n, V
+            a.indices, a.triangle_count, a.width, a.height = idx.data_ptr(), T, w, h
+            a.viewports, a.raster = vps.data_ptr(), raster.data_ptr()
+            a.tile_offsets, a.tile_triangles, a.capacity = offsets.data_ptr(), lst.data_ptr(), capacity
+            a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
+            ctx.status.zero_()
+            _native.check(L.pdr_render_forward(C.addressof(a), ctx.stream()))
+            ctx.defer_status("bake_raster")
             for j, k in enumerate(ks):
                 out[k] = raster[j]
         return out

@@ -19,20 +19,36 @@ namespace {
 
 __device__ __forceinline__ float lerp_hlsl(float x, float y, float s) { return x * (1.0f - s) + y * s; }
 
-__device__ __forceinline__ float load_channel(const pdr_projection_view& v, int32_t cx, int32_t cy, uint32_t ch) {
-    cx = clampi(cx, 0, (int32_t)v.width - 1);
-    cy = clampi(cy, 0, (int32_t)v.height - 1);
-    return __ldg(v.image + ((size_t)(uint32_t)cy * v.width + (uint32_t)cx) * v.channel_count + ch);
-}
+// project_texture.hlsl:46-56: the bilinear photo sample with clamped taps, for channels 0..2 (and 3 when
+// the image has four). The tap positions and weights are the same for every channel, so they are
+// computed once and each tap's channels are read together.
+struct PhotoSample {
+    float c0, c1, c2, alpha;
+};
 
-// project_texture.hlsl:46-56
-__device__ __forceinline__ float sample_photo(const pdr_projection_view& v, float ppx, float ppy, uint32_t ch) {
+__device__ __forceinline__ PhotoSample sample_photo_rgba(const pdr_projection_view& v, float ppx, float ppy) {
     const float tx = ppx - 0.5f, ty = ppy - 0.5f;
     const int32_t bx = f2i_sat(floorf(tx)), by = f2i_sat(floorf(ty));
     const float fx = tx - floorf(tx), fy = ty - floorf(ty);
-    const float v00 = load_channel(v, bx, by, ch), v10 = load_channel(v, add1(bx), by, ch);
-    const float v01 = load_channel(v, bx, add1(by), ch), v11 = load_channel(v, add1(bx), add1(by), ch);
-    return lerp_hlsl(lerp_hlsl(v00, v10, fx), lerp_hlsl(v01, v11, fx), fy);
+    const int32_t w = (int32_t)v.width - 1, h = (int32_t)v.height - 1;
+    const uint32_t x0 = (uint32_t)clampi(bx, 0, w), x1 = (uint32_t)clampi(add1(bx), 0, w);
+    const uint32_t y0 = (uint32_t)clampi(by, 0, h), y1 = (uint32_t)clampi(add1(by), 0, h);
+    const uint32_t C = v.channel_count;
+    const float* img = v.image;
+    const size_t t00 = ((size_t)y0 * v.width + x0) * C, t10 = ((size_t)y0 * v.width + x1) * C;
+    const size_t t01 = ((size_t)y1 * v.width + x0) * C, t11 = ((size_t)y1 * v.width + x1) * C;
+    float r[4];
+#pragma unroll
+    for (uint32_t ch = 0; ch < 4; ++ch) {
+        if (ch == 3 && C != 4) {
+            r[3] = 1.0f;
+            break;
+        }
+        const float v00 = __ldg(img + t00 + ch), v10 = __ldg(img + t10 + ch);
+        const float v01 = __ldg(img + t01 + ch), v11 = __ldg(img + t11 + ch);
+        r[ch] = lerp_hlsl(lerp_hlsl(v00, v10, fx), lerp_hlsl(v01, v11, fx), fy);
+    }
+    return {r[0], r[1], r[2], r[3]};
 }
 
 // project_texture.hlsl:58-74, with the host-side mask floor of texture_baker.cpp:283-292
@@ -127,9 +143,8 @@ __global__ void project_views_kernel(const float* __restrict__ apos, const float
             else if (visibility_mode == 1) vis *= shadow_visibility(v, ppx, ppy, ndz, (int32_t)pcf_radius);
             if (v.has_mask) vis *= clamp_hlsl(sample_mask(v, ppx, ppy, v.mask_floor), 0.0f, 1.0f);
             if (vis <= 0.0f) continue;
-            const float c0 = sample_photo(v, ppx, ppy, 0), c1 = sample_photo(v, ppx, ppy, 1);
-            const float c2 = sample_photo(v, ppx, ppy, 2);
-            const float alpha = v.channel_count == 4 ? sample_photo(v, ppx, ppy, 3) : 1.0f;
+            const PhotoSample ps = sample_photo_rgba(v, ppx, ppy);
+            const float c0 = ps.c0, c1 = ps.c1, c2 = ps.c2, alpha = ps.alpha;
             if (blend_mode == 2) {
                 const float dist = fmaxf(vl, 1e-6f);
                 const float footprint = cosv / (dist * dist);

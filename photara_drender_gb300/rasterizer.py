@@ -108,17 +108,22 @@ class Context:
         ev.record(torch.cuda.current_stream(self.device))
         self._pending.append((ev, buf, kind))
 
-    def poll_status(self, wait: bool = False):
+    def poll_status(self, wait: bool = False, kinds=None):
         """[(kind, status words)] of the queued copies whose work has finished (all of them when `wait`),
-        oldest first."""
+        oldest first; with `kinds`, only copies of those kinds are taken (the others stay queued)."""
         done = []
         if torch.cuda.is_current_stream_capturing():  # no event queries while a capture is recording
             return done
-        while self._pending and (wait or self._pending[0][0].query()):
-            ev, buf, kind = self._pending.pop(0)
-            ev.synchronize()
-            done.append((kind, [int(x) for x in buf.tolist()]))
-            self._spare.append(buf)
+        keep = []
+        for entry in self._pending:
+            ev, buf, kind = entry
+            if (kinds is None or kind in kinds) and (wait or ev.query()):
+                ev.synchronize()
+                done.append((kind, [int(x) for x in buf.tolist()]))
+                self._spare.append(buf)
+            else:
+                keep.append(entry)
+        self._pending = keep
         return done
 
 

@@ -227,7 +227,8 @@ def check_deferred_errors(rasterizer: Rasterizer) -> None:
     first error the device recorded for them (ValueError / IndexError / OverflowError, as the
     synchronous path raises at once)."""
     with rasterizer.context.lock:
-        _apply_status(rasterizer, rasterizer.context.poll_status(wait=True))
+        _apply_status(rasterizer, rasterizer.context.poll_status(wait=True, kinds=("render_forward",
+                                                                                   "render_backward")))
 
 
 def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, cull, mode, deferred=False):
@@ -251,7 +252,7 @@ def _render_forward(r: Rasterizer, clip, idx, h, w, attrs, uv_attrs, tex, vps, c
                # texel differences of each covered pixel's sample, kept for the backward (32 B per pixel)
                sdiff=torch.empty((views, h, w, 8), **f) if tex is not None else None)
     offsets = torch.empty(views * tiles + 1, dtype=torch.int32, device=dev)
-    _apply_status(r, ctx.poll_status())
+    _apply_status(r, ctx.poll_status(kinds=("render_forward", "render_backward")))
     capacity = max(getattr(r, "_render_capacity", 0), 2 * T * views + 1024)
     L = _native.lib()
     for _ in range(1 if deferred else 3):
@@ -366,7 +367,7 @@ class _RenderFunction(torch.autograd.Function):
                 a.sample_differences = sdiff.data_ptr()
             a.grad_clip_positions, a.status = grad_clip.data_ptr(), r.context.status.data_ptr()
             deferred = ctx.deferred or torch.cuda.is_current_stream_capturing()
-            _apply_status(r, r.context.poll_status())
+            _apply_status(r, r.context.poll_status(kinds=("render_forward", "render_backward")))
             r.context.status.zero_()
             _native.check(_native.lib().pdr_render_backward(C.addressof(a), r.context.stream()))
             if deferred:

@@ -195,7 +195,8 @@ def test_tile_configurations_give_identical_outputs():
     for key, got in outs.items():
         for a, b in zip(got, ref):
             assert torch.equal(a.view(torch.int32), b.view(torch.int32)), key
-    p = RenderFwdBwd(r, torch.tensor(idx.astype(np.int32)), V, 3, H, W, 3, tuple(tex.shape))
+    p = RenderFwdBwd(r, torch.tensor(idx.astype(np.int32)), V, 3, H, W, 3, tuple(tex.shape),
+                     viewports=[None, (5.0, -3.0, 120.0, 140.0), None])
     times = p.autotune(clip, attrs, uva, tex, reps=2)
     assert set(times) == set(TILE_CONFIGS) and p.tile_config in TILE_CONFIGS
     p.forward(clip, attrs, uva, tex, stream)
