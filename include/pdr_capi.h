@@ -234,6 +234,12 @@ typedef struct {
     uint32_t seam_polish_steps;
     float seam_learning_rate, seam_epsilon;
     float tv_scale, tv_epsilon;
+    /* Optional second atlas [height][width][3], 16-byte aligned. With the total variation on, plain
+     * refinement then alternates the texture between `texture` and this buffer, so each step's TV
+     * gradient (which needs the neighbours' values from before the step) and its Adam update run as one
+     * pass over the atlas instead of two. Results are bit-identical and end in `texture`. Null keeps the
+     * separate TV pass. */
+    float* texture_scratch;
 } pdr_refine_options;
 
 /* texture_refiner.cpp:228-242 for one view: target [P][3] and mask [P] from the image and raster. */

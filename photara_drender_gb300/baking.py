@@ -71,7 +71,7 @@ class RefineOptionsC(C.Structure):
         ("adam_beta1", C.c_float), ("adam_beta2", C.c_float), ("adam_epsilon", C.c_float),
         ("clamp_min", C.c_float), ("clamp_max", C.c_float), ("seam_polish_steps", C.c_uint32),
         ("seam_learning_rate", C.c_float), ("seam_epsilon", C.c_float), ("tv_scale", C.c_float),
-        ("tv_epsilon", C.c_float),
+        ("tv_epsilon", C.c_float), ("texture_scratch", C.c_void_p),
     ]
 
 
@@ -517,6 +517,10 @@ class TextureBaker:
         loss = torch.empty(int(steps) + seam_steps, dtype=torch.float32, device=ctx.device)
         n = len(st.weights)
         vw = (C.c_double * n)(*st.weights)
+        # a second atlas buffer lets the plain refinement run each step's TV gradient and Adam update as one
+        # pass (bit-identical; the result ends in tex)
+        scratch = torch.empty_like(tex) if precond is None and float(o.tv_scale) > 0.0 else None
+        o.texture_scratch = scratch.data_ptr() if scratch is not None else None
         if precond is None:
             _native.call("pdr_refine_run", C.addressof(o), _ptr(st.table_dev), n, C.addressof(vw), st.max_pixels,
                          _ptr(pairs), npairs, _ptr(st.tv_valid), _ptr(st.tv_chart), _ptr(tex), _ptr(grad), _ptr(m1),

@@ -54,7 +54,28 @@ pdr_status enqueue_refine(const pdr_refine_options* o, const pdr_refine_view* vi
     chk(cudaMemsetAsync(m1, 0, n * sizeof(float), stream));
     chk(cudaMemsetAsync(m2, 0, n * sizeof(float), stream));
     if (pc) chk(cudaMemsetAsync(pc->fallback, 0, sizeof(uint32_t), stream));
-    for (uint32_t step = 0; step < o->steps && err == cudaSuccess; ++step) {
+    // plain refinement with TV and a second atlas buffer: TV + Adam in one pass, the texture alternating
+    // between the two buffers (the one read this step, the one written)
+    const bool fused_tv = !pc && o->tv_scale > 0.0f && tv_valid && o->texture_scratch;
+    float* cur = tex;
+    float* other = fused_tv ? o->texture_scratch : nullptr;
+    for (uint32_t step = 0; fused_tv && step < o->steps && err == cudaSuccess; ++step) {
+        double bvw = 0.0;
+        for (uint32_t b = 0; b < o->batch_size; ++b) bvw += valid_weights[((size_t)step * o->batch_size + b) % nviews];
+        const float norm = bvw > 0.0 ? static_cast<float>(1.0 / (bvw * 3.0)) : 0.0f;
+        chk(launch_photometric(cur, o->width, o->height, views, nviews, max_pixels, step, o->batch_size,
+                               o->photometric_epsilon, norm, grad, loss, stream));
+        float lr, bc1, bc2;
+        refine_schedule(o, step, &lr, &bc1, &bc2);
+        chk(launch_adam_tv(cur, other, grad, m1, m2, o->width, o->height, tv_valid, tv_chart, o->tv_epsilon,
+                           o->tv_scale, lr, o->adam_beta1, o->adam_beta2, o->adam_epsilon, bc1, bc2, o->clamp_min,
+                           o->clamp_max, stream));
+        float* t = cur;
+        cur = other;
+        other = t;
+    }
+    if (fused_tv && cur != tex) chk(cudaMemcpyAsync(tex, cur, n * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    for (uint32_t step = 0; !fused_tv && step < o->steps && err == cudaSuccess; ++step) {
         if (pc && step % pc->refresh_interval == 0) {
             // learned multipliers from the state after `step` updates (moments corrected for that count)
             const uint32_t K = pc->refresh_interval;
@@ -110,8 +131,11 @@ pdr_status check_refine_run(const pdr_refine_options* o, const pdr_refine_view* 
         return fail(PDR_INVALID_ARGUMENT, "texture refinement needs at least one view");
     if (max_pixels > 0xffffffffull) return fail(PDR_INVALID_ARGUMENT, "texture refinement image or mask has an invalid shape");
     if (!tex || !grad || !m1 || !m2 || !loss) return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers are required");
-    if (!aligned(tex, 16) || !aligned(grad, 16) || !aligned(m1, 16) || !aligned(m2, 16))
+    if (!aligned(tex, 16) || !aligned(grad, 16) || !aligned(m1, 16) || !aligned(m2, 16) ||
+        !aligned(o->texture_scratch, 16))
         return fail(PDR_INVALID_ARGUMENT, "texture refinement buffers must be 16-byte aligned");
+    if (o->texture_scratch && (o->texture_scratch == tex || o->texture_scratch == m1 || o->texture_scratch == m2))
+        return fail(PDR_INVALID_ARGUMENT, "texture_scratch must be a buffer of its own");
     if (npairs && (!pairs || !aligned(pairs, 16))) return fail(PDR_INVALID_ARGUMENT, "seam_uv_pairs must be 16-byte aligned");
     return PDR_OK;
 }

@@ -114,6 +114,11 @@ cudaError_t launch_tv(const float* tex, uint32_t tw, uint32_t th, const uint8_t*
                       float scale, float* grad, cudaStream_t stream);
 cudaError_t launch_adam(float* tex, float* grad, float* m, float* v, size_t n, float lr, float b1, float b2, float eps,
                         float bc1, float bc2, float cmin, float cmax, cudaStream_t stream);
+// launch_tv followed by launch_adam in one pass, reading tex_in and writing tex_out (different buffers)
+cudaError_t launch_adam_tv(const float* tex_in, float* tex_out, float* grad, float* m, float* v, uint32_t tw,
+                           uint32_t th, const uint8_t* valid, const int32_t* chart, float tv_eps, float tv_scale,
+                           float lr, float b1, float b2, float eps, float bc1, float bc2, float cmin, float cmax,
+                           cudaStream_t stream);
 cudaError_t precond_prepare();  // sets the kernels' shared-memory limits (once; before any capture)
 cudaError_t launch_precond_forward(const float* params, const uint16_t* wbf, const uint16_t* feat, uint64_t n,
                                    float* out, uint32_t* status, cudaStream_t stream);

@@ -221,7 +221,67 @@ __global__ void adam_kernel(float* __restrict__ tex, float* __restrict__ grad, f
     }
 }
 
+// The TV gradient of texel i (tv_kernel's arithmetic on tex_in) added to its photometric gradient, then
+// the Adam update of adam_kernel into tex_out: one pass over the atlas for a step with total variation.
+// tex_in and tex_out are different buffers, so every texel reads its neighbours' values from before the
+// step, as the separate TV pass does. Bit-identical to tv_kernel followed by adam_kernel.
+__global__ void adam_tv_kernel(const float* __restrict__ tex_in, float* __restrict__ tex_out,
+                               float* __restrict__ grad, float* __restrict__ m1, float* __restrict__ m2,
+                               uint32_t tw, uint32_t th, const uint8_t* __restrict__ valid,
+                               const int32_t* __restrict__ chart, float tv_eps, float tv_scale, float lr, float b1,
+                               float b2, float eps, float bc1, float bc2, float cmin, float cmax) {
+    const size_t texels = (size_t)tw * th;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < texels; t += stride) {
+        float4 d = reinterpret_cast<const float4*>(grad)[t];
+        if (valid[t]) {
+            const uint32_t i = (uint32_t)t, x = i % tw, y = i / tw;
+            float g[3] = {0.0f, 0.0f, 0.0f};
+            const int32_t ci = chart ? chart[i] : 0;
+            const int64_t nb[4] = {x + 1 < tw ? (int64_t)i + 1 : -1, y + 1 < th ? (int64_t)i + tw : -1,
+                                   x > 0 ? (int64_t)i - 1 : -1, y > 0 ? (int64_t)i - tw : -1};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (nb[k] < 0) continue;
+                const size_t j = (size_t)nb[k];
+                if (!valid[j] || (chart && chart[j] != ci)) continue;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float dd = k < 2 ? tex_in[j * 3 + c] - tex_in[t * 3 + c] : tex_in[t * 3 + c] - tex_in[j * 3 + c];
+                    const float r = sqrtf(dd * dd + tv_eps * tv_eps);
+                    const float gg = dd / r * tv_scale;
+                    g[c] += k < 2 ? -gg : gg;
+                }
+            }
+            d.x += g[0];
+            d.y += g[1];
+            d.z += g[2];
+        }
+        float gv[3] = {d.x, d.y, d.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float x = tex_in[t * 3 + c];
+            adam_one(x, gv[c], m1[t * 3 + c], m2[t * 3 + c], lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+            tex_out[t * 3 + c] = x;
+        }
+        reinterpret_cast<float4*>(grad)[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_adam_tv(const float* tex_in, float* tex_out, float* grad, float* m, float* v, uint32_t tw,
+                           uint32_t th, const uint8_t* valid, const int32_t* chart, float tv_eps, float tv_scale,
+                           float lr, float b1, float b2, float eps, float bc1, float bc2, float cmin, float cmax,
+                           cudaStream_t stream) {
+    const size_t texels = (size_t)tw * th;
+    size_t blocks = (texels + 255) / 256;
+    if (blocks > 0x7FFFFFFFu) blocks = 0x7FFFFFFFu;
+    if (blocks == 0) blocks = 1;
+    adam_tv_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tex_in, tex_out, grad, m, v, tw, th, valid, chart, tv_eps,
+                                                         tv_scale, lr, b1, b2, eps, bc1, bc2, cmin, cmax);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_prepare_view(const float* image, uint32_t C, const float* ext_mask, const float* raster, size_t P,
                                 float* target, float* mask, cudaStream_t stream) {

@@ -226,3 +226,45 @@ def test_total_variation_kernel(masked):
         assert not grad[..., 3].any()
         got = grad[..., :3].cpu().numpy()
         assert np.all(np.abs(got - want) <= 1e-6 * np.abs(want) + 1e-7 * np.abs(want).max()), (H, W, masked)
+
+
+@pytest.mark.parametrize("steps", [7, 8])
+def test_refine_tv_fused_pass_is_bit_identical(baker, steps):
+    """With the chart-aware total variation on, pdr_refine_run given a second atlas buffer
+    (texture_scratch) runs each step's TV gradient and Adam update as one pass, alternating the texture
+    between the two buffers; texture, moments and loss history are bit-identical to the separate TV pass,
+    for an odd and an even step count (the result ends in the caller's texture either way)."""
+    import ctypes as C
+
+    import torch
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.rasterizer import _ptr
+
+    init, pos3, uv, idx, images, mats, masks, pairs = refine_scene(2)
+    valid = np.ones((64, 64), np.float32)
+    valid[:3] = 0.0
+    chart = (np.arange(64)[None, :] // 20 + 4 * (np.arange(64)[:, None] // 32)).astype(np.int32)
+    with baker.context.lock:
+        st = baker._refine_prepare(init, pos3, uv, idx, images, mats, masks, None, pairs, steps, 2, 0.05, 0.01,
+                                   1e-3, 3, 1e-3, 0.9, 0.999, 1e-8, 0.0, 1.0, 1e-4, 0.05, valid, chart, 1e-4)
+        o = st.options
+        assert float(o.tv_scale) > 0.0
+        n = len(st.weights)
+        vw = (C.c_double * n)(*st.weights)
+        outs = []
+        for fused in (False, True):
+            tex = st.init.clone().contiguous()
+            grad = torch.empty((64, 64, 4), dtype=torch.float32, device=tex.device)
+            m1, m2 = torch.empty_like(tex), torch.empty_like(tex)
+            loss = torch.empty(steps + 3, dtype=torch.float32, device=tex.device)
+            scratch = torch.empty_like(tex) if fused else None
+            o.texture_scratch = scratch.data_ptr() if fused else None
+            _native.call("pdr_refine_run", C.addressof(o), _ptr(st.table_dev), n, C.addressof(vw), st.max_pixels,
+                         _ptr(st.pairs), st.npairs, _ptr(st.tv_valid), _ptr(st.tv_chart), _ptr(tex), _ptr(grad),
+                         _ptr(m1), _ptr(m2), _ptr(loss), 1, baker.context.stream())
+            torch.cuda.synchronize()
+            outs.append([x.cpu().numpy() for x in (tex, m1, m2, loss)])
+        o.texture_scratch = None
+    for a, b in zip(*outs):
+        assert same_bits(a, b)
