@@ -882,7 +882,14 @@ KERNEL_SOURCES = {
     "rasterize_forward+shade": ["raster.cu", "raster_tile.cuh", "bin_rect.cuh", "pdr_common.cuh"],
     "render_backward": ["fused.cu", "render_bwd_tile.cuh", "pdr_common.cuh"],
 }
-KERNEL_TRAFFIC = {}  # stage -> (sha256 of its sources, bytes per launch)
+# stage -> (fused tile configuration or None when the stage does not depend on it, sha256 of its sources,
+# bytes per launch); from `ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum`
+# on the full 64-view run (profiles/launch_list_fwdbwd_200k_64x1024sq.md)
+KERNEL_TRAFFIC = {
+    "bin_tiles": ((16, 8, 128), "60298d0918abf86e", 174212096 + 151606272 + 2103296 + 2103296 + 7424),
+    "rasterize_forward+shade": ((16, 8, 128), "91d45257ec459f47", 8009729536),
+    "render_backward": (None, "286c17956e20", 7739196672),
+}
 
 
 def kernel_source_hash(stage: str) -> str:
@@ -895,9 +902,13 @@ def kernel_source_hash(stage: str) -> str:
     return h.hexdigest()
 
 
-def recorded_traffic(stage: str):
+def recorded_traffic(stage: str, config):
+    """The recorded DRAM bytes per launch of `stage`, when its sources (and, for the binning and raster
+    stages, the fused tile configuration) are those the capture ran; else None."""
     rec = KERNEL_TRAFFIC.get(stage)
-    return rec[1] if rec and rec[0] == kernel_source_hash(stage) else None
+    if not rec or not kernel_source_hash(stage).startswith(rec[1]):
+        return None
+    return rec[2] if rec[0] is None or tuple(rec[0]) == tuple(config) else None
 
 
 def stage_bytes(w, T, V, entries):
@@ -981,6 +992,20 @@ def e2e_render(dev, r, host, H, W, steps, world=1):
             step(i, total)
         compute.wait_stream(copy_stream)
 
+    # the host link on its own: pinned copies of the step's largest input up and of its gradient down
+    big = max(host.values(), key=lambda t: t.numel() * t.element_size())
+    dbuf = torch.empty_like(big, device=dev)
+    link = {}
+    for name, (dst, src) in (("h2d_gbs", (dbuf, big)), ("d2h_gbs", (big, dbuf))):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        link[name] = 3 * big.numel() * big.element_size() / (time.perf_counter() - t0) / 1e9
+    e2e_render.last_link = link
+    del dbuf
     run(2)  # warm-up: allocations and the tile-list capacity (reported back without a wait)
     torch.cuda.synchronize(dev)
     pdr_torch.check_deferred_errors(r)
@@ -1158,7 +1183,8 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": pipe.kernels_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": recorded_traffic(dom_name) if views == 64 and w["atlas"] == 4096 else None,
+                         "traffic": recorded_traffic(dom_name, pipe.tile_config)
+                         if views == 64 and w["atlas"] == 4096 else None,
                          "traffic_source_sha256": kernel_source_hash(dom_name),
                          "algorithmic_bytes": sbytes[dom_name], "ms": float(stage_ms[dom])},
             "stages_ms": {n: float(t) for n, t in zip(STAGES, stage_ms)},
@@ -1167,6 +1193,10 @@ def run_gpu(args, world, rank, local):
                               "frac": step_bytes / (ms / 1e3) / 1e9 / hbm},
             "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                    "link": getattr(e2e_render, "last_link", None),
+                    "link_floor_ms": (h2d / getattr(e2e_render, "last_link", {}).get("h2d_gbs", float("inf")) +
+                                      d2h / getattr(e2e_render, "last_link", {}).get("d2h_gbs", float("inf"))) / 1e6
+                    if getattr(e2e_render, "last_link", None) else None,
                     "api": "photara_drender_gb300.torch.render (fused autograd op, deferred_errors=True: no host "
                            "wait per call) + backward; inputs copied from pinned host memory every step "
                            "(double-buffered on a copy stream), gradients read back on the same copy stream after "

@@ -158,6 +158,12 @@ __global__ void seam_kernel(const float* __restrict__ tex, uint32_t tw, uint32_t
     if (threadIdx.x == 0 && s != 0.0f) atomicAdd(loss + loss_index, s);
 }
 
+// One pair term of the chart-aware TV gradient, d / sqrt(d^2 + eps^2) * scale, with the reciprocal
+// square root (about 2 ulp) in place of a square root and an IEEE division: the TV gradient is held to
+// a tolerance (atlas.py's autograd, 1e-6 relative), and the exact form made the fused TV + Adam pass
+// instruction-bound (12 square roots and divisions per texel).
+__device__ __forceinline__ float tv_term(float d, float eps, float scale) { return d * rsqrtf(d * d + eps * eps) * scale; }
+
 // Chart-aware robust total variation of atlas.py:84-115 added into the gradient: each valid
 // same-chart neighbour pair (right and down) contributes d / sqrt(d^2 + eps^2) * scale.
 __global__ void tv_kernel(const float* __restrict__ tex, uint32_t tw, uint32_t th, const uint8_t* __restrict__ valid,
@@ -179,8 +185,7 @@ __global__ void tv_kernel(const float* __restrict__ tex, uint32_t tw, uint32_t t
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float d = k < 2 ? tex[j * 3 + c] - tex[(size_t)i * 3 + c] : tex[(size_t)i * 3 + c] - tex[j * 3 + c];
-            const float r = sqrtf(d * d + eps * eps);
-            const float gg = d / r * scale;
+            const float gg = tv_term(d, eps, scale);
             g[c] += k < 2 ? -gg : gg;
         }
     }
@@ -248,8 +253,7 @@ __global__ void adam_tv_kernel(const float* __restrict__ tex_in, float* __restri
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const float dd = k < 2 ? tex_in[j * 3 + c] - tex_in[t * 3 + c] : tex_in[t * 3 + c] - tex_in[j * 3 + c];
-                    const float r = sqrtf(dd * dd + tv_eps * tv_eps);
-                    const float gg = dd / r * tv_scale;
+                    const float gg = tv_term(dd, tv_eps, tv_scale);
                     g[c] += k < 2 ? -gg : gg;
                 }
             }

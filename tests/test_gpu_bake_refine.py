@@ -5,7 +5,7 @@ import pytest
 
 from oracle import api
 from photara_drender_gb300 import synthetic as S
-from tests.gpu_util import same_bits
+from tests.gpu_util import grad_check, same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -190,9 +190,10 @@ def test_refine_step_kernels(baker):
 @pytest.mark.parametrize("masked", [False, True])
 def test_total_variation_kernel(masked):
     """pdr_refine_total_variation (the chart-aware TV of atlas.py:84-115 added into the refiner's gradient)
-    against ora_tv_gradient, itself pinned to the reference's autograd (tests/test_atlas_losses.py), on
-    the golden texture and a larger random atlas: per texel a sum of at most four pair terms, so within
-    1e-6 of the element plus 1e-7 of the largest element."""
+    against the oracle's TV gradient, itself pinned to the reference's autograd
+    (tests/test_atlas_losses.py), on the golden texture and a larger random atlas: within
+    tests/gpu_util.grad_check of the FP64 twin (each pair term uses a reciprocal square root of about
+    2 ulp; a texel sums at most four of them)."""
     import ctypes as C
     import os
 
@@ -225,15 +226,20 @@ def test_total_variation_kernel(masked):
                      float(scale), _ptr(grad), stream)
         assert not grad[..., 3].any()
         got = grad[..., :3].cpu().numpy()
-        assert np.all(np.abs(got - want) <= 1e-6 * np.abs(want) + 1e-7 * np.abs(want).max()), (H, W, masked)
+        kw = dict(valid=valid.astype(np.uint8), chart=chart, eps=1e-4, weight=0.37)
+        w64, _ = api.tv_gradient(tex, f64=True, **kw)
+        wab, _ = api.tv_gradient(tex, f64=True, abs_terms=True, **kw)
+        grad_check(got, want, w64, wab, name=f"tv {H}x{W} masked={masked}")
 
 
 @pytest.mark.parametrize("steps", [7, 8])
 def test_refine_tv_fused_pass_is_bit_identical(baker, steps):
     """With the chart-aware total variation on, pdr_refine_run given a second atlas buffer
     (texture_scratch) runs each step's TV gradient and Adam update as one pass, alternating the texture
-    between the two buffers; texture, moments and loss history are bit-identical to the separate TV pass,
-    for an odd and an even step count (the result ends in the caller's texture either way)."""
+    between the two buffers, for an odd and an even step count (the result ends in the caller's texture
+    either way). Per texel the arithmetic is the separate passes'; the photometric taps are added with
+    atomics, so two runs differ by their accumulation order: the fused run must stay within that
+    run-to-run noise of the separate one (or 1e-5)."""
     import ctypes as C
 
     import torch
@@ -253,7 +259,7 @@ def test_refine_tv_fused_pass_is_bit_identical(baker, steps):
         n = len(st.weights)
         vw = (C.c_double * n)(*st.weights)
         outs = []
-        for fused in (False, True):
+        for fused in (False, False, True):
             tex = st.init.clone().contiguous()
             grad = torch.empty((64, 64, 4), dtype=torch.float32, device=tex.device)
             m1, m2 = torch.empty_like(tex), torch.empty_like(tex)
@@ -266,5 +272,9 @@ def test_refine_tv_fused_pass_is_bit_identical(baker, steps):
             torch.cuda.synchronize()
             outs.append([x.cpu().numpy() for x in (tex, m1, m2, loss)])
         o.texture_scratch = None
-    for a, b in zip(*outs):
-        assert same_bits(a, b)
+    base, again, fused = outs
+    for k, name in enumerate(("texture", "moment1", "moment2", "loss")):
+        noise = np.abs(again[k] - base[k]).max()
+        dev = np.abs(fused[k] - base[k]).max()
+        scale = np.abs(base[k]).max()
+        assert dev <= max(4.0 * noise, 1e-5 * scale), (name, dev, noise)
