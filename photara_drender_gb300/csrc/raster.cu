@@ -302,7 +302,7 @@ __global__ void bin_sort_large_kernel(const uint32_t* __restrict__ offsets, cons
 // may bin with another tile shape and stage depth (the result is the same: a pixel's candidates are
 // the triangles whose bounding box holds it, whatever the tiles).
 
-constexpr int kRasterThreads = 256;  // the default: one 16x16 tile per CTA, eight 8x4 warp regions
+constexpr int kRasterThreads = 256;  // the default: one 16x16 tile per CTA
 
 // true when tile list [b, e) lost entries to the capacity, or the list offsets overflowed u32
 __device__ __forceinline__ bool tile_list_cut(uint32_t b, uint32_t e, unsigned long long capacity,
@@ -311,7 +311,7 @@ __device__ __forceinline__ bool tile_list_cut(uint32_t b, uint32_t e, unsigned l
 }
 
 template <bool kDeriv, bool kShade, int TW = kTile, int TH = kTile, int CHUNK = kRasterThreads>
-__global__ void __launch_bounds__(TW * TH)
+__global__ void __launch_bounds__(TW * TH, 1280 / (TW * TH))  // 48 registers: 40 warps per SM
 raster_forward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx,
                       uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t cull,
                       uint32_t tcx, uint32_t tiles, const uint32_t* __restrict__ offsets,

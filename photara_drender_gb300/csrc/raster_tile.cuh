@@ -4,28 +4,15 @@
 //
 // Per tile: the tile's triangles are staged in shared memory (structure of arrays) CHUNK at a time,
 // each with the rectangle of tile pixels whose samples can pass its edge tests (pixel_rect, a rigorous
-// bound). Each warp owns an 8x4 pixel region and, per group of 32 staged triangles:
-//   1. cull: every lane takes one triangle and keeps it when its rectangle meets the region (a triangle
-//      the bound does not cover is kept unless the rigorous region test below, edge_rejects_region,
-//      proves that no pixel of the region passes its edge tests);
-//   2. coverage: for each surviving triangle, every lane runs the edge tests for its pixel, and the
-//      passing (triangle, pixel) pairs are appended to a per-warp queue;
-//   3. depth: whenever 32 pairs are queued, each lane takes one pair, computes its depth with the
-//      reference's arithmetic and folds (depth, triangle) into the pixel's winner key with a
-//      shared-memory atomicMin.
-// Small triangles cover a few pixels of a region, so step 3 runs with full warps instead of the
-// few lanes a per-pixel loop would keep busy. Afterwards each pixel recomputes the winner's
-// barycentrics once. The result does not depend on the order of the tile's triangles.
-//
-// The cull is rigorous. The exact edge function e(s) = cross(a - s, b - s) is linear in the sample
-// s (the s x s terms cancel), so over the region's sample box its extremes sit at the four corner
-// samples. The fp32 value a pixel computes, fl(e) = fl(fl(fl(ax-sx)*fl(by-sy)) - fl(fl(ay-sy)*fl(bx-sx))),
-// differs from the exact e by at most 4u(|A B| + |C D|) (u = 2^-24, four roundings per term), and the
-// corner values computed in fp32 carry the same bound. A triangle is skipped for the region when,
-// for one edge, the corner maximum plus 1e-6 * max(|A B| + |C D|) (about 17u, a generous bound of
-// both errors) still fails the reference's test fl(e) * sign < -1e-7 -- then every pixel of the
-// region fails it too, and the per-pixel loop would have skipped the triangle. Results are
-// unchanged; the depth test keeps the minimum (depth, id) as the reference's sequential loop does.
+// bound including the reference's 1e-7 tolerance and fp32 rounding). The candidates, the (triangle,
+// pixel) pairs of those rectangles, are then spread over the lanes one pair per lane: each warp owns a
+// share of the staged triangles, numbers their candidates with a prefix sum and works through them 32 at
+// a time. A lane runs the reference's edge tests at its candidate's sample and, when they pass, computes
+// the depth with the reference's arithmetic and folds (depth, triangle) into the pixel's winner key with
+// a shared-memory atomicMin. Small triangles have a handful of candidates, so lanes stay busy where a
+// warp-per-region coverage pass would test 32 pixels to find a few. Afterwards each pixel recomputes the
+// winner's barycentrics once. The result does not depend on the order of the tile's triangles: the
+// minimum (depth, id) key is what the reference's sequential depth test keeps.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -61,14 +48,14 @@ struct RasterView {
 
 template <int CHUNK>
 struct TileStage {
-    float s0x[CHUNK], s0y[CHUNK], s1x[CHUNK], s1y[CHUNK], s2x[CHUNK], s2y[CHUNK], sign[CHUNK];
-    uint32_t t[CHUNK];
+    float4 edge_a[CHUNK];  // screen positions s0x, s0y, s1x, s1y
+    float4 edge_b[CHUNK];  // s2x, s2y, orientation sign, triangle index (bits)
     uint32_t rect[CHUNK];  // candidate rectangle (x0 | x1 << 8 | y0 << 16 | y1 << 24, tile-local), or below
     float4 p0[CHUNK], p1[CHUNK], p2[CHUNK];
 };
 
 constexpr uint32_t kRectNone = 0xFFFFFFFEu;   // no pixel of the tile can pass: nothing to do
-constexpr uint32_t kRectLarge = 0xFFFFFFFFu;  // the bound does not apply: region cull
+constexpr uint32_t kRectLarge = 0xFFFFFFFFu;  // the bound does not apply: every pixel of the tile
 
 // The pixels of tile [x_org, x_org + TW) x [y_org, y_org + TH) (clipped to the image) whose samples can pass
 // all three of the reference's edge tests fl(e) * sign >= -1e-7, as a rectangle, or kRectLarge when the
@@ -110,22 +97,6 @@ __device__ __forceinline__ uint32_t pixel_rect(float s0x, float s0y, float s1x, 
     const uint32_t x0 = (uint32_t)cx0 - x_org, x1 = (uint32_t)cx1 - x_org;
     const uint32_t y0 = (uint32_t)cy0 - y_org, y1 = (uint32_t)cy1 - y_org;
     return x0 | (x1 << 8) | (y0 << 16) | (y1 << 24);
-}
-
-// true when fl(cross(a - s, b - s)) * sign < -1e-7 holds for every sample s of the region box
-__device__ __forceinline__ bool edge_rejects_region(float ax, float ay, float bx, float by, float sign, float sx_lo,
-                                                    float sx_hi, float sy_lo, float sy_hi) {
-    const float e00 = cross2(ax - sx_lo, ay - sy_lo, bx - sx_lo, by - sy_lo);
-    const float e10 = cross2(ax - sx_hi, ay - sy_lo, bx - sx_hi, by - sy_lo);
-    const float e01 = cross2(ax - sx_lo, ay - sy_hi, bx - sx_lo, by - sy_hi);
-    const float e11 = cross2(ax - sx_hi, ay - sy_hi, bx - sx_hi, by - sy_hi);
-    const float mA = fmaxf(fabsf(ax - sx_lo), fabsf(ax - sx_hi)), mD = fmaxf(fabsf(bx - sx_lo), fabsf(bx - sx_hi));
-    const float mB = fmaxf(fabsf(by - sy_lo), fabsf(by - sy_hi)), mC = fmaxf(fabsf(ay - sy_lo), fabsf(ay - sy_hi));
-    const float slack = 1e-6f * (mA * mB + mC * mD);
-    const float probe = e00 + e10 + e01 + e11 + slack;
-    if (probe != probe || isinf(probe)) return false;  // NaN or overflow: never cull
-    if (sign > 0.0f) return fmaxf(fmaxf(e00, e10), fmaxf(e01, e11)) + slack < -1e-7f;
-    return fminf(fminf(e00, e10), fminf(e01, e11)) - slack > 1e-7f;
 }
 
 // The winner's outputs at sample (sx, sy), rasterize_forward.hlsl's arithmetic: clamped barycentrics,
@@ -184,33 +155,25 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                                             const uint32_t* __restrict__ list, uint32_t b, uint32_t e) {
     constexpr int kThreads = TW * TH;
     constexpr int kWarps = kThreads / 32;
-    constexpr int kRegionsX = TW / 8;
-    static_assert(TW % 8 == 0 && TH % 4 == 0 && kThreads % 32 == 0, "tiles are made of 8x4 warp regions");
+    static_assert(TW <= 64 && TH <= 64 && kThreads <= 512 && kThreads % 32 == 0,
+                  "candidate rectangles pack tile-local coordinates; li * width < 2^16");
     static_assert(CHUNK % 32 == 0 && CHUNK <= kThreads, "a stage holds at most one triangle per thread");
     __shared__ TileStage<CHUNK> tri;
-    // Winner per pixel as a 64-bit key (ordered depth bits << 32 | triangle index): the minimum key is
-    // the nearest depth, ties to the lowest id, exactly the reference's sequential test.
+    // Winner per pixel (row-major in the tile) as a 64-bit key (ordered depth bits << 32 | triangle
+    // index): the minimum key is the nearest depth, ties to the lowest id, exactly the reference's
+    // sequential test.
     __shared__ unsigned long long best_key[kThreads];
-    __shared__ uint32_t queue[kWarps][64];  // per warp: (triangle slot << 5) | pixel lane
     __shared__ float tile_sx[TW], tile_sy[TH];  // sample positions of the tile's columns and rows
+    __shared__ uint4 owners[kWarps][32];  // per warp: (first candidate, rectangle, row divisor, stage slot)
 
     const float4* __restrict__ clip = v.clip;
     const uint3* __restrict__ idx = v.idx;
     const float4 vp = v.vp;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t rx = tx * TW + (warp % kRegionsX) * 8u;  // region origin
-    const uint32_t ry = ty * TH + (warp / kRegionsX) * 4u;
-    const uint32_t px = rx + (lane & 7u);
-    const uint32_t py = ry + (lane >> 3);
-    const float sx = sample_ndc(px, vp.x, vp.z);
-    const float sy = sample_ndc(py, vp.y, vp.w);
-    const float sx_lo = sample_ndc(rx, vp.x, vp.z), sx_hi = sample_ndc(rx + 7u, vp.x, vp.z);
-    const float sy_lo = sample_ndc(ry, vp.y, vp.w), sy_hi = sample_ndc(ry + 3u, vp.y, vp.w);
-    uint32_t* q = queue[warp];
+    const uint32_t x_org = tx * TW, y_org = ty * TH;
+    const uint32_t px = x_org + threadIdx.x % (uint32_t)TW, py = y_org + threadIdx.x / (uint32_t)TW;
     best_key[threadIdx.x] = ~0ull;
     const bool in_image = px < v.W && py < v.H;
-    const uint32_t reg_x = (warp % kRegionsX) * 8u, reg_y = (warp / kRegionsX) * 4u;  // region in the tile
-    const uint32_t x_org = tx * TW, y_org = ty * TH;
     const uint32_t x_end = min(x_org + (uint32_t)TW, v.W), y_end = min(y_org + (uint32_t)TH, v.H);
     if (threadIdx.x < (uint32_t)TW) tile_sx[threadIdx.x] = sample_ndc(x_org + threadIdx.x, vp.x, vp.z);
     if (threadIdx.x < (uint32_t)TH) tile_sy[threadIdx.x] = sample_ndc(y_org + threadIdx.x, vp.y, vp.w);
@@ -235,7 +198,6 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                 p1 = clip[vi.y];
                 p2 = clip[vi.z];
             }
-            tri.t[threadIdx.x] = t;
             tri.p0[threadIdx.x] = p0; tri.p1[threadIdx.x] = p1; tri.p2[threadIdx.x] = p2;
             if (binned) {
                 if (!(p0.w <= 1e-8f || p1.w <= 1e-8f || p2.w <= 1e-8f)) {
@@ -253,93 +215,91 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
                     }
                 }
             }
-            tri.s0x[threadIdx.x] = s0x; tri.s0y[threadIdx.x] = s0y;
-            tri.s1x[threadIdx.x] = s1x; tri.s1y[threadIdx.x] = s1y;
-            tri.s2x[threadIdx.x] = s2x; tri.s2y[threadIdx.x] = s2y;
-            tri.sign[threadIdx.x] = sgn;
+            tri.edge_a[threadIdx.x] = make_float4(s0x, s0y, s1x, s1y);
+            tri.edge_b[threadIdx.x] = make_float4(s2x, s2y, sgn, __uint_as_float(t));
             tri.rect[threadIdx.x] = rect;
         }
         __syncthreads();
         const uint32_t n = min(e - chunk, (uint32_t)CHUNK);
-        // Depth test of up to 32 queued (triangle, pixel) pairs, one per lane: the reference's
-        // arithmetic at the pair's pixel, folded into the pixel's winner key.
-        auto depth_pairs = [&](uint32_t count) {
-            const uint32_t ent = lane < count ? q[lane] : 0u;
-            const uint32_t pl = ent & 31u, k = ent >> 5;
-            const float psx = __shfl_sync(0xffffffffu, sx, pl);
-            const float psy = __shfl_sync(0xffffffffu, sy, pl);
-            if (lane < count) {
-                const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
-                const float q0x = p0.x - psx * p0.w, q0y = p0.y - psy * p0.w;
-                const float q1x = p1.x - psx * p1.w, q1y = p1.y - psy * p1.w;
-                const float q2x = p2.x - psx * p2.w, q2y = p2.y - psy * p2.w;
-                const float a0 = cross2(q1x, q1y, q2x, q2y);
-                const float a1 = cross2(q2x, q2y, q0x, q0y);
-                const float a2 = cross2(q0x, q0y, q1x, q1y);
-                const float ha = a0 + a1 + a2;
-                if (!(fabsf(ha) <= 1e-12f)) {
-                    const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
-                    const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
-                    if (!(fabsf(iw) <= 1e-12f))
-                        atomicMin(&best_key[(warp << 5) | pl], depth_key(clamp_hlsl(iz / iw, -1.0f, 1.0f), tri.t[k]));
-                }
-            }
-        };
-        uint32_t qn = 0;  // queued pairs, warp-uniform
-        for (uint32_t g = 0; g < n; g += 32) {
-            const uint32_t j = g + lane;
-            bool maybe = false;
-            if (j < n) {
-                const uint32_t rc = tri.rect[j];
-                if (rc < kRectNone) {
-                    // the triangle's candidate rectangle meets the region
-                    maybe = (rc & 0xFFu) <= reg_x + 7u && ((rc >> 8) & 0xFFu) >= reg_x &&
-                            ((rc >> 16) & 0xFFu) <= reg_y + 3u && (rc >> 24) >= reg_y;
-                } else if (rc == kRectLarge) {
-                    const float sgn = tri.sign[j];
-                    const float ax0 = tri.s0x[j], ay0 = tri.s0y[j], ax1 = tri.s1x[j], ay1 = tri.s1y[j];
-                    const float ax2 = tri.s2x[j], ay2 = tri.s2y[j];
-                    maybe = !(edge_rejects_region(ax1, ay1, ax2, ay2, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
-                              edge_rejects_region(ax2, ay2, ax0, ay0, sgn, sx_lo, sx_hi, sy_lo, sy_hi) ||
-                              edge_rejects_region(ax0, ay0, ax1, ay1, sgn, sx_lo, sx_hi, sy_lo, sy_hi));
-                }
-            }
-            unsigned live = __ballot_sync(0xffffffffu, maybe);
-            while (live) {
-                const uint32_t k = g + (uint32_t)(__ffs(live) - 1);
-                live &= live - 1u;
-                // coverage (rasterize_forward.hlsl edge tests) for every pixel of the region at once
-                const float sgn = tri.sign[k];
-                const float s0x = tri.s0x[k], s0y = tri.s0y[k], s1x = tri.s1x[k], s1y = tri.s1y[k];
-                const float s2x = tri.s2x[k], s2y = tri.s2y[k];
-                const float e0 = cross2(s1x - sx, s1y - sy, s2x - sx, s2y - sy);
-                const float e1 = cross2(s2x - sx, s2y - sy, s0x - sx, s0y - sy);
-                const float e2 = cross2(s0x - sx, s0y - sy, s1x - sx, s1y - sy);
-                const float ceps = -1e-7f;
-                const bool pass = in_image && !(e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps);
-                const unsigned m = __ballot_sync(0xffffffffu, pass);
-                if (!m) continue;
-                if (pass) q[qn + __popc(m & ((1u << lane) - 1u))] = (k << 5) | lane;
-                qn += __popc(m);
-                if (qn >= 32) {
-                    __syncwarp();
-                    depth_pairs(32);
-                    __syncwarp();
-                    const uint32_t rest = qn - 32;
-                    const uint32_t moved = lane < rest ? q[32 + lane] : 0u;
-                    __syncwarp();
-                    if (lane < rest) q[lane] = moved;
-                    __syncwarp();
-                    qn = rest;
-                }
+        // Candidate expansion: lane j of warp w owns staged triangle k = w + kWarps * j and its candidate
+        // pixels, the tile pixels of its rectangle (the whole tile for kRectLarge). The warp numbers its
+        // triangles' candidates with a prefix sum, lists the triangles that have any (in that order) in
+        // a per-warp table, and works through the candidates 32 at a time, one per lane: a lane finds its
+        // candidate's triangle from the triangles whose last candidate precedes it, runs the reference's
+        // edge tests at the candidate's sample and, when they pass, folds (depth, triangle) into the
+        // pixel's winner key. Lanes stay busy whatever the triangles' sizes.
+        const uint32_t k_own = warp + (uint32_t)kWarps * lane;
+        uint32_t cnt = 0, geom = 0;  // candidate count; rectangle origin x | y << 8 | width << 16
+        if (k_own < n) {
+            const uint32_t rc = tri.rect[k_own];
+            if (rc < kRectNone) {
+                const uint32_t x0 = rc & 0xFFu, x1 = (rc >> 8) & 0xFFu, y0 = (rc >> 16) & 0xFFu, y1 = rc >> 24;
+                cnt = (x1 - x0 + 1u) * (y1 - y0 + 1u);
+                geom = x0 | (y0 << 8) | ((x1 - x0 + 1u) << 16);
+            } else if (rc == kRectLarge) {
+                cnt = (x_end - x_org) * (y_end - y_org);
+                geom = (x_end - x_org) << 16;
             }
         }
-        if (qn) {
-            __syncwarp();
-            depth_pairs(qn);
+        uint32_t incl = cnt;  // inclusive prefix sum over the warp's lanes
+#pragma unroll
+        for (uint32_t d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
         }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const unsigned nonzero = __ballot_sync(0xffffffffu, cnt > 0);
+        if (cnt > 0) {
+            // row of candidate li = li * m >> 16 with m = ceil(2^16 / width): exact for li * width < 2^16
+            const uint32_t w = geom >> 16;
+            owners[warp][__popc(nonzero & ((1u << lane) - 1u))] =
+                make_uint4(incl - cnt, geom, (65536u + w - 1u) / w, k_own);
+        }
+        __syncwarp();
+        uint32_t ended = 0;  // triangles (with candidates) whose last candidate precedes this batch
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t c = base + lane;
+            const uint32_t last = incl - 1u;  // this lane's triangle's last candidate
+            const uint32_t mark = (cnt > 0 && last >= base && last - base < 32u) ? 1u << (last - base) : 0u;
+            const uint32_t ends = __reduce_or_sync(0xffffffffu, mark);
+            const uint32_t r = ended + __popc(ends & ((1u << lane) - 1u));
+            ended += __popc(ends);
+            if (c >= total) continue;
+            const uint4 ow = owners[warp][r];
+            const uint32_t li = c - ow.x;  // candidate index within the rectangle
+            const uint32_t w = ow.y >> 16, qy = (li * ow.z) >> 16;
+            const uint32_t lx = (ow.y & 0xFFu) + (li - qy * w), ly = ((ow.y >> 8) & 0xFFu) + qy;
+            const uint32_t k = ow.w;
+            const float psx = tile_sx[lx], psy = tile_sy[ly];
+            // coverage: rasterize_forward.hlsl's edge tests at the candidate's sample
+            const float4 ea = tri.edge_a[k], eb = tri.edge_b[k];
+            const float s0x = ea.x, s0y = ea.y, s1x = ea.z, s1y = ea.w, s2x = eb.x, s2y = eb.y, sgn = eb.z;
+            const float e0 = cross2(s1x - psx, s1y - psy, s2x - psx, s2y - psy);
+            const float e1 = cross2(s2x - psx, s2y - psy, s0x - psx, s0y - psy);
+            const float e2 = cross2(s0x - psx, s0y - psy, s1x - psx, s1y - psy);
+            const float ceps = -1e-7f;
+            if (e0 * sgn < ceps || e1 * sgn < ceps || e2 * sgn < ceps) continue;
+            // depth with the reference's arithmetic at the pair's sample, folded into the winner key
+            const float4 p0 = tri.p0[k], p1 = tri.p1[k], p2 = tri.p2[k];
+            const float q0x = p0.x - psx * p0.w, q0y = p0.y - psy * p0.w;
+            const float q1x = p1.x - psx * p1.w, q1y = p1.y - psy * p1.w;
+            const float q2x = p2.x - psx * p2.w, q2y = p2.y - psy * p2.w;
+            const float a0 = cross2(q1x, q1y, q2x, q2y);
+            const float a1 = cross2(q2x, q2y, q0x, q0y);
+            const float a2 = cross2(q0x, q0y, q1x, q1y);
+            const float ha = a0 + a1 + a2;
+            if (fabsf(ha) <= 1e-12f) continue;
+            const float iz = p0.z * a0 + p1.z * a1 + p2.z * a2;
+            const float iw = p0.w * a0 + p1.w * a1 + p2.w * a2;
+            if (fabsf(iw) <= 1e-12f) continue;
+            const unsigned long long key = depth_key(clamp_hlsl(iz / iw, -1.0f, 1.0f), __float_as_uint(eb.w));
+            unsigned long long* slot = &best_key[ly * (uint32_t)TW + lx];
+            if (key < *slot) atomicMin(slot, key);  // keys only decrease: a stale read only adds an atomic
+        }
+        __syncwarp();  // the owner table is rewritten by the next stage
     }
-    __syncwarp();
+    // candidates of any warp may land on any pixel of the tile
+    __syncthreads();
     if (!in_image) return;
     const size_t pix = (size_t)py * v.W + px;
     const unsigned long long key = best_key[threadIdx.x];
@@ -355,6 +315,8 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
         }
         return;
     }
+    const float sx = sample_ndc(px, vp.x, vp.z);
+    const float sy = sample_ndc(py, vp.y, vp.w);
     // the winner's barycentrics and depth, recomputed with the reference's arithmetic
     const uint32_t best_tri = (uint32_t)key + 1u;
     const uint3 vi = idx[best_tri - 1];
