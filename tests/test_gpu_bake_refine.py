@@ -265,7 +265,7 @@ def test_refine_tv_fused_pass_is_bit_identical(baker, steps):
             tex = st.init.clone().contiguous()
             grad = torch.empty((64, 64, 4), dtype=torch.float32, device=tex.device)
             m1, m2 = torch.empty_like(tex), torch.empty_like(tex)
-            loss = torch.empty(steps + 3, dtype=torch.float32, device=tex.device)
+            loss = torch.zeros(steps + 3, dtype=torch.float32, device=tex.device)
             scratch = torch.empty_like(tex) if fused else None
             o.texture_scratch = scratch.data_ptr() if fused else None
             _native.call("pdr_refine_run", C.addressof(o), _ptr(st.table_dev), n, C.addressof(vw), st.max_pixels,
