@@ -310,7 +310,8 @@ typedef struct {
     uint32_t* tile_offsets;       /* [views*tiles + 1] */
     uint32_t* tile_triangles;     /* [capacity] */
     uint64_t capacity;
-    void* workspace;              /* pdr_render_workspace_bytes() bytes */
+    void* workspace;              /* forward: pdr_render_workspace_bytes() bytes; backward: optional,
+                                   * see pdr_render_backward_workspace_bytes() */
     size_t workspace_bytes;
     uint32_t* status;             /* PDR_STATUS_WORDS words */
     float* raster;                /* [views][H][W][4] */
@@ -353,8 +354,15 @@ PDR_API pdr_status pdr_render_forward(const pdr_render_args* args, void* stream)
 PDR_API pdr_status pdr_render_bin(const pdr_render_args* args, void* stream);
 PDR_API pdr_status pdr_render_raster(const pdr_render_args* args, void* stream);
 /* The adjoints of the forward in one pixel pass: texture_backward, interpolate_backward for both
- * attribute sets (raster gradients summed) and rasterize_backward. */
+ * attribute sets (raster gradients summed) and rasterize_backward. With a 16-byte aligned workspace of
+ * at least pdr_render_backward_workspace_bytes() bytes, the per-vertex gradients of each view are
+ * gathered in records of the workspace (16-byte reductions, uv + attributes + clip together) and summed
+ * into grad_uv_attributes / grad_attributes over the views in view order by a second pass; without
+ * one they are added into the outputs directly. The gradients agree to float rounding either way. */
 PDR_API pdr_status pdr_render_backward(const pdr_render_args* args, void* stream);
+/* Workspace bytes for pdr_render_backward's per-view vertex-gradient records:
+ * views * vertex_count * 4 * ceil((attribute_count + 5) / 4) * sizeof(float); 0 for attribute_count > 8. */
+PDR_API size_t pdr_render_backward_workspace_bytes(uint32_t views, uint32_t vertex_count, uint32_t attribute_count);
 
 
 /* ---- calibration --------------------------------------------------------------------------------

@@ -89,6 +89,7 @@ _SIGNATURES = {
                                       _vp]),
     "pdr_calibrate_reductions": (_i32, [_vp, _u64, _u64, _u32, _vp]),
     "pdr_render_workspace_bytes_tiled": (_sz, [_u32, _u32, _u32, _u32, _u64, _u32, _u32]),
+    "pdr_render_backward_workspace_bytes": (_sz, [_u32, _u32, _u32]),
     "pdr_refine_seam": (_i32, [_vp, _u32, _u32, _vp, _u32, C.c_float, C.c_float, _vp, _vp, _u32, _vp]),
     "pdr_refine_total_variation": (_i32, [_vp, _u32, _u32, _vp, _vp, C.c_float, C.c_float, _vp, _vp]),
     "pdr_refine_adam": (_i32, [_vp, _vp, _vp, _vp, _u64] + [C.c_float] * 8 + [_vp]),

@@ -185,6 +185,7 @@ batch_backward_kernel(const BatchJob* __restrict__ jobs, const unsigned long lon
     const BatchJob& b = jobs[j];
     const uint32_t tile = (uint32_t)(tg - btile_base[j]);
     BackwardView v;
+    v.g_vtx = nullptr;
     v.clip = b.clip;
     v.V = b.V;
     v.idx = b.idx;

@@ -30,7 +30,8 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
                        const float4* __restrict__ raster, const float2* __restrict__ uv,
                        const float* __restrict__ grad_attr_out, const float4* __restrict__ grad_sampled,
                        float* __restrict__ g_clip_all, float* __restrict__ g_attr, float* __restrict__ g_uv,
-                       float* __restrict__ g_tex, const float4* __restrict__ sdiff, uint32_t* __restrict__ status) {
+                       float* __restrict__ g_tex, const float4* __restrict__ sdiff, uint32_t* __restrict__ status,
+                       float* __restrict__ g_vtx_all) {
     const uint32_t view = blockIdx.y;
     const uint32_t tile = blockIdx.x;
     const size_t P = (size_t)W * H;
@@ -58,7 +59,48 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
     v.g_tex = g_tex;
     v.sdiff = sdiff ? sdiff + view * P * 2 : nullptr;
     v.status = status;
+    v.g_vtx = g_vtx_all ? g_vtx_all + (size_t)view * V * vertex_record_floats(kA) : nullptr;
     render_backward_tile<kA, kTexAgg>(v, tile % tcx, tile / tcx);
+}
+
+// The vertex-gradient records of all views into the outputs: each view's clip gradient (x, y, 0, w), and
+// the uv and attribute gradients summed over the views in view order. One thread per vertex; every
+// output element is written, so none needs clearing first.
+template <int kA>
+__global__ void __launch_bounds__(256)
+vertex_grad_finish_kernel(const float* __restrict__ rec_all, uint32_t views, uint32_t V, float* __restrict__ g_clip_all,
+                          float* __restrict__ g_attr, float* __restrict__ g_uv) {
+    constexpr uint32_t kR = vertex_record_floats(kA);
+    constexpr uint32_t kNV = 2 + kA + 3;
+    const uint32_t vtx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vtx >= V) return;
+    float acc[2 + kA];
+#pragma unroll
+    for (int j = 0; j < 2 + kA; ++j) acc[j] = 0.0f;
+    for (uint32_t view = 0; view < views; ++view) {
+        const float4* rec = reinterpret_cast<const float4*>(rec_all + ((size_t)view * V + vtx) * kR);
+        float r[kR];
+#pragma unroll
+        for (uint32_t c = 0; c < kR / 4; ++c) {
+            const float4 q = __ldcs(rec + c);
+            r[4 * c] = q.x;
+            r[4 * c + 1] = q.y;
+            r[4 * c + 2] = q.z;
+            r[4 * c + 3] = q.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 2 + kA; ++j) acc[j] += r[j];
+        reinterpret_cast<float4*>(g_clip_all)[(size_t)view * V + vtx] =
+            make_float4(r[kNV - 3], r[kNV - 2], 0.0f, r[kNV - 1]);
+    }
+    if (g_uv) {
+        g_uv[(size_t)vtx * 2] = acc[0];
+        g_uv[(size_t)vtx * 2 + 1] = acc[1];
+    }
+    if (g_attr) {
+#pragma unroll
+        for (int a = 0; a < kA; ++a) g_attr[(size_t)vtx * kA + a] = acc[2 + a];
+    }
 }
 
 }  // namespace
@@ -68,6 +110,11 @@ render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const ui
 using namespace pdr;
 
 extern "C" {
+
+size_t pdr_render_backward_workspace_bytes(uint32_t views, uint32_t vertex_count, uint32_t attribute_count) {
+    if (attribute_count > 8) return 0;
+    return (size_t)views * vertex_count * vertex_record_floats((int)attribute_count) * sizeof(float);
+}
 
 size_t pdr_render_workspace_bytes(uint32_t views, uint32_t triangle_count, uint32_t width, uint32_t height,
                                   uint64_t capacity) {
@@ -164,17 +211,28 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
         ((uintptr_t)a->sample_differences & 15u))
         return set_error(PDR_INVALID_ARGUMENT, "gradient outputs must be 16-byte (clip, texture, attributes) / 8-byte (uv) aligned");
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t err = cudaMemsetAsync(a->grad_clip_positions, 0, (size_t)a->views * a->vertex_count * 4 * sizeof(float), s);
-    if (err == cudaSuccess && a->grad_attributes)
-        err = cudaMemsetAsync(a->grad_attributes, 0, (size_t)a->vertex_count * a->attribute_count * sizeof(float), s);
-    if (err == cudaSuccess && a->grad_uv_attributes)
-        err = cudaMemsetAsync(a->grad_uv_attributes, 0, (size_t)a->vertex_count * 2 * sizeof(float), s);
+    const uint32_t A = a->attributes ? a->attribute_count : 0;
+    // with a workspace of pdr_render_backward_workspace_bytes(): per-view vertex-gradient records, summed
+    // into the outputs afterwards; without one, reductions straight into the outputs
+    const size_t rec_bytes = pdr_render_backward_workspace_bytes(a->views, a->vertex_count, A);
+    float* g_vtx = (a->workspace && a->workspace_bytes >= rec_bytes && !((uintptr_t)a->workspace & 15u))
+                       ? static_cast<float*>(a->workspace)
+                       : nullptr;
+    cudaError_t err = cudaSuccess;
+    if (g_vtx) {
+        err = cudaMemsetAsync(g_vtx, 0, rec_bytes, s);
+    } else {
+        err = cudaMemsetAsync(a->grad_clip_positions, 0, (size_t)a->views * a->vertex_count * 4 * sizeof(float), s);
+        if (err == cudaSuccess && a->grad_attributes)
+            err = cudaMemsetAsync(a->grad_attributes, 0, (size_t)a->vertex_count * a->attribute_count * sizeof(float), s);
+        if (err == cudaSuccess && a->grad_uv_attributes)
+            err = cudaMemsetAsync(a->grad_uv_attributes, 0, (size_t)a->vertex_count * 2 * sizeof(float), s);
+    }
     if (err == cudaSuccess && a->grad_texture)
         err = cudaMemsetAsync(a->grad_texture, 0, (size_t)a->texture_width * a->texture_height * 4 * sizeof(float), s);
     if (err != cudaSuccess) return set_cuda_error(err, "render_backward(memset)");
     const uint32_t tcx = (a->width + kTile - 1) / kTile, tcy = (a->height + kTile - 1) / kTile;
     const dim3 grid(tcx * tcy, a->views);
-    const uint32_t A = a->attributes ? a->attribute_count : 0;
     // warp-aggregated texture-gradient taps for magnified textures (see red_add_v4_texel)
     const bool magnified = (uint64_t)a->texture_width * a->texture_height < (uint64_t)a->width * a->height;
 #define PDR_RENDER_BWD_AGG(KA, AGG)                                                                                  \
@@ -185,7 +243,7 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
         a->texture_width, a->texture_height, a->address_mode, reinterpret_cast<const float4*>(a->raster),           \
         reinterpret_cast<const float2*>(a->uv), a->grad_interpolated, reinterpret_cast<const float4*>(a->grad_sampled), \
         a->grad_clip_positions, a->grad_attributes, a->grad_uv_attributes, a->grad_texture,                     \
-        reinterpret_cast<const float4*>(a->texture ? a->sample_differences : nullptr), a->status)
+        reinterpret_cast<const float4*>(a->texture ? a->sample_differences : nullptr), a->status, g_vtx)
 #define PDR_RENDER_BWD(KA)                  \
     if (magnified) {                        \
         PDR_RENDER_BWD_AGG(KA, 1);          \
@@ -205,6 +263,23 @@ pdr_status pdr_render_backward(const pdr_render_args* a, void* stream) {
     }
 #undef PDR_RENDER_BWD
 #undef PDR_RENDER_BWD_AGG
+    if (g_vtx) {
+        const unsigned blocks = (a->vertex_count + 255) / 256;
+        float* gc = a->grad_clip_positions;
+        float* ga = a->grad_attributes;
+        float* gu = a->grad_uv_attributes;
+        switch (A) {
+            case 0: vertex_grad_finish_kernel<0><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 1: vertex_grad_finish_kernel<1><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 2: vertex_grad_finish_kernel<2><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 3: vertex_grad_finish_kernel<3><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 4: vertex_grad_finish_kernel<4><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 5: vertex_grad_finish_kernel<5><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 6: vertex_grad_finish_kernel<6><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            case 7: vertex_grad_finish_kernel<7><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+            default: vertex_grad_finish_kernel<8><<<blocks, 256, 0, s>>>(g_vtx, a->views, a->vertex_count, gc, ga, gu); break;
+        }
+    }
     return set_cuda_error(cudaGetLastError(), "render_backward");
 }
 

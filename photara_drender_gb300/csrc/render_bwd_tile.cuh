@@ -94,7 +94,14 @@ struct BackwardView {
     float* g_tex;                 // [th][tw][4]
     const float4* sdiff;          // [H][W][2] texel differences of the forward's sample, or nullptr
     uint32_t* status;
+    // When set: this view's vertex-gradient records [V][vertex_record_floats(kA)] (uv, attributes,
+    // clip x/y/w, zero padding), added with 16-byte reductions and summed over the views afterwards
+    // (vertex_grad_finish_kernel); g_clip, g_attr and g_uv are then not touched here.
+    float* g_vtx;
 };
+
+// Floats per vertex-gradient record: uv 2 + attributes kA + clip x/y/w 3, rounded up to 16 bytes.
+__host__ __device__ constexpr uint32_t vertex_record_floats(int kA) { return (uint32_t)((5 + kA + 3) / 4 * 4); }
 
 // kTexAgg: texture-gradient taps warp-aggregated (1), plain (0), or decided from the texture and image
 // sizes (-1: aggregated when the texture has fewer texels than the view has pixels).
@@ -304,7 +311,21 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
     for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (uint32_t j = 0; j < kNV; ++j) cv[k][j] = scan.sum(cv[k][j]);
-    if (valid && scan.tail) {
+    if (valid && scan.tail && v.g_vtx) {
+        // one record per vertex and view: kNV values in 16-byte reductions (two for up to three attributes,
+        // against five reductions into the shared uv / attribute rows and the clip row otherwise)
+        constexpr uint32_t kR = vertex_record_floats(kA);
+        const uint32_t corners[3] = {vi.x, vi.y, vi.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (corners[k] >= V) continue;
+            float* rec = v.g_vtx + (size_t)corners[k] * kR;
+#pragma unroll
+            for (uint32_t c = 0; c < kR; c += 4)
+                red_v4(rec + c, make_float4(c < kNV ? cv[k][c] : 0.0f, c + 1 < kNV ? cv[k][c + 1] : 0.0f,
+                                            c + 2 < kNV ? cv[k][c + 2] : 0.0f, c + 3 < kNV ? cv[k][c + 3] : 0.0f));
+        }
+    } else if (valid && scan.tail) {
         const uint32_t corners[3] = {vi.x, vi.y, vi.z};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {

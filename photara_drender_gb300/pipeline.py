@@ -91,8 +91,11 @@ class RenderFwdBwd:
         self.offsets = torch.empty(self.views * tiles + 1, dtype=torch.int32, device=dev)
         self.capacity = int(capacity) if capacity else 4 * self.T * self.views + 1024
         self.list = torch.empty(self.capacity, dtype=torch.int32, device=dev)
-        self.ws_bytes = _native.lib().pdr_render_workspace_bytes_tiled(self.views, self.T, self.W, self.H,
-                                                                       self.capacity, tw, th)
+        # one workspace for the binning and for the backward's per-view vertex-gradient records
+        L = _native.lib()
+        self.ws_bytes = max(L.pdr_render_workspace_bytes_tiled(self.views, self.T, self.W, self.H, self.capacity, tw,
+                                                               th),
+                            L.pdr_render_backward_workspace_bytes(self.views, self.V, self.A))
         self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=dev)
 
     def autotune(self, clip, attrs, uv_attrs, texture, reps: int = 5, configs=TILE_CONFIGS):

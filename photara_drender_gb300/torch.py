@@ -366,6 +366,11 @@ class _RenderFunction(torch.autograd.Function):
                 a.grad_sampled, a.grad_texture = gs.data_ptr(), grad_tex.data_ptr()
                 a.sample_differences = sdiff.data_ptr()
             a.grad_clip_positions, a.status = grad_clip.data_ptr(), r.context.status.data_ptr()
+            # per-view vertex-gradient records for the adjoint (16-byte reductions, summed over the views after)
+            ws_bytes = _native.lib().pdr_render_backward_workspace_bytes(
+                views, V, attrs.shape[1] if attrs is not None else 0)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+            a.workspace, a.workspace_bytes = ws.data_ptr(), ws_bytes
             deferred = ctx.deferred or torch.cuda.is_current_stream_capturing()
             _apply_status(r, r.context.poll_status(kinds=("render_forward", "render_backward")))
             r.context.status.zero_()
