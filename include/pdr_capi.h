@@ -331,8 +331,10 @@ typedef struct {
      * texels again. Null: the backward gathers them. Results are identical either way. */
     float* sample_differences;
     /* Tile shape and triangles staged per pass of the fused render's binning and raster; zeros mean
-     * 16 x 16 and 256 (the reference's tile). Supported: 16x16 with 256 or 128, 16x8 with 128, 32x8
-     * with 256. Outputs are bit-identical for every shape; tile_offsets then has
+     * 16 x 16 and 256 (the reference's tile). Supported: 16x16 with 256 or 128, 16x8 with 128 (shapes
+     * dividing the reference's tile: a triangle is listed in every sub-tile of the 16 x 16 tiles the
+     * reference lists it in, so the (triangle, pixel) pairs tested are the reference's). Outputs are
+     * bit-identical for every shape; tile_offsets then has
      * views * ceil(W / tile_width) * ceil(H / tile_height) + 1 entries. */
     uint32_t tile_width, tile_height, stage_triangles;
 } pdr_render_args;
@@ -505,7 +507,8 @@ typedef struct {
 } pdr_render_mesh;
 
 /* Forward tile shape and the triangles staged in shared memory per pass (the bin depth): 16x8/128,
- * 16x16/128, 16x16/256, 32x16/256 or 32x16/512. The outputs do not depend on the choice. */
+ * 16x16/128 or 16x16/256 (sub-tiles of the reference's 16x16 tile). The outputs do not depend on the
+ * choice. */
 typedef struct {
     uint32_t tile_width, tile_height, stage_triangles;
 } pdr_batch_config;

@@ -16,7 +16,7 @@ import torch
 from . import _native
 from .rasterizer import Rasterizer, _ptr, _viewports
 
-CONFIGS: Tuple[Tuple[int, int, int], ...] = ((16, 8, 128), (16, 16, 128), (16, 16, 256), (32, 16, 256), (32, 16, 512))
+CONFIGS: Tuple[Tuple[int, int, int], ...] = ((16, 8, 128), (16, 16, 128), (16, 16, 256))
 _MODES = {"none": 0, "back": 1, "front": 2}
 _ADDRESS = {"clamp": 0, "wrap": 1, "mirror": 2}
 

@@ -221,16 +221,14 @@ struct BatchPlan {
 bool config_supported(const pdr_batch_config* c) {
     if (!c) return false;
     const uint32_t w = c->tile_width, h = c->tile_height, k = c->stage_triangles;
-    return (w == 16 && h == 8 && k == 128) || (w == 16 && h == 16 && (k == 128 || k == 256)) ||
-           (w == 32 && h == 16 && (k == 256 || k == 512));
+    return (w == 16 && h == 8 && k == 128) || (w == 16 && h == 16 && (k == 128 || k == 256));
 }
 
 pdr_status plan_batch(const pdr_render_mesh* meshes, uint32_t n, const pdr_batch_config* cfg, uint32_t A,
                       bool need_grads, BatchPlan* plan) {
     if (!meshes || n == 0) return set_error(PDR_INVALID_ARGUMENT, "a batch needs at least one mesh");
     if (!config_supported(cfg))
-        return set_error(PDR_INVALID_ARGUMENT, "batch tile shape must be 16x8 (stage 128), 16x16 (stage 128 or 256) "
-                                               "or 32x16 (stage 256 or 512)");
+        return set_error(PDR_INVALID_ARGUMENT, "batch tile shape must be 16x8 (stage 128) or 16x16 (stage 128 or 256)");
     if (A > 8) return set_error(PDR_INVALID_ARGUMENT, "batches support 0..8 attributes");
     plan->tri_base.assign(1, 0);
     plan->tile_base.assign(1, 0);
@@ -401,11 +399,7 @@ pdr_status pdr_render_batch_forward(const pdr_render_mesh* meshes, uint32_t mesh
                                                                  attribute_count, cull_mode, address_mode, s);
     else if (tw == 16 && k == 128) e = launch_batch_raster<16, 16, 128>(w, plan, tile_offsets, tile_triangles, capacity,
                                                                        attribute_count, cull_mode, address_mode, s);
-    else if (tw == 16) e = launch_batch_raster<16, 16, 256>(w, plan, tile_offsets, tile_triangles, capacity,
-                                                            attribute_count, cull_mode, address_mode, s);
-    else if (k == 256) e = launch_batch_raster<32, 16, 256>(w, plan, tile_offsets, tile_triangles, capacity,
-                                                            attribute_count, cull_mode, address_mode, s);
-    else e = launch_batch_raster<32, 16, 512>(w, plan, tile_offsets, tile_triangles, capacity, attribute_count,
+    else e = launch_batch_raster<16, 16, 256>(w, plan, tile_offsets, tile_triangles, capacity, attribute_count,
                                               cull_mode, address_mode, s);
     return set_cuda_error(e, "render_batch_forward");
 }

@@ -16,7 +16,12 @@ struct TriRect {
     uint32_t y;  // ty0 | ty1 << 16
 };
 
-// src/rasterizer.cpp:73-125 for one triangle: pixel bounding box of the NDC bounds, clamped.
+// src/rasterizer.cpp:73-125 for one triangle: pixel bounding box of the NDC bounds, clamped, in the
+// reference's 16 x 16 tiles. Which tiles list a triangle decides which pixels it can cover (a sample that
+// passes the edge tests inside their 1e-7 tolerance may lie outside the triangle's pixel box, and the
+// reference tests it when its 16 x 16 tile lists the triangle), so smaller tiles (tile_w, tile_h dividing
+// 16) list a triangle in every sub-tile of the 16 x 16 tiles the reference lists it in: the set of
+// (triangle, pixel) pairs tested is the reference's for every tile shape.
 __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__ pos, const uint3 vi,
                                                       uint32_t W, uint32_t H, float4 vp, uint32_t tile_w = kTile,
                                                       uint32_t tile_h = kTile) {
@@ -45,8 +50,10 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
     const uint32_t x1 = (uint32_t)(px1 < 0 ? 0 : (px1 > wm ? wm : px1));
     const uint32_t y0 = (uint32_t)(py0 < 0 ? 0 : (py0 > hm ? hm : py0));
     const uint32_t y1 = (uint32_t)(py1 < 0 ? 0 : (py1 > hm ? hm : py1));
-    r.x = (x0 / tile_w) | ((x1 / tile_w) << 16);
-    r.y = (y0 / tile_h) | ((y1 / tile_h) << 16);
+    const uint32_t sx = kTile / tile_w, sy = kTile / tile_h;  // sub-tiles per reference tile
+    const uint32_t tx_last = (W + tile_w - 1) / tile_w - 1, ty_last = (H + tile_h - 1) / tile_h - 1;
+    r.x = (x0 / kTile * sx) | (min((x1 / kTile + 1) * sx - 1, tx_last) << 16);
+    r.y = (y0 / kTile * sy) | (min((y1 / kTile + 1) * sy - 1, ty_last) << 16);
     return r;
 }
 

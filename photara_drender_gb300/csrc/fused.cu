@@ -151,8 +151,7 @@ pdr_status check_render_forward(const pdr_render_args* a) {
         return set_error(PDR_INVALID_ARGUMENT, "texture sampling needs uv attributes and uv/sampled outputs");
     const TileConfig tc = tile_config(a);
     if (!raster_config_supported(tc.w, tc.h, tc.k))
-        return set_error(PDR_INVALID_ARGUMENT, "tile shape and stage depth must be 16x16/256, 16x16/128, 16x8/128 or "
-                                               "32x8/256");
+        return set_error(PDR_INVALID_ARGUMENT, "tile shape and stage depth must be 16x16/256, 16x16/128 or 16x8/128");
     const uint64_t tiles = (uint64_t)((a->width + tc.w - 1) / tc.w) * ((a->height + tc.h - 1) / tc.h);
     if (tiles * a->views >= 0x7fffffffull || (uint64_t)a->triangle_count * a->views >= 0x7fffffffull)
         return set_error(PDR_OVERFLOW, "Rasterization output size overflow");

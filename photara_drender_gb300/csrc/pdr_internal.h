@@ -55,7 +55,7 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
                                   const RasterShade* shade = nullptr, const uint32_t* status = nullptr,
                                   uint32_t tile_w = 16, uint32_t tile_h = 16, uint32_t chunk = 256);
 // Tile shapes and stage depths the raster kernels are compiled for: 16x16 with 256 or 128 staged
-// triangles, 16x8 with 128, 32x8 with 256.
+// triangles, 16x8 with 128 (shapes that divide the reference's 16x16 tile: triangle_tile_rect).
 bool raster_config_supported(uint32_t tile_w, uint32_t tile_h, uint32_t chunk);
 
 cudaError_t launch_raster_backward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,

@@ -593,8 +593,7 @@ cudaError_t launch_raster_config(const float4* c4, uint32_t views, uint32_t V, c
 }  // namespace
 
 bool raster_config_supported(uint32_t tile_w, uint32_t tile_h, uint32_t chunk) {
-    return (tile_w == 16 && tile_h == 16 && (chunk == 256 || chunk == 128)) ||
-           (tile_w == 16 && tile_h == 8 && chunk == 128) || (tile_w == 32 && tile_h == 8 && chunk == 256);
+    return (tile_w == 16 && tile_h == 16 && (chunk == 256 || chunk == 128)) || (tile_w == 16 && tile_h == 8 && chunk == 128);
 }
 
 cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V, const uint32_t* idx, uint32_t T,
@@ -630,9 +629,6 @@ cudaError_t launch_raster_forward(const float* clip, uint32_t views, uint32_t V,
                                                  sa, sh, status, stream);
     if (tile_w == 16 && tile_h == 8 && chunk == 128)
         return launch_raster_config<16, 8, 128>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
-                                                sa, sh, status, stream);
-    if (tile_w == 32 && tile_h == 8 && chunk == 256)
-        return launch_raster_config<32, 8, 256>(c4, views, V, i3, T, W, H, v4, cull, offsets, list, capacity, r4, d4,
                                                 sa, sh, status, stream);
     return cudaErrorInvalidValue;
 }

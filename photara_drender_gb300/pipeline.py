@@ -37,7 +37,7 @@ class RenderArgsC(C.Structure):
 
 # Tile shapes and stage depths of the fused render (pdr_render_args.tile_width / tile_height /
 # stage_triangles): the raster kernels are compiled for these.
-TILE_CONFIGS = ((16, 16, 256), (16, 16, 128), (16, 8, 128), (32, 8, 256))
+TILE_CONFIGS = ((16, 16, 256), (16, 16, 128), (16, 8, 128))
 
 
 class RenderFwdBwd:
