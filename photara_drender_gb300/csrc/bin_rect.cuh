@@ -52,8 +52,43 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
     const uint32_t y1 = (uint32_t)(py1 < 0 ? 0 : (py1 > hm ? hm : py1));
     const uint32_t sx = kTile / tile_w, sy = kTile / tile_h;  // sub-tiles per reference tile
     const uint32_t tx_last = (W + tile_w - 1) / tile_w - 1, ty_last = (H + tile_h - 1) / tile_h - 1;
-    r.x = (x0 / kTile * sx) | (min((x1 / kTile + 1) * sx - 1, tx_last) << 16);
-    r.y = (y0 / kTile * sy) | (min((y1 / kTile + 1) * sy - 1, ty_last) << 16);
+    uint32_t rx0 = x0 / kTile * sx, rx1 = min((x1 / kTile + 1) * sx - 1, tx_last);
+    uint32_t ry0 = y0 / kTile * sy, ry1 = min((y1 / kTile + 1) * sy - 1, ty_last);
+    if (sx > 1 || sy > 1) {
+        // Sub-tiles that no sample passing the edge tests can reach are left out. The raster's candidate
+        // rectangle (raster_tile.cuh pixel_rect) reaches from its first row ceil(c - D' - 0.5 - s) to its
+        // last floor(c' + D' - 0.5 + s) (c, c' the box's edges in pixels, D' its bound D in pixels, s its
+        // slack 0.05 + 1e-6 S, S the viewport size plus offset), each within 4e-7 S of exact, against the
+        // pixel box's floor(c) .. ceil(c') - 1: with D' <= 1 it stays within the box grown by one pixel
+        // while 0.05 + 1.8e-6 S < 0.5 (S <= 1e5), by two pixels while S <= 5e5. D grows with the largest
+        // distance L between a vertex and a sample of the tile, so D computed here with L over the whole
+        // reference-tile rectangle bounds D in every sub-tile of it.
+        const float4 p0 = pos[v[0]], p1 = pos[v[1]], p2 = pos[v[2]];
+        const float s0x = p0.x / p0.w, s0y = p0.y / p0.w, s1x = p1.x / p1.w, s1y = p1.y / p1.w;
+        const float s2x = p2.x / p2.w, s2y = p2.y / p2.w;
+        const float area = (s1x - s0x) * (s2y - s0y) - (s1y - s0y) * (s2x - s0x);
+        const float tsx_lo = sample_ndc(x0 / kTile * kTile, vp.x, vp.z);
+        const float tsx_hi = sample_ndc(min(x1 / kTile * kTile + kTile - 1, W - 1), vp.x, vp.z);
+        const float tsy_lo = sample_ndc(y0 / kTile * kTile, vp.y, vp.w);
+        const float tsy_hi = sample_ndc(min(y1 / kTile * kTile + kTile - 1, H - 1), vp.y, vp.w);
+        const float L = 1.01f * fmaxf(fmaxf(fabsf(max_x - tsx_lo), fabsf(tsx_hi - min_x)),
+                                      fmaxf(fabsf(max_y - tsy_lo), fabsf(tsy_hi - min_y)));
+        const float perim = fabsf(s1x - s0x) + fabsf(s1y - s0y) + fabsf(s2x - s1x) + fabsf(s2y - s1y) +
+                            fabsf(s0x - s2x) + fabsf(s0y - s2y);
+        const float D = 2.0f * (1e-7f + 2e-6f * L * L) * perim / fabsf(area);
+        const float ext = fmaxf(max_x - min_x, max_y - min_y);
+        const float S = fmaxf(vp.z + fabsf(vp.x), vp.w + fabsf(vp.y));
+        const bool bounded = D <= fminf(2.0f / vp.z, 2.0f / vp.w) && fabsf(area) >= 1e-4f * ext * ext && S <= 5e5f;
+        if (bounded) {
+            const uint32_t m = S <= 1e5f ? 1u : 2u;
+            rx0 = max(rx0, (x0 < m ? 0u : x0 - m) / tile_w);
+            rx1 = min(rx1, min(x1 + m, (uint32_t)wm) / tile_w);
+            ry0 = max(ry0, (y0 < m ? 0u : y0 - m) / tile_h);
+            ry1 = min(ry1, min(y1 + m, (uint32_t)hm) / tile_h);
+        }
+    }
+    r.x = rx0 | (rx1 << 16);
+    r.y = ry0 | (ry1 << 16);
     return r;
 }
 
