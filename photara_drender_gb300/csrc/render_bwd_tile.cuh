@@ -311,6 +311,22 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
     for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (uint32_t j = 0; j < kNV; ++j) cv[k][j] = scan.sum(cv[k][j]);
+    if (v.g_vtx) {
+        // A warp covers two tile rows, so a triangle usually ends a run in each: the second run's sums move
+        // to the first run's tail (one shuffle per value) and one tail adds them.
+        const bool tail = valid && scan.tail;
+        const unsigned same = __match_any_sync(0xffffffffu, tail ? id : (0x80000000u | lane));
+        const bool pair = tail && __popc(same) == 2;
+        const uint32_t partner = pair ? (uint32_t)(__ffs(same & ~(1u << lane)) - 1) : lane;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (uint32_t j = 0; j < kNV; ++j) {
+                const float o = __shfl_sync(0xffffffffu, cv[k][j], partner);
+                if (pair && partner > lane) cv[k][j] += o;
+            }
+        if (pair && partner < lane) valid = false;  // its sums went to the first tail
+    }
     if (valid && scan.tail && v.g_vtx) {
         // one record per vertex and view: kNV values in 16-byte reductions (two for up to three attributes,
         // against five reductions into the shared uv / attribute rows and the clip row otherwise)
