@@ -28,6 +28,7 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
     TriRect r{kNoRect, 0};
     float min_x = INFINITY, min_y = INFINITY, max_x = -INFINITY, max_y = -INFINITY;
     const uint32_t v[3] = {vi.x, vi.y, vi.z};
+    float sx_[3], sy_[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float4 p = pos[v[c]];
@@ -35,6 +36,8 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
         const float x = p.x / p.w;
         const float y = p.y / p.w;
         if (!isfinite(x) || !isfinite(y)) return r;
+        sx_[c] = x;
+        sy_[c] = y;
         min_x = x < min_x ? x : min_x;
         min_y = y < min_y ? y : min_y;
         max_x = max_x < x ? x : max_x;
@@ -63,14 +66,16 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
         // while 0.05 + 1.8e-6 S < 0.5 (S <= 1e5), by two pixels while S <= 5e5. D grows with the largest
         // distance L between a vertex and a sample of the tile, so D computed here with L over the whole
         // reference-tile rectangle bounds D in every sub-tile of it.
-        const float4 p0 = pos[v[0]], p1 = pos[v[1]], p2 = pos[v[2]];
-        const float s0x = p0.x / p0.w, s0y = p0.y / p0.w, s1x = p1.x / p1.w, s1y = p1.y / p1.w;
-        const float s2x = p2.x / p2.w, s2y = p2.y / p2.w;
+        const float s0x = sx_[0], s0y = sy_[0], s1x = sx_[1], s1y = sy_[1], s2x = sx_[2], s2y = sy_[2];
         const float area = (s1x - s0x) * (s2y - s0y) - (s1y - s0y) * (s2x - s0x);
-        const float tsx_lo = sample_ndc(x0 / kTile * kTile, vp.x, vp.z);
-        const float tsx_hi = sample_ndc(min(x1 / kTile * kTile + kTile - 1, W - 1), vp.x, vp.z);
-        const float tsy_lo = sample_ndc(y0 / kTile * kTile, vp.y, vp.w);
-        const float tsy_hi = sample_ndc(min(y1 / kTile * kTile + kTile - 1, H - 1), vp.y, vp.w);
+        // sample positions of the reference-tile rectangle's first and last column and row, from one
+        // reciprocal per axis instead of sample_ndc's division, widened by 1e-5 (far more than the few
+        // roundings by which they can differ) so that the range holds every sample the raster uses
+        const float ix = 2.0f / vp.z, iy = 2.0f / vp.w;
+        const float tsx_lo = ((float)(x0 / kTile * kTile) - vp.x + 0.5f) * ix - 1.0f - 1e-5f;
+        const float tsx_hi = ((float)min(x1 / kTile * kTile + kTile - 1, W - 1) - vp.x + 0.5f) * ix - 1.0f + 1e-5f;
+        const float tsy_lo = ((float)(y0 / kTile * kTile) - vp.y + 0.5f) * iy - 1.0f - 1e-5f;
+        const float tsy_hi = ((float)min(y1 / kTile * kTile + kTile - 1, H - 1) - vp.y + 0.5f) * iy - 1.0f + 1e-5f;
         const float L = 1.01f * fmaxf(fmaxf(fabsf(max_x - tsx_lo), fabsf(tsx_hi - min_x)),
                                       fmaxf(fabsf(max_y - tsy_lo), fabsf(tsy_hi - min_y)));
         const float perim = fabsf(s1x - s0x) + fabsf(s1y - s0y) + fabsf(s2x - s1x) + fabsf(s2y - s1y) +
@@ -78,7 +83,7 @@ __device__ __forceinline__ TriRect triangle_tile_rect(const float4* __restrict__
         const float D = 2.0f * (1e-7f + 2e-6f * L * L) * perim / fabsf(area);
         const float ext = fmaxf(max_x - min_x, max_y - min_y);
         const float S = fmaxf(vp.z + fabsf(vp.x), vp.w + fabsf(vp.y));
-        const bool bounded = D <= fminf(2.0f / vp.z, 2.0f / vp.w) && fabsf(area) >= 1e-4f * ext * ext && S <= 5e5f;
+        const bool bounded = D <= fminf(ix, iy) && fabsf(area) >= 1e-4f * ext * ext && S <= 5e5f;
         if (bounded) {
             const uint32_t m = S <= 1e5f ? 1u : 2u;
             rx0 = max(rx0, (x0 < m ? 0u : x0 - m) / tile_w);
