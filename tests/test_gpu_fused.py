@@ -202,3 +202,48 @@ def test_tile_configurations_give_identical_outputs():
     p.forward(clip, attrs, uva, tex, stream)
     torch.cuda.synchronize()
     assert p.check_capacity() > 0 and torch.equal(p.raster.view(torch.int32), ref[0].view(torch.int32))
+
+
+@pytest.mark.parametrize("attributes", [3, 8, 0])
+def test_backward_with_and_without_vertex_records(attributes):
+    """pdr_render_backward with a workspace of pdr_render_backward_workspace_bytes() (per-view vertex
+    records, summed over the views by a second pass) and without one (reductions straight into the
+    outputs): every gradient agrees to float rounding, the texture gradient (the same reductions both
+    ways) included."""
+    from photara_drender_gb300 import Rasterizer, _native
+    from photara_drender_gb300.pipeline import RenderFwdBwd
+
+    rng = np.random.default_rng(7)
+    pos3, idx = S.icosphere(3)
+    mats, _ = S.orbit_cameras(3)
+    clip = S.clip_positions(pos3, mats)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)  # noqa: E731
+    V, H, W = pos3.shape[0], 96, 112
+    A = max(attributes, 1)
+    p = RenderFwdBwd(Rasterizer(0), torch.tensor(idx.astype(np.int32)), V, 3, H, W, A, (64, 48, 4))
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    args = [t(clip), t(rng.uniform(size=(V, A)).astype(np.float32)), t(S.spherical_uv(pos3).astype(np.float32)),
+            t(rng.uniform(size=(64, 48, 4)).astype(np.float32))]
+    g_attr = t(rng.standard_normal((3, H, W, A)).astype(np.float32))
+    g_samp = t(rng.standard_normal((3, H, W, 4)).astype(np.float32))
+    p.forward(*args, stream)
+    L = _native.lib()
+    res = []
+    for records in (True, False):
+        a = p._args(*args, g_attr, g_samp)
+        if not attributes:
+            a.attributes, a.attribute_count, a.grad_attributes, a.grad_interpolated = None, 0, None, None
+        if not records:
+            a.workspace, a.workspace_bytes = None, 0
+        else:
+            assert a.workspace_bytes >= L.pdr_render_backward_workspace_bytes(3, V, attributes)
+        _native.check(L.pdr_render_backward(C.addressof(a), stream))
+        torch.cuda.synchronize()
+        res.append({k: getattr(p, k).cpu().numpy().copy() for k in ("grad_tex", "grad_uv_attr", "grad_clip")
+                    + (("grad_attr",) if attributes else ())})
+    for k, want in res[1].items():
+        got = res[0][k]
+        scale = np.abs(want).max()
+        assert scale > 0, k
+        assert np.allclose(got, want, rtol=1e-5, atol=1e-6 * scale), (k, np.abs(got - want).max(), scale)
