@@ -170,13 +170,16 @@ class TextureBaker:
             n = len(ks)
             sub = clip[ks].contiguous()
             vps, _ = _viewports([viewports[k] for k in ks], n, w, h, ctx.device)
-            tiles = ((w + 15) // 16) * ((h + 15) // 16)
+            # 16x8 tiles with 128 staged triangles: the fused render's fastest shape on the bake's meshes and
+            # views (the autotuner's pick for the 200k-triangle views); outputs are the same for every shape
+            tw_, th_, stage = 16, 8, 128
+            tiles = ((w + tw_ - 1) // tw_) * ((h + th_ - 1) // th_)
             # four tiles per triangle plus one entry per tile covers meshes of small triangles; a larger need
             # costs time on the first call only (the count then sizes later calls)
             capacity = max(getattr(self, "_raster_capacity", 0), 4 * T * n + tiles * n + 1024)
             offsets = torch.empty(n * tiles + 1, dtype=torch.int32, device=ctx.device)
             lst = torch.empty(capacity, dtype=torch.int32, device=ctx.device)
-            ws_bytes = L.pdr_render_workspace_bytes(n, T, w, h, capacity)
+            ws_bytes = L.pdr_render_workspace_bytes_tiled(n, T, w, h, capacity, tw_, th_)
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=ctx.device)
             raster = torch.empty((n, h, w, 4), dtype=torch.float32, device=ctx.device)
             a = RenderArgsC()
@@ -185,6 +188,7 @@ class TextureBaker:
             a.viewports, a.raster = vps.data_ptr(), raster.data_ptr()
             a.tile_offsets, a.tile_triangles, a.capacity = offsets.data_ptr(), lst.data_ptr(), capacity
             a.workspace, a.workspace_bytes, a.status = ws.data_ptr(), ws_bytes, ctx.status.data_ptr()
+            a.tile_width, a.tile_height, a.stage_triangles = tw_, th_, stage
             ctx.status.zero_()
             _native.check(L.pdr_render_forward(C.addressof(a), ctx.stream()))
             ctx.defer_status("bake_raster")
