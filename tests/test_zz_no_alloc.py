@@ -77,3 +77,65 @@ def test_no_alloc_binning_matches_workspace_binning():
     with pytest.raises(ValueError, match="scratch"):
         _native.check(fn(p(clip), views, V, p(tidx), T, W, H, p(vps), p(ref_off), p(big_list), huge, p(ref_status),
                          stream))
+
+
+def test_no_alloc_binning_inside_a_graph_capture():
+    """The use case the entry point exists for: after a first call outside any capture (which looks the
+    scratch array's device address up), a call recorded into someone else's CUDA graph (memset and
+    kernels only) replays to the bins a workspace call gives, twice in a row."""
+    import torch
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300 import synthetic as S
+
+    L = _native.lib()
+    fn = L.pdr_bin_tiles_no_alloc
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
+    dev = torch.device("cuda", 0)
+    pos3, idx = S.icosphere(3)
+    mats, _ = S.orbit_cameras(2)
+    clip = torch.tensor(S.clip_positions(pos3, mats), device=dev)
+    tidx = torch.tensor(idx.astype(np.int32), device=dev)
+    views, V, T, H, W = 2, pos3.shape[0], idx.shape[0], 96, 80
+    vps = torch.tensor([[0.0, 0.0, W, H]] * views, dtype=torch.float32, device=dev)
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    capacity = 8 * T
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def outputs():
+        return (torch.full((views * tiles + 1,), -1, dtype=torch.int32, device=dev),
+                torch.full((capacity,), -1, dtype=torch.int32, device=dev),
+                torch.zeros(_native.STATUS_WORDS, dtype=torch.int32, device=dev))
+
+    ref_off, ref_list, ref_status = outputs()
+    ws_bytes = L.pdr_bin_tiles_workspace_bytes(views, T, W, H, capacity)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    _native.check(L.pdr_bin_tiles(p(clip), views, V, p(tidx), T, W, H, p(vps), p(ref_off), p(ref_list), capacity,
+                                  p(ws), ws_bytes, p(ref_status), stream))
+    off, lst, status = outputs()
+    _native.check(fn(p(clip), views, V, p(tidx), T, W, H, p(vps), p(off), p(lst), capacity, p(status), stream))
+    torch.cuda.synchronize()
+    total = int(ref_status[0])
+    assert total > 0
+
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    graph = torch.cuda.CUDAGraph()
+    off.fill_(-1)
+    lst.fill_(-1)
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        cap = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        _native.check(fn(p(clip), views, V, p(tidx), T, W, H, p(vps), p(off), p(lst), capacity, p(status), cap))
+    for _ in range(2):
+        off.fill_(-1)
+        lst.fill_(-1)
+        status.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(off, ref_off)
+        assert torch.equal(lst[:total], ref_list[:total])
+        assert int(status[0]) == total and int(status[2]) == 0
