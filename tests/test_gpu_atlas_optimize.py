@@ -76,7 +76,7 @@ def reference_loop_f64(init, uvs, rasters, targets, masks, valid, charts, pairs,
         opt.step()
         with torch.no_grad():
             param.clamp_(o.clamp_min, o.clamp_max)
-        history.append(float(loss))
+        history.append(float(loss.detach()))
     return param.detach(), history
 
 
