@@ -204,9 +204,11 @@ class RenderFwdBwd:
 
     def kernels_per_step(self) -> int:
         """Kernels one step launches: binning (count, three scan phases, fill; the unfused path also
-        sorts each tile, two passes), then fused: raster with the shading epilogue + one backward;
-        unfused: raster, three forwards, texture backward, two interpolate backwards, raster backward."""
-        return 5 + 1 + 1 if self.fused else 5 + 2 + 1 + 3 + 1 + 2 + 1
+        sorts each tile, two passes), the raster (the main launch and the pass over tiles whose lists were
+        cut), then fused: the shading is the raster's epilogue and the backward is the adjoint plus the pass
+        that sums its per-view vertex records; unfused: three forwards, texture backward, two interpolate
+        backwards, raster backward."""
+        return 5 + 2 + 2 if self.fused else 5 + 2 + 2 + 3 + 1 + 2 + 1
 
     def capture(self, clip, attrs, uv_attrs, texture, grad_attr_out, grad_sampled) -> "torch.cuda.CUDAGraph":
         """Records one step into a CUDA graph (replay with .replay()); for small, launch-bound batches.
