@@ -219,7 +219,11 @@ __device__ __forceinline__ void red_add_v4_texel(float* addr, float4 v, bool agg
         red_add_v4_aggregated(addr, v);
         return;
     }
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+    // evict-last priority in L2: a texel's gradient line is hit again by the next views' pixels
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile("red.global.add.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(addr), "f"(v.x), "f"(v.y),
+                 "f"(v.z), "f"(v.w), "l"(pol)
                  : "memory");
 }
 #endif
