@@ -22,7 +22,7 @@ namespace pdr {
 namespace {
 
 template <int kA, int kTexAgg>
-__global__ void __launch_bounds__(kFusedThreads, 5)
+__global__ void __launch_bounds__(kFusedThreads, 6)  // 40 registers (a few spills): 48 warps per SM
 render_backward_kernel(const float4* __restrict__ clip_all, uint32_t V, const uint3* __restrict__ idx, uint32_t T,
                        uint32_t W, uint32_t H, const float4* __restrict__ viewports, uint32_t tcx,
                        const float* __restrict__ attrs, const float2* __restrict__ uv_attrs,
