@@ -27,7 +27,8 @@ constexpr uint32_t kWindowBits = 8192 * 32;  // id window of the large-tile bitm
 
 // Pass 1: per (view, triangle) tile rectangle and per-tile counts (warp-aggregated when the
 // lanes of a warp land in the same single tile).
-__global__ void __launch_bounds__(256, 6) bin_count_kernel(const float4* __restrict__ clip, uint32_t V, const uint3* __restrict__ idx,
+__global__ void __launch_bounds__(256, 6)  // 40 registers: 48 warps per SM for the gathers and atomics
+bin_count_kernel(const float4* __restrict__ clip, uint32_t V, const uint3* __restrict__ idx,
                                  uint32_t T, uint32_t W, uint32_t H, const float4* __restrict__ viewports,
                                  uint32_t tcx, uint32_t tiles, TriRect* __restrict__ rects,
                                  uint32_t* __restrict__ counts, uint32_t tile_w, uint32_t tile_h) {
