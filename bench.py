@@ -886,11 +886,11 @@ KERNEL_SOURCES = {
 # bytes per launch); from `ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum`
 # on the full 64-view run (profiles/launch_list_fwdbwd_200k_64x1024sq.md)
 KERNEL_TRAFFIC = {
-    "bin_tiles": ((16, 8, 128), "18dfd3efbbc7b5b3",
-                  108500480 + 66192640 + 2103296 + 7168 + 2103040 + 104333568 + 55572224),
-    "rasterize_forward+shade": ((16, 8, 128), "9ef58eb2aa439a97", 2228738816 + 5732511232),
+    "bin_tiles": ((16, 8, 128), "ed20208abe26a4d1",
+                  108488192 + 67244288 + 2103296 + 11520 + 2103296 + 104388608 + 55637760),
+    "rasterize_forward+shade": ((16, 8, 128), "8e087469c7d9c88e", 2228451840 + 5732461824),
     # the adjoint kernel and the finishing pass over the per-view vertex records
-    "render_backward": (None, "9e07127dcd2ef834", 5515164928 + 1182292992 + 208687360 + 45270016),
+    "render_backward": (None, "deb36df30e237d9f", 5652964096 + 1178972928 + 208677632 + 45262336),
 }
 
 
