@@ -230,7 +230,8 @@ __global__ void adam_kernel(float* __restrict__ tex, float* __restrict__ grad, f
 // the Adam update of adam_kernel into tex_out: one pass over the atlas for a step with total variation.
 // tex_in and tex_out are different buffers, so every texel reads its neighbours' values from before the
 // step, as the separate TV pass does. Bit-identical to tv_kernel followed by adam_kernel.
-__global__ void adam_tv_kernel(const float* __restrict__ tex_in, float* __restrict__ tex_out,
+__global__ void __launch_bounds__(256, 8)  // 32 registers: full occupancy for the streaming pass
+adam_tv_kernel(const float* __restrict__ tex_in, float* __restrict__ tex_out,
                                float* __restrict__ grad, float* __restrict__ m1, float* __restrict__ m2,
                                uint32_t tw, uint32_t th, const uint8_t* __restrict__ valid,
                                const int32_t* __restrict__ chart, float tv_eps, float tv_scale, float lr, float b1,
