@@ -93,7 +93,7 @@ __device__ __forceinline__ float block_sum(float v) {
 
 // One launch covers the batch views of one step (blockIdx.y = batch slot); view choice follows
 // texture_refiner.cpp:318-340: view = (step * batch + slot) % view_count.
-__global__ void __launch_bounds__(kPhotoThreads)
+__global__ void __launch_bounds__(kPhotoThreads, 8)  // 32 registers: full occupancy
 photometric_kernel(const float* __restrict__ tex, uint32_t tw, uint32_t th, const pdr_refine_view* __restrict__ views,
                    uint32_t nviews, uint32_t step, uint32_t batch, float eps, float norm, float* __restrict__ grad,
                    float* __restrict__ loss) {
