@@ -94,7 +94,8 @@ __device__ __forceinline__ float shadow_visibility(const pdr_projection_view& v,
 constexpr uint32_t kViewChunk = 32;
 static_assert(sizeof(pdr_projection_view) % sizeof(uint4) == 0, "view records are copied as 16-byte words");
 
-__global__ void project_views_kernel(const float* __restrict__ apos, const float* __restrict__ anrm,
+__global__ void __launch_bounds__(128, 12)  // 40 registers: 48 warps per SM for the gathers
+project_views_kernel(const float* __restrict__ apos, const float* __restrict__ anrm,
                                      const float4* __restrict__ araster, uint32_t N,
                                      const pdr_projection_view* __restrict__ views, uint32_t nviews,
                                      uint32_t blend_mode, uint32_t pcf_radius, uint32_t visibility_mode,
