@@ -1,8 +1,9 @@
 """The raster forward's per-triangle candidate rectangle (photara_drender_gb300/csrc/raster_tile.cuh
 pixel_rect) must contain every pixel of the tile whose sample passes the reference's edge tests
 (rasterize_forward.hlsl: fl(cross(a - s, b - s)) * sign >= -1e-7 for the three edges), or else decline
-(the kernel then enumerates the whole tile); and on 16x8 tiles the per-row spans cut from the rectangle
-(raster_tile.cuh row_spans) must contain every such pixel of their row. Restated here in NumPy float32,
+(the kernel then enumerates the whole tile); on 16x8 tiles the per-row spans cut from the rectangle
+(raster_tile.cuh row_spans) must contain every such pixel of their row; and the 16x8 binning
+(bin_rect.cuh triangle_tile_rect) may leave out only sub-tiles none of whose pixels pass. Restated here in NumPy float32,
 operation by operation, and checked against brute-force edge tests over whole tiles on triangles of
 every scale: microscopic ones (whose tolerance reaches beyond their bounding box), slivers, large ones
 crossing the tile, vertices on the sample lattice, and odd viewports."""
@@ -208,3 +209,74 @@ def test_row_spans_contain_every_covered_pixel():
             rect_total += int((((x1 - x0 + 1) * (y1 - y0 + 1)) * use).sum())
     print(f"\nrow spans: {spans_total} candidates, rectangles: {rect_total}")
     assert spans_total < 0.8 * rect_total, (spans_total, rect_total)
+
+
+def subtile_rows(s, area, vp, W, H):
+    """NumPy float32 restatement of bin_rect.cuh triangle_tile_rect's row range for 16x8 sub-tiles: the
+    reference's 16x16 rows expanded to sub-tile rows, then (when the bound holds) cut to the pixel box
+    grown by one or two pixels. Returns (ref_row0, ref_row1, row0, row1) in 8-row sub-tiles."""
+    vp = [f(v) for v in vp]
+    sx, sy = s[..., 0], s[..., 1]
+    min_x, max_x = sx.min(1), sx.max(1)
+    min_y, max_y = sy.min(1), sy.max(1)
+    px0 = np.floor((min_x * f(0.5) + f(0.5)) * vp[2] + vp[0]).astype(np.int64)
+    px1 = np.ceil((max_x * f(0.5) + f(0.5)) * vp[2] + vp[0]).astype(np.int64) - 1
+    py0 = np.floor((min_y * f(0.5) + f(0.5)) * vp[3] + vp[1]).astype(np.int64)
+    py1 = np.ceil((max_y * f(0.5) + f(0.5)) * vp[3] + vp[1]).astype(np.int64) - 1
+    x0, x1 = np.clip(px0, 0, W - 1), np.clip(px1, 0, W - 1)
+    y0, y1 = np.clip(py0, 0, H - 1), np.clip(py1, 0, H - 1)
+    ty_last = (H + 7) // 8 - 1
+    ry0, ry1 = y0 // 16 * 2, np.minimum((y1 // 16 + 1) * 2 - 1, ty_last)
+    ix, iy = f(2.0) / vp[2], f(2.0) / vp[3]
+    tsx_lo = ((x0 // 16 * 16).astype(np.float32) - vp[0] + f(0.5)) * ix - f(1.0) - f(1e-5)
+    tsx_hi = (np.minimum(x1 // 16 * 16 + 15, W - 1).astype(np.float32) - vp[0] + f(0.5)) * ix - f(1.0) + f(1e-5)
+    tsy_lo = ((y0 // 16 * 16).astype(np.float32) - vp[1] + f(0.5)) * iy - f(1.0) - f(1e-5)
+    tsy_hi = (np.minimum(y1 // 16 * 16 + 15, H - 1).astype(np.float32) - vp[1] + f(0.5)) * iy - f(1.0) + f(1e-5)
+    L = f(1.01) * np.fmax(np.fmax(np.abs(max_x - tsx_lo), np.abs(tsx_hi - min_x)),
+                          np.fmax(np.abs(max_y - tsy_lo), np.abs(tsy_hi - min_y)))
+    perim = (np.abs(sx[:, 1] - sx[:, 0]) + np.abs(sy[:, 1] - sy[:, 0]) + np.abs(sx[:, 2] - sx[:, 1]) +
+             np.abs(sy[:, 2] - sy[:, 1]) + np.abs(sx[:, 0] - sx[:, 2]) + np.abs(sy[:, 0] - sy[:, 2]))
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        D = f(2.0) * (f(1e-7) + f(2e-6) * L * L) * perim / np.abs(area)
+    ext = np.fmax(max_x - min_x, max_y - min_y)
+    S = max(vp[2] + abs(vp[0]), vp[3] + abs(vp[1]))
+    bounded = (D <= np.fmin(ix, iy)) & (np.abs(area) >= f(1e-4) * ext * ext) & (S <= f(5e5))
+    m = 1 if S <= 1e5 else 2
+    row0 = np.where(bounded, np.maximum(ry0, np.maximum(y0 - m, 0) // 8), ry0)
+    row1 = np.where(bounded, np.minimum(ry1, np.minimum(y1 + m, H - 1) // 8), ry1)
+    inside = ~((max_x < -1) | (min_x > 1) | (max_y < -1) | (min_y > 1))
+    return ry0, ry1, row0, row1, x0 // 16, x1 // 16, inside
+
+
+def test_subtile_binning_leaves_out_only_unreachable_subtiles():
+    """16x8 binning lists a triangle in the 8-row sub-tiles of the reference's 16x16 tiles, minus those the
+    pixel box grown by one pixel (two for very large viewports) does not reach when the candidate
+    rectangle's bound holds over the whole reference-tile rectangle. Every sub-tile left out is checked
+    by brute force: no pixel of it passes the triangle's edge tests, so the (triangle, pixel) pairs tested
+    stay the reference's."""
+    rng = np.random.default_rng(14)
+    left_out = 0
+    for vp in [(0.0, 0.0, 64.0, 64.0), (-3.0, 2.5, 75.0, 58.0), (0.0, 0.0, 1024.0, 1024.0)]:
+        W, H = int(vp[2]), int(vp[3])
+        s = triangles(rng, 300)
+        # also triangles in random places of the image, not only around one tile
+        s = np.concatenate([s, (s + rng.uniform(-0.8, 0.8, size=(len(s), 1, 2))).astype(np.float32)])
+        lat = rng.uniform(size=s.shape[:2]) < 0.2
+        k = np.round((s[..., 0] + 1) * 0.5 * vp[2] + vp[0] - 0.5)
+        s[..., 0] = np.where(lat, sample_ndc(k, vp[0], vp[2]), s[..., 0])
+        area = ((s[:, 1, 0] - s[:, 0, 0]) * (s[:, 2, 1] - s[:, 0, 1]) -
+                (s[:, 1, 1] - s[:, 0, 1]) * (s[:, 2, 0] - s[:, 0, 0])).astype(np.float32)
+        keep = ~(np.abs(area) <= f(1e-12))
+        s, area = s[keep], area[keep]
+        sign = np.where(area > 0, f(1.0), f(-1.0))
+        ry0, ry1, row0, row1, tx0, tx1, inside = subtile_rows(s, area, vp, W, H)
+        for i in np.nonzero(inside)[0]:
+            rows = [r for r in range(int(ry0[i]), int(ry1[i]) + 1) if r < row0[i] or r > row1[i]]
+            if not rows:
+                continue
+            px, py = np.meshgrid(np.arange(int(tx0[i]) * 16, min(int(tx1[i]) * 16 + 16, W)),
+                                 np.concatenate([np.arange(r * 8, min(r * 8 + 8, H)) for r in rows]))
+            cov = covered(s[i:i + 1], sign[i:i + 1], px.reshape(-1), py.reshape(-1), vp)
+            assert not cov.any(), (vp, i, rows)
+            left_out += len(rows)
+    assert left_out > 100  # the narrowing is exercised
