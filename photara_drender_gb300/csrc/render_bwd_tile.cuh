@@ -1,6 +1,7 @@
 // The fused adjoint of rasterize -> interpolate(attributes), interpolate(uv) -> texture for the
-// pixels of one 16x16 tile of one view; shared by the per-mesh launch (fused.cu) and the uneven
-// multi-mesh batch (batch.cu). The kernel that calls render_backward_tile runs 256 threads.
+// pixels of one 16 x kTH tile of one view; shared by the per-mesh launch (fused.cu, 16x8 tiles) and the
+// uneven multi-mesh batch (batch.cu, 16x16). The kernel that calls render_backward_tile runs 16 * kTH
+// threads, each warp on two tile rows.
 //
 // One thread per pixel runs, in the reference's order and arithmetic, texture_grad_texture
 // (double-exact weights, vector atomics, warp-aggregated for magnified textures), texture_grad_uv,
@@ -105,7 +106,7 @@ __host__ __device__ constexpr uint32_t vertex_record_floats(int kA) { return (ui
 
 // kTexAgg: texture-gradient taps warp-aggregated (1), plain (0), or decided from the texture and image
 // sizes (-1: aggregated when the texture has fewer texels than the view has pixels).
-template <int kA, int kTexAgg = -1>
+template <int kA, int kTexAgg = -1, int kTH = kTile>
 __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint32_t tile_x, uint32_t tile_y) {
     const float4* __restrict__ clip_view = v.clip;
     const uint32_t V = v.V, T = v.T, W = v.W, H = v.H;
@@ -130,7 +131,7 @@ __device__ __forceinline__ void render_backward_tile(const BackwardView& v, uint
     const uint32_t lane = threadIdx.x & 31u;
 
     const uint32_t px = tile_x * kTile + (threadIdx.x & 15u);
-    const uint32_t py = tile_y * kTile + (threadIdx.x >> 4);
+    const uint32_t py = tile_y * (uint32_t)kTH + (threadIdx.x >> 4);
     bool valid = false;           // pixel contributes vertex gradients (id in [1, T])
     uint3 vi = make_uint3(0, 0, 0);
     float cv[3][kNV];             // per corner contributions
