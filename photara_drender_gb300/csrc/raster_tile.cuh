@@ -317,7 +317,7 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
     // tiles of at most 16 x 8 pixels enumerate per-row spans of the rectangles (row_spans), larger ones
     // the rectangles themselves
     constexpr bool kRowSpans = TW <= 16 && TH <= 8;
-    constexpr uint32_t kSpanMin = 16;
+    constexpr uint32_t kSpanMin = 8;
     __shared__ TileStage<CHUNK> tri;
     // Winner per pixel (row-major in the tile) as a 64-bit key (ordered depth bits << 32 | triangle
     // index): the minimum key is the nearest depth, ties to the lowest id, exactly the reference's
