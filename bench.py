@@ -886,11 +886,10 @@ KERNEL_SOURCES = {
 # bytes per launch); from `ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum`
 # on the full 64-view run (profiles/launch_list_fwdbwd_200k_64x1024sq.md)
 KERNEL_TRAFFIC = {
-    "bin_tiles": ((16, 8, 128), "ed20208abe26a4d1",
-                  108488192 + 67244288 + 2103296 + 11520 + 2103296 + 104388608 + 55637760),
-    "rasterize_forward+shade": ((16, 8, 128), "8e087469c7d9c88e", 2228451840 + 5732461824),
-    # the adjoint kernel and the finishing pass over the per-view vertex records
-    "render_backward": (None, "deb36df30e237d9f", 5652964096 + 1178972928 + 208677632 + 45262336),
+    "bin_tiles": ((16, 8, 128), "ed20208abe26a4d1", 340085248),
+    "rasterize_forward+shade": ((16, 8, 128), "a280d70fc0a17476", 7962652416),
+    # the adjoint kernel (16x8 tiles) and the finishing pass over the per-view vertex records
+    "render_backward": (None, "75c07abc353cd1c9", 7130837760),
 }
 
 
