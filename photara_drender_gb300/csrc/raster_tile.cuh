@@ -4,15 +4,19 @@
 //
 // Per tile: the tile's triangles are staged in shared memory (structure of arrays) CHUNK at a time,
 // each with the rectangle of tile pixels whose samples can pass its edge tests (pixel_rect, a rigorous
-// bound including the reference's 1e-7 tolerance and fp32 rounding). The candidates, the (triangle,
-// pixel) pairs of those rectangles, are then spread over the lanes one pair per lane: each warp owns a
+// bound including the reference's 1e-7 tolerance and fp32 rounding); on 16x8 tiles, rectangles of more
+// than kSpanMin pixels are cut to per-row spans (span_coefficients, row_span, another rigorous bound).
+// The candidates, the (triangle, pixel) pairs of those rectangles or spans, are then spread over the
+// lanes one pair per lane: each warp owns a
 // share of the staged triangles, numbers their candidates with a prefix sum and works through them 32 at
 // a time. A lane runs the reference's edge tests at its candidate's sample and, when they pass, computes
 // the depth with the reference's arithmetic and folds (depth, triangle) into the pixel's winner key with
 // a shared-memory atomicMin. Small triangles have a handful of candidates, so lanes stay busy where a
 // warp-per-region coverage pass would test 32 pixels to find a few. Afterwards each pixel recomputes the
 // winner's barycentrics once. The result does not depend on the order of the tile's triangles: the
-// minimum (depth, id) key is what the reference's sequential depth test keeps.
+// minimum (depth, id) key is what the reference's sequential depth test keeps. Which triangles a tile
+// lists follows the reference's 16x16 binning for every tile shape (bin_rect.cuh triangle_tile_rect), so
+// the (triangle, pixel) pairs tested are the reference's.
 #pragma once
 
 #include <cuda_runtime.h>
