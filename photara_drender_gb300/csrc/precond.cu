@@ -641,7 +641,8 @@ __device__ __forceinline__ float step_multiplier(const float* __restrict__ mult,
     return expf(fminf(fmaxf(mult[t * 4 + (k - t * 3)], -2.0794415f), 2.7725887f));
 }
 
-__global__ void adam_scaled_kernel(float* __restrict__ tex, float* __restrict__ grad, float* __restrict__ m1,
+__global__ void __launch_bounds__(256, 8)  // 32 registers: full occupancy for the streaming update
+adam_scaled_kernel(float* __restrict__ tex, float* __restrict__ grad, float* __restrict__ m1,
                                    float* __restrict__ m2, uint64_t texels, const float* __restrict__ mult,
                                    const uint32_t* __restrict__ fallback, float lr, float b1, float b2, float eps,
                                    float bc1, float bc2, float cmin, float cmax) {
