@@ -94,3 +94,32 @@ def test_binning_argument_checks_without_gpu():
         _native.check(L.pdr_bin_tiles(odd, 1, 3, idx, 1, 32, 32, vps, off, lst, 64, ws, 1 << 30, status, None))
     with pytest.raises(OverflowError, match="capacity"):
         _native.check(L.pdr_bin_tiles(clip, 1, 3, idx, 1, 32, 32, vps, off, lst, 1 << 62, ws, 1 << 30, status, None))
+
+
+def test_render_workspace_queries_without_gpu():
+    """The fused render's workspace queries answer on the host: the backward's per-view vertex records take
+    4 * ceil((attributes + 5) / 4) floats per vertex and view (0 above 8 attributes), the tiled forward query
+    takes only the tile shapes the raster is compiled for, and a shape that does not divide the reference's
+    16x16 tile is refused by the render entry points before any launch."""
+    import ctypes as C
+
+    from photara_drender_gb300 import _native
+    from photara_drender_gb300.pipeline import TILE_CONFIGS, RenderArgsC
+
+    L = _native.lib()
+    for a in range(9):
+        want = 3 * 1000 * 4 * ((a + 5 + 3) // 4) * 4
+        assert L.pdr_render_backward_workspace_bytes(3, 1000, a) == want, a
+    assert L.pdr_render_backward_workspace_bytes(3, 1000, 9) == 0
+    assert L.pdr_render_workspace_bytes_tiled(2, 100, 64, 64, 1024, 0, 8) == 0
+    for tw, th, _ in TILE_CONFIGS:
+        assert L.pdr_render_workspace_bytes_tiled(2, 100, 64, 64, 1024, tw, th) > 0
+    base = 1 << 20
+    a = RenderArgsC()
+    a.clip_positions, a.indices, a.viewports, a.raster = base, base + 4096, base + 8192, base + 12288
+    a.tile_offsets, a.tile_triangles, a.workspace, a.status = base + 16384, base + 20480, base + 24576, base + 28672
+    a.views, a.vertex_count, a.triangle_count, a.width, a.height = 1, 3, 1, 64, 64
+    a.capacity, a.workspace_bytes = 1024, 1 << 30
+    a.tile_width, a.tile_height, a.stage_triangles = 32, 8, 256
+    with pytest.raises(ValueError, match="tile shape"):
+        _native.check(L.pdr_render_bin(C.addressof(a), None))
