@@ -887,7 +887,7 @@ KERNEL_SOURCES = {
 # on the full 64-view run (profiles/launch_list_fwdbwd_200k_64x1024sq.md)
 KERNEL_TRAFFIC = {
     "bin_tiles": ((16, 8, 128), "ed20208abe26a4d1", 340085248),
-    "rasterize_forward+shade": ((16, 8, 128), "11c5943f693e831b", 7962652416),
+    "rasterize_forward+shade": ((16, 8, 128), "55b8bd4c31220dd3", 7962652416),
     # the adjoint kernel (16x8 tiles) and the finishing pass over the per-view vertex records
     "render_backward": (None, "75c07abc353cd1c9", 7130837760),
 }

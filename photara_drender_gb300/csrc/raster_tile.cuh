@@ -318,8 +318,8 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
     static_assert(TW <= 64 && TH <= 64 && kThreads <= 512 && kThreads % 32 == 0,
                   "candidate rectangles pack tile-local coordinates; li * width < 2^16");
     static_assert(CHUNK % 32 == 0 && CHUNK <= kThreads, "a stage holds at most one triangle per thread");
-    // tiles of at most 16 x 8 pixels enumerate per-row spans of the rectangles (row_spans), larger ones
-    // the rectangles themselves
+    // tiles of at most 16 x 8 pixels enumerate per-row spans of their rectangles of more than kSpanMin pixels
+    // (span_coefficients, row_span; 8 measured fastest), larger tiles the rectangles themselves
     constexpr bool kRowSpans = TW <= 16 && TH <= 8;
     constexpr uint32_t kSpanMin = 8;
     __shared__ TileStage<CHUNK> tri;
@@ -392,8 +392,8 @@ __device__ __forceinline__ void raster_tile(const RasterView& v, uint32_t tx, ui
             tri.edge_b[threadIdx.x] = make_float4(s2x, s2y, sgn, __uint_as_float(t));
             tri.rect[threadIdx.x] = rect;
             if constexpr (kRowSpans) {
-                // rectangles of more than kSpanMin pixels (slivers, and triangles the bound declines) are cut
-                // to row spans; smaller ones are enumerated whole
+                // rectangles of more than kSpanMin pixels (the whole tile where the bound declines) are cut to
+                // row spans; smaller ones are enumerated whole
                 uint32_t x0 = 0, x1 = x_end - x_org - 1u, y0 = 0, y1 = y_end - y_org - 1u;
                 if (rect < kRectNone) {
                     x0 = rect & 0xFFu;
